@@ -1,0 +1,66 @@
+"""Extract the reference's own golden vectors for the (MC)SOR/SCF path.
+
+Reads test-sets/<system>/set-NN/{input.data,reference.lst} from an x2dhf
+checkout (default /root/reference) and writes, per case, the input deck and a
+JSON file with every per-iteration orbital-energy line (scf iteration,
+orbital label, orbital energy, energy difference, 1-norm), the final total
+energy and the (MC)SOR sweep count printed by the reference program.
+
+These files are the pins of the CPU oracle (tests/test_oracle_golden.py).
+Run:  python tests/golden/make_golden.py [/path/to/x2dhf]
+"""
+import json
+import os
+import re
+import sys
+
+CASES = {
+    # name: (test-set dir, input override applied by the tests)
+    "h2_set01": "h2/set-01",   # H2 151x211, SOR, frozen-orbital start
+    "he_set01": "he/set-01",   # He 91x121, SOR
+    "he_set02": "he/set-02",   # He 91x121, MCSOR (1 thread)
+    "ne_set01": "ne/set-01",   # Ne 151x181, 4 orbitals incl. 1pi, SOR
+    "h_set04": "h/set-04",     # H 1pi, 131x?, one electron
+}
+
+LINE = re.compile(r"^\s*(\d+)\s+(\d+)\s+(sigma|pi|delta|phi)\s*([gu]?)\s+"
+                  r"(-?\d\.\d+E[+-]\d+)\s+(-?\d\.\d+E[+-]\d+)\s+(-?\d\.\d+E[+-]\d+)")
+
+
+def extract(lst):
+    recs, etot, sweeps = [], None, None
+    for ln in lst.splitlines():
+        m = LINE.match(ln)
+        if m:
+            recs.append([int(m.group(1)), f"{m.group(2)} {m.group(3)} {m.group(4)}".strip(),
+                         float(m.group(5)), float(m.group(6)), float(m.group(7))])
+            continue
+        m = re.match(r"^\s+total energy:\s+(-?\d\.\d+E[+-]\d+)\s*$", ln)
+        if m:
+            etot = float(m.group(1))
+        m = re.search(r"\(MC\)SOR iterations:\s+(\d+)", ln)
+        if m:
+            sweeps = int(m.group(1))
+    return recs, etot, sweeps
+
+
+def main():
+    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    out = os.path.dirname(os.path.abspath(__file__))
+    for name, rel in CASES.items():
+        d = os.path.join(root, "test-sets", rel)
+        with open(os.path.join(d, "input.data")) as f:
+            deck = f.read()
+        with open(os.path.join(d, "reference.lst")) as f:
+            lst = f.read()
+        recs, etot, sweeps = extract(lst)
+        with open(os.path.join(out, name + ".input"), "w") as f:
+            f.write(deck)
+        with open(os.path.join(out, name + ".json"), "w") as f:
+            json.dump({"source": f"test-sets/{rel}/reference.lst", "records": recs,
+                       "total_energy": etot, "sweeps": sweeps}, f, indent=0)
+        print(f"{name}: {len(recs)} records, E={etot}, sweeps={sweeps}")
+
+
+if __name__ == "__main__":
+    main()
