@@ -1,0 +1,229 @@
+/*
+ * x2dhf_gpu.h -- C ABI of the GB300 (sm_103a) relaxation library for x2dhf.
+ *
+ * The library replaces the (MC)SOR relaxation hot path of x2dhf 3.0
+ * (src/sormcsor.F90, src/relaxOrbs.F90, src/relaxPots.F90, src/inout.F90 and
+ * the C backend src/c/*.c) and the Newton-Cotes quadratures the SCF loop
+ * calls between sweeps, with hand-written CUDA kernels on one GPU.
+ *
+ * Two layers are exported:
+ *
+ *  1. Reference-named entry points with the reference's exact C signatures,
+ *     so a PTHREAD build of x2dhf links this library instead of src/c/*.c.
+ *     They read the Fortran COMMON blocks c_interface_*_, c_sorptr_,
+ *     c_supplptr_, c_orbptr_, c_exchptr_, c_i4b_, c_iadex_ (layouts of
+ *     src/c/sorpt.h:58-249), which the library references weakly; without a
+ *     Fortran program that defines them these entry points return without
+ *     touching memory and set x2g_last_status() to X2G_ERR_NO_COMMON.
+ *
+ *  2. Explicit entry points (x2g_*) taking plain pointers and sizes.  They
+ *     return an int status (0 = success, see X2G_ERR_*) and never abort.
+ *
+ * All arrays are FP64, column-major as in the reference: nu (N_nu points) is
+ * the fastest index, mu (N_mu points) the slowest.  "plain" arrays hold
+ * N_nu*N_mu values; "extended" arrays hold (N_nu+8)*(N_mu+8) values with the
+ * function at (nu+4, mu+4) and 4-point ghost margins (src/inout.F90:23-82).
+ */
+#ifndef X2DHF_GPU_H
+#define X2DHF_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* status codes                                                       */
+/* ------------------------------------------------------------------ */
+#define X2G_OK 0
+#define X2G_ERR_ARG 1          /* bad argument (dimension, pointer, range)          */
+#define X2G_ERR_CUDA 2         /* CUDA runtime error (message in x2g_last_error)    */
+#define X2G_ERR_ALLOC 3        /* device allocation failed                          */
+#define X2G_ERR_TIMEOUT 4      /* a device-side barrier wait ran out (no hang)      */
+#define X2G_ERR_NAN 5          /* NaN detected in an orbital or potential           */
+#define X2G_ERR_SCHEDULE 6     /* colour/level schedule failed its host-side check  */
+#define X2G_ERR_NO_COMMON 7    /* reference COMMON blocks not linked                */
+#define X2G_ERR_UNSUPPORTED 8  /* case outside the supported scope (open shells)    */
+#define X2G_ERR_NO_DEVICE 9    /* no CUDA device                                    */
+
+#define X2G_MAXORB 36          /* src/params.h MAXORB */
+
+/* precision forms */
+#define X2G_FP64 0   /* plain: FP64 MCSOR, reference colour order, bit-exact sweeps    */
+#define X2G_MIXED 1  /* FP32 sweeps on CUDA cores + FP64 defect correction per call      */
+
+typedef struct x2g_ctx x2g_ctx;    /* one GPU, one stream, owned device memory */
+typedef struct x2g_grid x2g_grid;  /* prolate-spheroidal grid + operator tables + sweep schedule */
+typedef struct x2g_scf x2g_scf;    /* device-resident SCF state of one molecule */
+
+/* Last status / message of the calling thread (never NULL). */
+int x2g_last_status(void);
+const char *x2g_last_error(void);
+
+/* ------------------------------------------------------------------ */
+/* context                                                            */
+/* ------------------------------------------------------------------ */
+/* Create a context on CUDA device `device` with its own non-blocking stream. */
+int x2g_create(x2g_ctx **ctx, int device);
+int x2g_destroy(x2g_ctx *ctx);
+/* Wait for all work queued on the context's stream. */
+int x2g_synchronize(x2g_ctx *ctx);
+/* The context's cudaStream_t, as an opaque pointer. */
+void *x2g_stream(x2g_ctx *ctx);
+
+/* ------------------------------------------------------------------ */
+/* grid                                                               */
+/* ------------------------------------------------------------------ */
+/* Build the grid, every supplementary array of src/initCBAllocArrays.F90
+ * initSuppl:1636-2051 (b, d, e, f0..f4, g, wgt1, wgt2, Legendre tables),
+ * the "middle" point ordering of mesh:2503-2544 and the colour/level
+ * schedule of the GPU sweep.  nnu, nmu must already satisfy the reference's
+ * n = 1 (mod 30) rounding (x2g_round_grid). */
+int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, double z1, double z2, int mpole,
+                    x2g_grid **grid);
+int x2g_grid_destroy(x2g_grid *grid);
+/* The reference's grid rounding (src/inputInterface.F90:2961-3095). */
+int x2g_round_grid(int n);
+/* Number of mu points the reference derives from nnu and R_inf when the grid
+ * card gives no mu count (nmucalc with n=0, inputInterface.F90:2983-2992). */
+int x2g_nmu_from_rinf(int nnu, double r, double rinf);
+/* Default overrelaxation parameters (setOmega, initCBAllocArrays.F90:636-650,
+ * 1010-1040): omega_pot and omega_orb = (omega_pot-1)*omega_pot - 0.001*max(Z1,Z2). */
+int x2g_default_omega(int nnu, int nmu, double z1, double z2, double *omega_orb, double *omega_pot);
+/* Copy a host table of the grid: which = 0 borb 1 bpot 2 d 3 e 4 f0 5 f1 6 f2
+ * 7 f3 8 f4 9 g 10 wgt1 11 wgt2 (plain, N_nu*N_mu values). */
+int x2g_grid_table(x2g_grid *grid, int which, double *host_out);
+/* Host-only (no CUDA call) copies of the same tables and of the sweep
+ * schedule, for checking the setup without a GPU.  x2g_host_schedule fills
+ * order[k] (extended index, 0-based) with tile[k], colour[k], level[k] of
+ * the k-th scheduled point when tile/colour/level are non-NULL, else the
+ * reference's list order. */
+int x2g_host_table(int nnu, int nmu, double r, double rinf, double z1, double z2, int which, double *out);
+int x2g_host_schedule(int nnu, int nmu, int *npoints, int *ntiles, int *nlevels, int *order, int *tile,
+                      int *colour, int *level);
+/* Schedule statistics: tiles (row bands), colour levels, points per sweep. */
+int x2g_grid_info(x2g_grid *grid, int *nnu, int *nmu, int *ntiles, int *nlevels, int *npoints);
+
+/* ------------------------------------------------------------------ */
+/* relaxation (src/sormcsor.F90 mcsor:143-386)                        */
+/* ------------------------------------------------------------------ */
+/* One function to relax.  All pointers are DEVICE pointers.
+ *   u    extended array, relaxed in place (ghosts are refreshed from the
+ *        interior first, as putin does, src/inout.F90:23-82)
+ *   lhs  plain diagonal term; NULL for a potential: lhs = f3 + idel^2 e
+ *   rhs  plain right-hand side; NULL for a potential: rhs = psa*psb*g
+ *        (relaxPots.F90:81-95) built from psa/psb (extended orbitals)
+ *   kind 0 orbital (b = borb), 1 potential (b = bpot)              */
+typedef struct {
+  double *u;
+  const double *lhs;
+  const double *rhs;
+  const double *psa;
+  const double *psb;
+  double omega;
+  int isym;
+  int idel;
+  int kind;
+  int pad;
+} x2g_job;
+
+/* Relax `njobs` independent functions on the same grid with `nsweeps`
+ * micro-sweeps each, in one persistent cooperative launch on the context's
+ * stream.  `jobs` is a HOST array.  precision: X2G_FP64 or X2G_MIXED. */
+int x2g_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, int nsweeps, int precision);
+
+/* putin / putout on device buffers (src/inout.F90:23-82, 165-183). */
+int x2g_putin(x2g_ctx *ctx, x2g_grid *grid, int isym, const double *fun_plain, double *work_ext);
+int x2g_putout(x2g_ctx *ctx, x2g_grid *grid, const double *work_ext, double *fun_plain);
+
+/* Host-buffer form of one relaxation call, the unit the reference's
+ * mcsor_pthread_ performs (mcsor_pthread.c:32): copies wk2/lhs/rhs to the
+ * device, relaxes, copies wk2 back.  kind as in x2g_job. */
+int x2g_mcsor_host(x2g_ctx *ctx, x2g_grid *grid, int isym, int kind, double omega, int nsweeps,
+                   double *wk2_ext_host, const double *lhs_host, const double *rhs_host);
+
+/* ------------------------------------------------------------------ */
+/* quadratures (src/normOrtho.F90, src/integrals.F90)                  */
+/* ------------------------------------------------------------------ */
+/* sum_i w_i * a_i * b_i * c_i over the plain grid (c may be NULL), with w =
+ * wgt1 (which=1) or wgt2 (which=2); a, b, c are EXTENDED device arrays.
+ * Deterministic two-pass reduction; result written to host *out. */
+int x2g_quadrature(x2g_ctx *ctx, x2g_grid *grid, int which, const double *a_ext, const double *b_ext,
+                   const double *c_ext, double *out);
+
+/* ------------------------------------------------------------------ */
+/* SCF (src/doSCF.F90 prepSCF:24, scf:211, relaxDriver:943)            */
+/* ------------------------------------------------------------------ */
+/* A closed-shell HF case, the fields of the reference's input cards. */
+typedef struct {
+  double z1, z2, r;        /* nuclei card (bohr) */
+  int nnu, nmu;            /* grid card after rounding (x2g_round_grid) */
+  double rinf;             /* practical infinity (bohr) */
+  int norb;                /* config card: orbitals in input order */
+  int m[X2G_MAXORB];       /* |lambda|: 0 sigma 1 pi 2 delta 3 phi */
+  char gu[X2G_MAXORB];     /* 'g', 'u' or ' ' */
+  double occ[X2G_MAXORB];  /* 2 (sigma) or 4 (non-sigma): closed shells only */
+  /* lcao card (hydrogenic start, initHyd initOrbitalsPotentials.F90:714) */
+  double co1[X2G_MAXORB], co2[X2G_MAXORB], za[X2G_MAXORB], zb[X2G_MAXORB];
+  int n1[X2G_MAXORB], l1[X2G_MAXORB], n2[X2G_MAXORB], l2[X2G_MAXORB];
+  /* scf / conv / orbpot cards */
+  int maxscf, ienterm, inoterm, ienterm4init;
+  int nscf2skip, nenlast, nnolast;
+  int maxsor_orb, maxsor_pot;   /* micro sweeps per relaxation (10) */
+  double omega_orb, omega_pot;  /* <= 0: reference default */
+  double recalc_mm;             /* recalcMMfactor (1.15) */
+  int mpole;                    /* multipole terms (4) */
+  int homonuclear;              /* g/u labels given: enforce C_i (setCi) */
+  int precision;                /* X2G_FP64 or X2G_MIXED */
+} x2g_case;
+
+typedef struct {
+  int iterations;          /* SCF iterations performed */
+  int converged;           /* 1 energy threshold, 2 norm threshold, 0 limit/other */
+  long sweeps;             /* (MC)SOR sweeps: nsor4orb + nsor4pot */
+  double total_energy;     /* etot (Eh) */
+  double electronic_energy;
+  double virial;
+  double ee[X2G_MAXORB];   /* orbital energies (diagonal Lagrange multipliers) */
+  double norm_error[X2G_MAXORB];
+} x2g_result;
+
+int x2g_case_defaults(x2g_case *c);
+int x2g_scf_create(x2g_ctx *ctx, const x2g_case *c, x2g_scf **scf);
+int x2g_scf_destroy(x2g_scf *scf);
+/* Run up to max_iterations SCF iterations (prepSCF on the first call).
+ * Returns X2G_OK; result->converged tells why the loop stopped. */
+int x2g_scf_run(x2g_scf *scf, int max_iterations, x2g_result *result);
+/* Copy orbital iorb (1-based, input order) / its Coulomb potential to a host
+ * plain array of N_nu*N_mu values. */
+int x2g_scf_get_orbital(x2g_scf *scf, int iorb, double *host_plain);
+int x2g_scf_get_coulomb(x2g_scf *scf, int iorb, double *host_plain);
+/* Per-iteration record i (0-based): iscf, iorb, ee, delta ee, 1-norm. */
+int x2g_scf_nrecords(x2g_scf *scf);
+int x2g_scf_record(x2g_scf *scf, int i, int *iscf, int *iorb, double *ee, double *dee, double *dnorm);
+/* Device launches of this library's kernels so far on the scf's context. */
+long x2g_kernel_launches(x2g_ctx *ctx);
+
+/* ------------------------------------------------------------------ */
+/* reference-named entry points (link-compatible with src/c/*.c)       */
+/* ------------------------------------------------------------------ */
+/* src/c/mcsor_pthread.c:32 -- relax the orbital held in wk2 (extended),
+ * lhs/rhs plain; nthreads is accepted and ignored (one GPU). */
+void mcsor_pthread_(int *isym, int *nthreads, double *wk2, double *lhs, double *rhs);
+/* src/c/mcsor_tpool.c:135 -- same contract as mcsor_pthread_. */
+void mcsor_tpool_(int *isym, int *nthreads, double *wk2, double *lhs, double *rhs);
+/* src/c/coulExch_pthread.c:19 -- relax every Coulomb/exchange potential of
+ * orbital c_interface_46_.iorbc in one batched launch. */
+void coulExch_pthread_(void);
+/* src/c/coulExch_tpool.c:109 -- same contract as coulExch_pthread_. */
+void coulExch_tpool_(void);
+/* x2dhf.F90:44-55 tpool shutdown hooks: release the GPU context. */
+void tpoolStop4mcsor_(int *nthreads);
+void tpoolStop4pots_(int *nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

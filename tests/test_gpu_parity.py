@@ -1,0 +1,176 @@
+"""GPU parity: the CUDA path against the CPU oracle on the same inputs.
+
+Sweeps are compared bit for bit (the FP64 kernel reproduces the
+single-thread MCSOR order and the reference's unfused arithmetic); SCF
+results within the stated tolerances (reduction order differs)."""
+import numpy as np
+import pytest
+
+import x2dhf_gb300 as xg
+from conftest import golden_deck, golden_json
+from oracle.pyoracle import Case, with_hydrogen0
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = xg.Context(0)
+    yield c
+    c.close()
+
+
+def _all_mcsor(deck):
+    """The GPU relaxes orbitals and potentials with MCSOR; the oracle does the
+    same with the mcsor and mcsor-ce cards."""
+    lines = [ln for ln in deck.splitlines() if not ln.strip().lower().startswith(("mcsor", "stop"))]
+    return "\n".join(lines + ["mcsor", "mcsor-ce", "stop"]) + "\n"
+
+
+def _grid(ctx, deck):
+    c = xg.parse_deck(deck)
+    return c, xg.Grid(ctx, c.nnu, c.nmu, c.r, c.rinf, c.z1, c.z2)
+
+
+ORB_CASES = [("he_set01", 1), ("h2_set01", 1), ("ne_set01", 1), ("ne_set01", 4), ("h_set04", 1)]
+
+
+@pytest.mark.parametrize("name,iorb", ORB_CASES)
+@pytest.mark.parametrize("nsweeps", [1, 10])
+def test_orbital_mcsor_bitexact(ctx, name, iorb, nsweeps):
+    deck = golden_deck(name)
+    oc = Case(deck)
+    c, g = _grid(ctx, deck)
+    f1, f2 = oc.fock(iorb)
+    diag = oc.coeffs()[5]
+    lhs, rhs = f1 + diag, f2.copy()
+    isym = 1 if c.m[iorb - 1] % 2 == 0 else -1
+    uext = oc.putin(isym, oc.orbital(iorb))
+    omega = oc.omega()[0]
+    ref = oc.sweep(1, isym, nsweeps, omega, uext, lhs, rhs, oc.suppl(0), oc.suppl(2))
+    got = xg.mcsor_host(ctx, g, isym, 0, omega, nsweeps, uext.copy(), lhs, rhs)
+    assert np.array_equal(got, ref), np.abs(got - ref).max()
+
+
+@pytest.mark.parametrize("name,iorb", [("he_set01", 1), ("ne_set01", 1), ("ne_set01", 2)])
+def test_potential_mcsor_bitexact(ctx, name, iorb):
+    deck = golden_deck(name)
+    oc = Case(deck)
+    c, g = _grid(ctx, deck)
+    e, f3, gg = oc.suppl(3), oc.suppl(7), oc.suppl(9)
+    for k in range(1, oc.npots(iorb) + 1):
+        in1, in2, idel, isym = oc.pot_info(iorb, k)
+        rhs = (oc.orbital(in1) * oc.orbital(in2)) * gg
+        lhs = f3.copy() if idel == 0 else f3 + float(idel * idel) * e
+        uext = oc.putin(isym, oc.pot(iorb, k))
+        omega = oc.omega()[1]
+        ref = oc.sweep(1, isym, 10, omega, uext, lhs, rhs, oc.suppl(1), oc.suppl(2))
+        got = xg.mcsor_host(ctx, g, isym, 1, omega, 10, uext.copy(), lhs, rhs)
+        assert np.array_equal(got, ref), (k, np.abs(got - ref).max())
+
+
+def test_batched_potentials_from_orbitals_bitexact(ctx):
+    """All potentials of one orbital in one launch, rhs built on the device."""
+    torch = pytest.importorskip("torch")
+    deck = golden_deck("ne_set01")
+    oc = Case(deck)
+    c, g = _grid(ctx, deck)
+    iorb = 1
+    dev = torch.device("cuda:0")
+    orbs = {i: torch.tensor(oc.putin(1 if c.m[i - 1] % 2 == 0 else -1, oc.orbital(i)), device=dev)
+            for i in range(1, oc.norb + 1)}
+    jobs, bufs, refs = [], [], []
+    omega = oc.omega()[1]
+    for k in range(1, oc.npots(iorb) + 1):
+        in1, in2, idel, isym = oc.pot_info(iorb, k)
+        u = torch.tensor(oc.putin(isym, oc.pot(iorb, k)), device=dev)
+        bufs.append(u)
+        jobs.append(xg.Job(u=u.data_ptr(), psa=orbs[in1].data_ptr(), psb=orbs[in2].data_ptr(), omega=omega,
+                           isym=isym, idel=idel, kind=1))
+        oc.relax_pot(iorb, k, 1)
+        refs.append(oc.putin(isym, oc.pot(iorb, k)))
+    torch.cuda.synchronize()
+    xg.relax(ctx, g, jobs, 10)
+    ctx.synchronize()
+    n8 = c.nnu + 8
+    for k, (u, ref) in enumerate(zip(bufs, refs)):
+        got = u.cpu().numpy().reshape(c.nmu + 8, n8)[4:c.nmu + 4, 4:c.nnu + 4]
+        exp = ref.reshape(c.nmu + 8, n8)[4:c.nmu + 4, 4:c.nnu + 4]
+        assert np.array_equal(got, exp), (k, np.abs(got - exp).max())
+
+
+def test_mixed_relaxation_tracks_fp64(ctx):
+    """FP32 sweeps + FP64 defect correction stay within FP32 rounding of the FP64 result."""
+    deck = golden_deck("he_set01")
+    oc = Case(deck)
+    c, g = _grid(ctx, deck)
+    f1, f2 = oc.fock(1)
+    lhs, rhs = f1 + oc.coeffs()[5], f2.copy()
+    uext = oc.putin(1, oc.orbital(1))
+    omega = oc.omega()[0]
+    exact = xg.mcsor_host(ctx, g, 1, 0, omega, 10, uext.copy(), lhs, rhs)
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    u = torch.tensor(uext, device=dev)
+    dl, dr = torch.tensor(lhs, device=dev), torch.tensor(rhs, device=dev)
+    xg.relax(ctx, g, [xg.Job(u=u.data_ptr(), lhs=dl.data_ptr(), rhs=dr.data_ptr(), omega=omega, isym=1, kind=0)],
+             10, xg.MIXED)
+    ctx.synchronize()
+    got = u.cpu().numpy()
+    change = np.abs(exact - uext).max()
+    assert np.abs(got - exact).max() <= 1e-5 * change + 1e-14
+
+
+def _scf_records_match(name, niter, transform=None, tol=1e-11):
+    deck = golden_deck(name)
+    if transform:
+        deck = transform(deck)
+    deck = _all_mcsor(deck)
+    oc = Case(deck)
+    oc.steps(niter)
+    ctx = xg.Context(0)
+    s = xg.SCF(ctx, xg.parse_deck(deck))
+    s.run(niter)
+    ro, rg = oc.records(), s.records()
+    assert len(ro) == len(rg)
+    for a, b in zip(ro, rg):
+        assert a[:2] == b[:2]
+        assert abs(a[2] - b[2]) <= tol * max(1.0, abs(a[2])), (a, b)
+    s.close()
+    ctx.close()
+
+
+def test_scf_he_trajectory_matches_oracle():
+    _scf_records_match("he_set02", 40, with_hydrogen0)
+
+
+def test_scf_h2_trajectory_matches_oracle():
+    _scf_records_match("h2_set01", 40)
+
+
+def test_scf_ne_trajectory_matches_oracle():
+    _scf_records_match("ne_set01", 25)
+
+
+def test_scf_he_converged_energy_vs_golden():
+    """He MCSOR converged to 1e-12: the reference's own final energy."""
+    deck = _all_mcsor(with_hydrogen0(golden_deck("he_set02")))
+    ctx = xg.Context(0)
+    s = xg.SCF(ctx, xg.parse_deck(deck))
+    res = s.run()
+    g = golden_json("he_set02")
+    assert abs(res.total_energy - g["total_energy"]) < 1e-10
+    s.close()
+    ctx.close()
+
+
+def test_scf_he_mixed_converges_to_fp64():
+    deck = _all_mcsor(with_hydrogen0(golden_deck("he_set02")))
+    ctx = xg.Context(0)
+    e = {}
+    for prec in (xg.FP64, xg.MIXED):
+        s = xg.SCF(ctx, xg.parse_deck(deck, precision=prec))
+        e[prec] = s.run().total_energy
+        s.close()
+    assert abs(e[xg.MIXED] - e[xg.FP64]) < 1e-9
+    ctx.close()

@@ -1,0 +1,400 @@
+"""x2dhf_gb300 -- GB300 (sm_103a) relaxation path of x2dhf.
+
+Python host mirror of the reference's operator surface over the C ABI of
+libx2dhf_gpu.so (include/x2dhf_gpu.h):
+
+    parse_deck(text)        input cards -> x2g_case (src/inputInterface.F90)
+    Context(device)         one GPU, one stream
+    Grid(ctx, ...)          grid, operator tables, sweep schedule
+    relax(ctx, grid, jobs)  batched (MC)SOR relaxation of device arrays
+    SCF(ctx, case)          device-resident closed-shell HF SCF (src/doSCF.F90)
+
+The library must be built (x2dhf_gb300.build.build()); there is no CPU
+fallback: every call here runs the CUDA kernels or raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "libx2dhf_gpu.so")
+
+MAXORB = 36
+FP64, MIXED = 0, 1
+_ERRORS = {1: "bad argument", 2: "CUDA error", 3: "allocation failed", 4: "device barrier timeout",
+           5: "NaN detected", 6: "schedule check failed", 7: "COMMON blocks not linked",
+           8: "unsupported case", 9: "no CUDA device"}
+
+
+class X2GError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"x2g error {code} ({_ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class Case(C.Structure):
+    _fields_ = [
+        ("z1", C.c_double), ("z2", C.c_double), ("r", C.c_double),
+        ("nnu", C.c_int), ("nmu", C.c_int), ("rinf", C.c_double),
+        ("norb", C.c_int), ("m", C.c_int * MAXORB), ("gu", C.c_byte * MAXORB), ("occ", C.c_double * MAXORB),
+        ("co1", C.c_double * MAXORB), ("co2", C.c_double * MAXORB),
+        ("za", C.c_double * MAXORB), ("zb", C.c_double * MAXORB),
+        ("n1", C.c_int * MAXORB), ("l1", C.c_int * MAXORB), ("n2", C.c_int * MAXORB), ("l2", C.c_int * MAXORB),
+        ("maxscf", C.c_int), ("ienterm", C.c_int), ("inoterm", C.c_int), ("ienterm4init", C.c_int),
+        ("nscf2skip", C.c_int), ("nenlast", C.c_int), ("nnolast", C.c_int),
+        ("maxsor_orb", C.c_int), ("maxsor_pot", C.c_int),
+        ("omega_orb", C.c_double), ("omega_pot", C.c_double), ("recalc_mm", C.c_double),
+        ("mpole", C.c_int), ("homonuclear", C.c_int), ("precision", C.c_int),
+    ]
+
+
+class Result(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_int), ("converged", C.c_int), ("sweeps", C.c_long),
+        ("total_energy", C.c_double), ("electronic_energy", C.c_double), ("virial", C.c_double),
+        ("ee", C.c_double * MAXORB), ("norm_error", C.c_double * MAXORB),
+    ]
+
+
+class Job(C.Structure):
+    _fields_ = [
+        ("u", C.c_void_p), ("lhs", C.c_void_p), ("rhs", C.c_void_p), ("psa", C.c_void_p), ("psb", C.c_void_p),
+        ("omega", C.c_double), ("isym", C.c_int), ("idel", C.c_int), ("kind", C.c_int), ("pad", C.c_int),
+    ]
+
+
+EXPORTS = [
+    "x2g_last_status", "x2g_last_error", "x2g_create", "x2g_destroy", "x2g_synchronize", "x2g_stream",
+    "x2g_grid_create", "x2g_grid_destroy", "x2g_round_grid", "x2g_nmu_from_rinf", "x2g_default_omega",
+    "x2g_grid_table", "x2g_grid_info", "x2g_relax", "x2g_putin", "x2g_putout", "x2g_mcsor_host",
+    "x2g_quadrature", "x2g_case_defaults", "x2g_scf_create", "x2g_scf_destroy", "x2g_scf_run",
+    "x2g_scf_get_orbital", "x2g_scf_get_coulomb", "x2g_scf_nrecords", "x2g_scf_record",
+    "x2g_kernel_launches", "mcsor_pthread_", "mcsor_tpool_", "coulExch_pthread_", "coulExch_tpool_",
+    "tpoolStop4mcsor_", "tpoolStop4pots_", "x2g_host_table", "x2g_host_schedule",
+]
+
+_lib = None
+
+
+def lib():
+    """Load libx2dhf_gpu.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIBPATH):
+        raise RuntimeError(f"{LIBPATH} missing: run x2dhf_gb300.build.build() (no CPU fallback exists)")
+    L = C.CDLL(LIBPATH)
+    P, I, D = C.c_void_p, C.c_int, C.c_double
+    PP = C.POINTER(C.c_void_p)
+    dp = C.POINTER(C.c_double)
+    L.x2g_last_status.restype = I
+    L.x2g_last_error.restype = C.c_char_p
+    L.x2g_create.argtypes = [PP, I]
+    L.x2g_destroy.argtypes = [P]
+    L.x2g_synchronize.argtypes = [P]
+    L.x2g_stream.restype = P
+    L.x2g_stream.argtypes = [P]
+    L.x2g_grid_create.argtypes = [P, I, I, D, D, D, D, I, PP]
+    L.x2g_grid_destroy.argtypes = [P]
+    L.x2g_round_grid.argtypes = [I]
+    L.x2g_nmu_from_rinf.argtypes = [I, D, D]
+    L.x2g_default_omega.argtypes = [I, I, D, D, dp, dp]
+    L.x2g_grid_table.argtypes = [P, I, dp]
+    L.x2g_grid_info.argtypes = [P] + [C.POINTER(C.c_int)] * 5
+    L.x2g_relax.argtypes = [P, P, C.POINTER(Job), I, I, I]
+    L.x2g_putin.argtypes = [P, P, I, P, P]
+    L.x2g_putout.argtypes = [P, P, P, P]
+    L.x2g_mcsor_host.argtypes = [P, P, I, I, D, I, dp, dp, dp]
+    L.x2g_quadrature.argtypes = [P, P, I, P, P, P, dp]
+    L.x2g_case_defaults.argtypes = [C.POINTER(Case)]
+    L.x2g_scf_create.argtypes = [P, C.POINTER(Case), PP]
+    L.x2g_scf_destroy.argtypes = [P]
+    L.x2g_scf_run.argtypes = [P, I, C.POINTER(Result)]
+    L.x2g_scf_get_orbital.argtypes = [P, I, dp]
+    L.x2g_scf_get_coulomb.argtypes = [P, I, dp]
+    L.x2g_scf_nrecords.argtypes = [P]
+    L.x2g_scf_record.argtypes = [P, I, C.POINTER(C.c_int), C.POINTER(C.c_int), dp, dp, dp]
+    L.x2g_host_table.argtypes = [I, I, D, D, D, D, I, dp]
+    ip = C.POINTER(C.c_int)
+    L.x2g_host_schedule.argtypes = [I, I, ip, ip, ip, ip, ip, ip, ip]
+    L.x2g_kernel_launches.restype = C.c_long
+    L.x2g_kernel_launches.argtypes = [P]
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        L = lib()
+        raise X2GError(rc, L.x2g_last_error().decode())
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+# ---------------------------------------------------------------------------
+# input cards (src/inputInterface.F90:681-818, HF subset)
+# ---------------------------------------------------------------------------
+def round_grid(n):
+    """nnucalc/nmucalc rounding: n = 1 (mod 6) and n - 6 = 0 (mod 5), rounding down."""
+    return lib().x2g_round_grid(int(n))
+
+
+def parse_deck(text, precision=FP64):
+    """Parse a reference input deck into an x2g_case (closed-shell HF)."""
+    L = lib()
+    c = Case()
+    L.x2g_case_defaults(C.byref(c))
+    c.precision = precision
+    lines = [ln.split("!")[0].replace(",", " ").split() for ln in text.splitlines()]
+    lines = [[t.lower() for t in ln] for ln in lines if ln]
+    i = 0
+    grid = None
+    norb = 0
+    hydrogen = False
+
+    def nums(tok):
+        out = []
+        for t in tok:
+            try:
+                out.append(float(t.replace("d", "e")))
+            except ValueError:
+                break
+        return out
+
+    while i < len(lines):
+        ln = lines[i]
+        lab = ln[0][:8]
+        i += 1
+        if lab == "nuclei":
+            v = nums(ln[1:])
+            c.z1, c.z2, c.r = v[0], v[1], v[2]
+            if len(ln) > 4 and ln[4] == "angstrom":
+                c.r = c.r / 0.52917721067121204
+        elif lab == "method":
+            if ln[1] != "hf":
+                raise ValueError("only method hf is supported")
+        elif lab == "config":
+            while True:
+                card = lines[i]
+                i += 1
+                nb = int(card[0])
+                sym = card[1]
+                mt = {"sigma": 0, "pi": 1, "delta": 2, "phi": 3}[sym]
+                rest = card[2:]
+                gu = " "
+                if rest and rest[0] in ("g", "u"):
+                    gu = rest[0]
+                    c.homonuclear = 1
+                    rest = rest[1:]
+                spins = [t for t in rest if t != "end"]
+                if spins and spins[0][0] in "+-.":
+                    raise ValueError("open-shell configurations are not supported")
+                for _ in range(nb):
+                    c.m[norb] = mt
+                    c.gu[norb] = ord(gu)
+                    c.occ[norb] = 2.0 if mt == 0 else 4.0
+                    norb += 1
+                if "end" in rest:
+                    break
+            c.norb = norb
+            for k in range(norb):
+                c.co1[k] = 1.0 if c.z1 > 2.2e-16 else 0.0
+                c.co2[k] = 1.0 if c.z2 > 2.2e-16 else 0.0
+        elif lab == "grid":
+            grid = ln[1:]
+        elif lab == "orbpot":
+            if ln[1] != "hydrogen":
+                raise ValueError("only orbpot hydrogen is supported")
+            hydrogen = True
+            v = nums(ln[2:])
+            if v:
+                c.ienterm4init = int(v[0])
+        elif lab == "lcao":
+            v = nums(ln[1:])
+            inclorb = int(v[0]) if v else 1
+            for k in range(norb):
+                a = lines[i]
+                i += 1
+                c.co1[k], c.n1[k], c.l1[k], c.za[k] = float(a[0]), int(a[1]), int(a[2]), float(a[3])
+                c.co2[k], c.n2[k], c.l2[k], c.zb[k] = float(a[4]), int(a[5]), int(a[6]), float(a[7])
+                if inclorb == 2:
+                    c.za[k] = c.z1 - c.za[k]
+                    c.zb[k] = c.z2 - c.zb[k]
+        elif lab == "scf":
+            v = [int(x) for x in nums(ln[1:])]
+            for name, x in zip(("maxscf", "saveScfData", "ienterm", "inoterm", "verbose"), v):
+                if hasattr(c, name):
+                    setattr(c, name, x)
+        elif lab == "conv":
+            v = [int(x) for x in nums(ln[1:])]
+            for name, x in zip(("nscf2skip", "nenlast", "nnolast"), v):
+                setattr(c, name, x)
+        elif lab in ("mcsor", "mcsor-o"):
+            v = [int(x) for x in nums(ln[1:])]
+            if len(v) > 1:
+                c.maxsor_orb = v[1]
+            if lab == "mcsor" and len(v) > 2:
+                c.maxsor_pot = v[2]
+        elif lab == "omega":
+            v = nums(ln[1:])
+            if v and abs(v[0]) > 0:
+                c.omega_orb = v[0]
+            if len(v) > 1 and abs(v[1]) > 0:
+                c.omega_pot = v[1]
+        elif lab == "multipol":
+            v = nums(ln[1:])
+            c.recalc_mm = v[0] if v and v[0] > 2.2e-16 else 1e15
+            if len(v) > 1:
+                c.mpole = int(v[1])
+        elif lab == "stop":
+            break
+    if grid is None or norb == 0 or not hydrogen:
+        raise ValueError("deck needs nuclei, config, grid, orbpot hydrogen and lcao cards")
+    # lcao coefficients normalised |c1|+|c2| = 1 (read_lcao, read_stop)
+    for k in range(norb):
+        s = abs(c.co1[k]) + abs(c.co2[k])
+        if s > 2.2e-16:
+            c.co1[k] /= s
+            c.co2[k] /= s
+    g = nums(grid)
+    c.nnu = round_grid(int(g[0]))
+    if len(g) >= 3 and abs(g[2]) > 0:
+        c.nmu = round_grid(int(round(g[1])))
+        c.rinf = g[2]
+    else:
+        c.rinf = g[1]
+        c.nmu = lib().x2g_nmu_from_rinf(c.nnu, c.r, c.rinf)
+    return c
+
+
+def host_table(nnu, nmu, r, rinf, z1, z2, which):
+    """Operator table built by the library's host setup (no GPU needed)."""
+    out = np.zeros(nnu * nmu)
+    _check(lib().x2g_host_table(nnu, nmu, r, rinf, z1, z2, which, _dp(out)))
+    return out
+
+
+def host_schedule(nnu, nmu):
+    """(order, tile, colour, level) of every scheduled interior point (no GPU needed)."""
+    L = lib()
+    n, t, l = C.c_int(), C.c_int(), C.c_int()
+    _check(L.x2g_host_schedule(nnu, nmu, C.byref(n), C.byref(t), C.byref(l), None, None, None, None))
+    arrs = [np.zeros(n.value, np.int32) for _ in range(4)]
+    ip = [a.ctypes.data_as(C.POINTER(C.c_int)) for a in arrs]
+    _check(L.x2g_host_schedule(nnu, nmu, C.byref(n), C.byref(t), C.byref(l), *ip))
+    list_order = np.zeros(n.value, np.int32)
+    _check(L.x2g_host_schedule(nnu, nmu, C.byref(n), C.byref(t), C.byref(l),
+                               list_order.ctypes.data_as(C.POINTER(C.c_int)), None, None, None))
+    return list_order, arrs[0], arrs[1], arrs[2], arrs[3]
+
+
+# ---------------------------------------------------------------------------
+# objects
+# ---------------------------------------------------------------------------
+class Context:
+    def __init__(self, device=0):
+        self.L = lib()
+        h = C.c_void_p()
+        _check(self.L.x2g_create(C.byref(h), device))
+        self.h = h
+
+    def synchronize(self):
+        _check(self.L.x2g_synchronize(self.h))
+
+    @property
+    def launches(self):
+        return self.L.x2g_kernel_launches(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.x2g_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Grid:
+    def __init__(self, ctx, nnu, nmu, r, rinf, z1=1.0, z2=1.0, mpole=4):
+        self.ctx = ctx
+        self.L = lib()
+        h = C.c_void_p()
+        _check(self.L.x2g_grid_create(ctx.h, nnu, nmu, r, rinf, z1, z2, mpole, C.byref(h)))
+        self.h = h
+        self.nnu, self.nmu = nnu, nmu
+
+    def info(self):
+        v = [C.c_int() for _ in range(5)]
+        _check(self.L.x2g_grid_info(self.h, *[C.byref(x) for x in v]))
+        return dict(zip(("nnu", "nmu", "ntiles", "nlevels", "npoints"), [x.value for x in v]))
+
+    def table(self, which):
+        out = np.zeros(self.nnu * self.nmu)
+        _check(self.L.x2g_grid_table(self.h, which, _dp(out)))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.x2g_grid_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+
+def relax(ctx, grid, jobs, nsweeps, precision=FP64):
+    """Relax a list of Job structures (device pointers) in one launch."""
+    arr = (Job * len(jobs))(*jobs)
+    _check(lib().x2g_relax(ctx.h, grid.h, arr, len(jobs), nsweeps, precision))
+
+
+def mcsor_host(ctx, grid, isym, kind, omega, nsweeps, wk2, lhs, rhs):
+    """One relaxation call on host arrays (wk2 extended, relaxed in place)."""
+    _check(lib().x2g_mcsor_host(ctx.h, grid.h, isym, kind, omega, nsweeps, _dp(wk2), _dp(lhs), _dp(rhs)))
+    return wk2
+
+
+class SCF:
+    def __init__(self, ctx, case):
+        self.ctx = ctx
+        self.L = lib()
+        h = C.c_void_p()
+        _check(self.L.x2g_scf_create(ctx.h, C.byref(case), C.byref(h)))
+        self.h = h
+        self.case = case
+
+    def run(self, max_iterations=1 << 30):
+        res = Result()
+        _check(self.L.x2g_scf_run(self.h, max_iterations, C.byref(res)))
+        return res
+
+    def records(self):
+        n = self.L.x2g_scf_nrecords(self.h)
+        out = []
+        a, b = C.c_int(), C.c_int()
+        x, y, z = C.c_double(), C.c_double(), C.c_double()
+        for i in range(n):
+            _check(self.L.x2g_scf_record(self.h, i, C.byref(a), C.byref(b), C.byref(x), C.byref(y), C.byref(z)))
+            out.append((a.value, b.value, x.value, y.value, z.value))
+        return out
+
+    def orbital(self, iorb):
+        out = np.zeros(self.case.nnu * self.case.nmu)
+        _check(self.L.x2g_scf_get_orbital(self.h, iorb, _dp(out)))
+        return out
+
+    def coulomb(self, iorb):
+        out = np.zeros(self.case.nnu * self.case.nmu)
+        _check(self.L.x2g_scf_get_coulomb(self.h, iorb, _dp(out)))
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.x2g_scf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

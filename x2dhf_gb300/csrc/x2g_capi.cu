@@ -1,0 +1,350 @@
+// C ABI of the x2dhf GB300 library: context, grid, relaxation, quadrature
+// entry points and the reference-named link-compatible symbols.
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "x2g_kernels.cuh"
+
+namespace {
+thread_local int g_status = 0;
+thread_local std::string g_msg;
+}  // namespace
+
+namespace x2g {
+
+int set_status(int code, const std::string &msg) {
+  g_status = code;
+  g_msg = msg;
+  return code;
+}
+
+int cuda_status(cudaError_t e, const char *where) {
+  std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+  (void)cudaGetLastError();
+  return set_status(X2G_ERR_CUDA, m);
+}
+
+void *ctx_workspace(x2g_ctx *ctx, size_t bytes) {
+  if (ctx->work_bytes < bytes) {
+    if (ctx->work) {
+      cudaStreamSynchronize(ctx->stream);
+      cudaFree(ctx->work);
+    }
+    ctx->work = nullptr;
+    ctx->work_bytes = 0;
+    size_t want = bytes + bytes / 4;
+    if (cudaMalloc(&ctx->work, want) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return nullptr;
+    }
+    ctx->work_bytes = want;
+  }
+  return ctx->work;
+}
+
+}  // namespace x2g
+
+using namespace x2g;
+
+extern "C" {
+
+int x2g_last_status(void) { return g_status; }
+const char *x2g_last_error(void) { return g_msg.c_str(); }
+
+int x2g_create(x2g_ctx **out, int device) {
+  if (!out) return set_status(X2G_ERR_ARG, "null context pointer");
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    (void)cudaGetLastError();
+    return set_status(X2G_ERR_NO_DEVICE, "no CUDA device available");
+  }
+  if (device < 0 || device >= ndev) return set_status(X2G_ERR_ARG, "device index out of range");
+  if ((e = cudaSetDevice(device)) != cudaSuccess) return cuda_status(e, "cudaSetDevice");
+  auto *c = new x2g_ctx();
+  c->device = device;
+  cudaDeviceProp prop;
+  if ((e = cudaGetDeviceProperties(&prop, device)) != cudaSuccess) {
+    delete c;
+    return cuda_status(e, "cudaGetDeviceProperties");
+  }
+  if (!prop.cooperativeLaunch) {
+    delete c;
+    return set_status(X2G_ERR_UNSUPPORTED, "device lacks cooperative launch");
+  }
+  c->num_sms = prop.multiProcessorCount;
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    delete c;
+    return cuda_status(e, "cudaStreamCreate");
+  }
+  if ((e = cudaMalloc(&c->bar, 4 * sizeof(unsigned))) != cudaSuccess ||
+      (e = cudaMemset(c->bar, 0, 4 * sizeof(unsigned))) != cudaSuccess) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return cuda_status(e, "barrier allocation");
+  }
+  c->red_bytes = size_t(160) * 16 * sizeof(double) + 64 * sizeof(double);
+  if ((e = cudaMalloc(&c->red, c->red_bytes)) != cudaSuccess ||
+      (e = cudaMallocHost(&c->host_red, 1024 * sizeof(double))) != cudaSuccess) {
+    cudaFree(c->bar);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return cuda_status(e, "reduction buffers");
+  }
+  *out = c;
+  return set_status(X2G_OK, "");
+}
+
+int x2g_destroy(x2g_ctx *c) {
+  if (!c) return X2G_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  if (c->work) cudaFree(c->work);
+  if (c->red) cudaFree(c->red);
+  if (c->bar) cudaFree(c->bar);
+  if (c->host_red) cudaFreeHost(c->host_red);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return X2G_OK;
+}
+
+int x2g_synchronize(x2g_ctx *c) {
+  if (!c) return set_status(X2G_ERR_ARG, "null context");
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_status(e, "stream synchronize");
+  int err = 0;
+  e = cudaMemcpy(&err, c->bar + 2, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_status(e, "error word readback");
+  if (err) {
+    cudaMemset(c->bar, 0, 4 * sizeof(unsigned));
+    return set_status(err, "device-side barrier wait timed out (kernel returned early)");
+  }
+  return X2G_OK;
+}
+
+void *x2g_stream(x2g_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+long x2g_kernel_launches(x2g_ctx *c) { return c ? c->launches : 0; }
+
+int x2g_round_grid(int n) {
+  // nnucalc/nmucalc (inputInterface.F90:2961-3095): n = 1 (mod 6) and
+  // n - 6 = 0 (mod 5) enforced alternately, always rounding down.
+  if (n < 7) return 0;
+  for (;;) {
+    while ((n - 1) % 6 != 0) n--;
+    int nt = n;
+    while (((n - 6) / 5) * 5 != n - 6) n--;
+    if (n > 1 && n != nt) continue;
+    return n;
+  }
+}
+
+int x2g_nmu_from_rinf(int nnu, double r, double rinf) {
+  double hnu = kPi / double(nnu - 1);
+  double x = 2.0 * rinf / r;
+  x = std::log(x + std::sqrt(x * x - 1.0));
+  long n = lround(x / hnu + 1.0);
+  return x2g_round_grid(int(n));
+}
+
+int x2g_default_omega(int nnu, int nmu, double z1, double z2, double *oorb, double *opot) {
+  double rho = 0.5 * (std::cos(kPi / double(nmu)) + std::cos(kPi / double(nnu)));
+  double w = 2.0 * 0.603 / (1.0 + std::sqrt(1.0 - rho * rho)) + 0.79;
+  if (opot) *opot = w;
+  if (oorb) *oorb = (w - 1.0) * w - 0.001 * (z1 > z2 ? z1 : z2);
+  return X2G_OK;
+}
+
+static int upload(x2g_grid *gr, const void *src, size_t bytes, const void **dst) {
+  void *p = nullptr;
+  cudaError_t e = cudaMalloc(&p, bytes < 16 ? 16 : bytes);
+  if (e != cudaSuccess) return cuda_status(e, "grid table allocation");
+  gr->allocs.push_back(p);
+  e = cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_status(e, "grid table upload");
+  *dst = p;
+  return X2G_OK;
+}
+
+int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, double z1, double z2, int mpole,
+                    x2g_grid **out) {
+  if (!ctx || !out) return set_status(X2G_ERR_ARG, "null argument");
+  *out = nullptr;
+  auto *gr = new x2g_grid();
+  gr->ctx = ctx;
+  std::string msg = build_host_grid(gr->h, nnu, nmu, r, rinf, z1, z2, mpole);
+  if (!msg.empty()) {
+    delete gr;
+    return set_status(msg.rfind("schedule", 0) == 0 ? X2G_ERR_SCHEDULE : X2G_ERR_ARG, msg);
+  }
+  cudaSetDevice(ctx->device);
+  const HostGrid &h = gr->h;
+  GridDev &d = gr->d;
+  d.nni = h.nni;
+  d.nmu = h.nmu;
+  d.n8 = h.n8;
+  d.m8 = h.m8;
+  d.next = h.next;
+  d.mxsize = h.mxsize;
+  d.ntiles = h.ntiles;
+  d.nlev = h.nlev;
+  d.mpole = h.mpole;
+  d.r2 = h.r2;
+  std::memcpy(d.dmu1, h.dmu1, sizeof d.dmu1);
+  std::memcpy(d.dmu2, h.dmu2, sizeof d.dmu2);
+  std::memcpy(d.dni1, h.dni1, sizeof d.dni1);
+  std::memcpy(d.dni2, h.dni2, sizeof d.dni2);
+  std::memcpy(d.exeven, h.exeven, sizeof d.exeven);
+  d.diag = h.diag;
+  std::vector<float> b32(h.borb_mu.begin(), h.borb_mu.end()), p32(h.bpot_mu.begin(), h.bpot_mu.end()),
+      d32(h.d_nu.begin(), h.d_nu.end());
+  const void *tmp;
+  int rc = X2G_OK;
+#define UP(vec, field)                                                                  \
+  do {                                                                                  \
+    if ((rc = upload(gr, vec.data(), vec.size() * sizeof(vec[0]), &tmp)) != X2G_OK) { \
+      x2g_grid_destroy(gr);                                                             \
+      return rc;                                                                        \
+    }                                                                                   \
+    d.field = static_cast<decltype(d.field)>(tmp);                                     \
+  } while (0)
+  UP(h.borb_mu, borb_mu);
+  UP(h.bpot_mu, bpot_mu);
+  UP(h.f3_mu, f3_mu);
+  UP(h.d_nu, d_nu);
+  UP(h.e, e);
+  UP(h.f0, f0);
+  UP(h.f1, f1);
+  UP(h.f2, f2);
+  UP(h.f4, f4);
+  UP(h.g, g);
+  UP(h.wgt1, wgt1);
+  UP(h.wgt2, wgt2);
+  UP(h.leg, leg);
+  UP(h.dmu9, dmu9);
+  UP(h.dni9, dni9);
+  UP(h.vxi, vxi);
+  UP(h.vxisq, vxisq);
+  UP(h.veta, veta);
+  UP(h.vetasq, vetasq);
+  UP(h.tile_row0, tile_row0);
+  UP(h.tile_row1, tile_row1);
+  UP(h.pts, pts);
+  UP(h.off, off);
+  UP(b32, borb_mu32);
+  UP(p32, bpot_mu32);
+  UP(d32, d_nu32);
+#undef UP
+  *out = gr;
+  return set_status(X2G_OK, "");
+}
+
+int x2g_grid_destroy(x2g_grid *gr) {
+  if (!gr) return X2G_OK;
+  if (gr->ctx) cudaStreamSynchronize(gr->ctx->stream);
+  for (void *p : gr->allocs) cudaFree(p);
+  delete gr;
+  return X2G_OK;
+}
+
+int x2g_grid_table(x2g_grid *gr, int which, double *out) {
+  if (!gr || !out) return set_status(X2G_ERR_ARG, "null argument");
+  const HostGrid &h = gr->h;
+  const int nni = h.nni, nmu = h.nmu;
+  for (int i = 0; i < nmu; ++i)
+    for (int j = 0; j < nni; ++j) {
+      const int k = i * nni + j;
+      double v;
+      switch (which) {
+        case 0: v = h.borb_mu[i]; break;
+        case 1: v = h.bpot_mu[i]; break;
+        case 2: v = h.d_nu[j]; break;
+        case 3: v = h.e[k]; break;
+        case 4: v = h.f0[k]; break;
+        case 5: v = h.f1[k]; break;
+        case 6: v = h.f2[k]; break;
+        case 7: v = h.f3_mu[i]; break;
+        case 8: v = h.f4[k]; break;
+        case 9: v = h.g[k]; break;
+        case 10: v = h.wgt1[k]; break;
+        case 11: v = h.wgt2[k]; break;
+        default: return set_status(X2G_ERR_ARG, "unknown table");
+      }
+      out[k] = v;
+    }
+  return X2G_OK;
+}
+
+int x2g_grid_info(x2g_grid *gr, int *nnu, int *nmu, int *ntiles, int *nlevels, int *npoints) {
+  if (!gr) return set_status(X2G_ERR_ARG, "null grid");
+  if (nnu) *nnu = gr->h.nni;
+  if (nmu) *nmu = gr->h.nmu;
+  if (ntiles) *ntiles = gr->h.ntiles;
+  if (nlevels) *nlevels = gr->h.nlev;
+  if (npoints) *npoints = int(gr->h.order.size());
+  return X2G_OK;
+}
+
+int x2g_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, int nsweeps, int precision) {
+  if (!ctx || !grid || (!jobs && njobs > 0) || njobs < 0) return set_status(X2G_ERR_ARG, "null argument");
+  if (precision != X2G_FP64 && precision != X2G_MIXED) return set_status(X2G_ERR_ARG, "unknown precision");
+  return launch_relax(ctx, grid, jobs, njobs, nsweeps, precision);
+}
+
+int x2g_putin(x2g_ctx *ctx, x2g_grid *grid, int isym, const double *fun, double *work) {
+  if (!ctx || !grid || !fun || !work || (isym != 1 && isym != -1)) return set_status(X2G_ERR_ARG, "bad argument");
+  launch_putin(ctx, grid->d, isym, fun, work);
+  return X2G_OK;
+}
+
+int x2g_putout(x2g_ctx *ctx, x2g_grid *grid, const double *work, double *fun) {
+  if (!ctx || !grid || !fun || !work) return set_status(X2G_ERR_ARG, "bad argument");
+  launch_putout(ctx, grid->d, work, fun);
+  return X2G_OK;
+}
+
+int x2g_mcsor_host(x2g_ctx *ctx, x2g_grid *grid, int isym, int kind, double omega, int nsweeps, double *wk2,
+                   const double *lhs, const double *rhs) {
+  if (!ctx || !grid || !wk2 || !lhs || !rhs) return set_status(X2G_ERR_ARG, "null argument");
+  if (kind != 0 && kind != 1) return set_status(X2G_ERR_ARG, "kind must be 0 or 1");
+  const GridDev &g = grid->d;
+  const size_t eb = size_t(g.next) * sizeof(double), pb = size_t(g.mxsize) * sizeof(double);
+  double *buf = nullptr;
+  cudaError_t e = cudaMallocAsync(&buf, eb + 2 * pb, ctx->stream);
+  if (e != cudaSuccess) return cuda_status(e, "mcsor buffers");
+  double *du = buf, *dl = buf + g.next, *dr = dl + g.mxsize;
+  cudaMemcpyAsync(du, wk2, eb, cudaMemcpyHostToDevice, ctx->stream);
+  cudaMemcpyAsync(dl, lhs, pb, cudaMemcpyHostToDevice, ctx->stream);
+  cudaMemcpyAsync(dr, rhs, pb, cudaMemcpyHostToDevice, ctx->stream);
+  x2g_job j{};
+  j.u = du;
+  j.lhs = dl;
+  j.rhs = dr;
+  j.omega = omega;
+  j.isym = isym;
+  j.kind = kind;
+  int rc = launch_relax(ctx, grid, &j, 1, nsweeps, X2G_FP64);
+  cudaMemcpyAsync(wk2, du, eb, cudaMemcpyDeviceToHost, ctx->stream);
+  cudaFreeAsync(buf, ctx->stream);
+  int s = x2g_synchronize(ctx);
+  return rc != X2G_OK ? rc : s;
+}
+
+int x2g_quadrature(x2g_ctx *ctx, x2g_grid *grid, int which, const double *a, const double *b, const double *c,
+                   double *out) {
+  if (!ctx || !grid || !a || !b || !out || (which != 2)) return set_status(X2G_ERR_ARG, "bad argument");
+  TripleItem it{a, b, c};
+  double *dout = static_cast<double *>(ctx->red) + size_t(160) * 16;
+  launch_triples(ctx, grid->d, &it, 1, dout);
+  cudaError_t e = cudaMemcpyAsync(ctx->host_red, dout, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e != cudaSuccess) return cuda_status(e, "quadrature readback");
+  int s = x2g_synchronize(ctx);
+  if (s != X2G_OK) return s;
+  *out = ctx->host_red[0];
+  return X2G_OK;
+}
+
+}  // extern "C"

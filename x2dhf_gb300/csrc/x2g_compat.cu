@@ -1,0 +1,220 @@
+// Reference-named, link-compatible entry points (src/c/mcsor_pthread.c:32,
+// src/c/coulExch_pthread.c:19, src/c/mcsor_tpool.c:135,
+// src/c/coulExch_tpool.c:109).  They read the Fortran COMMON blocks whose C
+// layouts are given in src/c/sorpt.h:58-249; the blocks are referenced
+// weakly so the library also loads in programs without them.
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "x2g_kernels.cuh"
+
+#define MAXORB X2G_MAXORB
+#define MAXTHREADS4MCSOR 16
+
+extern "C" {
+struct x2g_cb1 { int v[2 * MAXORB][MAXORB]; };
+struct x2g_cb7 { int i1bc[MAXORB]; };
+struct x2g_cb8 { int nexchpotsc[MAXORB]; int maxpotsc; };
+struct x2g_cb17 {
+  int mxnmuc, mxsizec, ngrd6ac, ngrd6bc, ngrd7c, nnu1c, nnu2c, nnu3c, nnu4c, nnu5c, isstartc, isstopc, maxsor1c,
+      maxsor2c;
+};
+struct x2g_cb4d { double v[4]; };
+struct x2g_cb5d { double v[5]; };
+struct x2g_cb45 { double omegac, omega1c; };
+struct x2g_cb46 { int iorbc, isymc, nthreadsc; };
+struct x2g_cbptrd { double *p; };
+struct x2g_cbptri { int *p; };
+struct x2g_cbi4b { int i4barr[20]; };
+
+extern struct x2g_cb1 c_interface_1_ __attribute__((weak));   // ins1
+extern struct x2g_cb1 c_interface_2_ __attribute__((weak));   // ins2
+extern struct x2g_cb1 c_interface_3_ __attribute__((weak));   // ibexcpc
+extern struct x2g_cb1 c_interface_4_ __attribute__((weak));   // deltam4potc
+extern struct x2g_cb1 c_interface_6_ __attribute__((weak));   // isymsc
+extern struct x2g_cb7 c_interface_7_ __attribute__((weak));   // i1bc
+extern struct x2g_cb8 c_interface_8_ __attribute__((weak));   // nexchpotsc
+extern struct x2g_cb17 c_interface_17_ __attribute__((weak));
+extern struct x2g_cb4d c_interface_40_ __attribute__((weak));  // dmu1
+extern struct x2g_cb4d c_interface_41_ __attribute__((weak));  // dmu2
+extern struct x2g_cb4d c_interface_42_ __attribute__((weak));  // dnu1
+extern struct x2g_cb4d c_interface_43_ __attribute__((weak));  // dnu2
+extern struct x2g_cb5d c_interface_44_ __attribute__((weak));  // exeven
+extern struct x2g_cb45 c_interface_45_ __attribute__((weak));
+extern struct x2g_cb46 c_interface_46_ __attribute__((weak));
+extern struct x2g_cbptrd c_orbptr_ __attribute__((weak));
+extern struct x2g_cbptrd c_exchptr_ __attribute__((weak));
+extern struct x2g_cbptrd c_supplptr_ __attribute__((weak));
+extern struct x2g_cbi4b c_i4b_ __attribute__((weak));
+}
+
+using namespace x2g;
+
+namespace {
+
+std::mutex g_mu;
+x2g_ctx *g_ctx = nullptr;
+x2g_grid *g_grid = nullptr;
+int g_nni = 0, g_nmu = 0;
+
+bool have_common() {
+  return &c_interface_17_ && &c_interface_40_ && &c_interface_41_ && &c_interface_42_ && &c_interface_43_ &&
+         &c_interface_44_ && &c_interface_45_ && &c_supplptr_ && &c_i4b_;
+}
+
+// Grid for the COMMON-block dimensions; operator coefficients and the
+// b/d tables are taken from the Fortran program's own arrays.
+int ensure_grid() {
+  const int nni = c_interface_17_.nnu1c - 8, nmu = c_interface_17_.mxnmuc;
+  if (!g_ctx) {
+    int rc = x2g_create(&g_ctx, 0);
+    if (rc) return rc;
+  }
+  if (g_grid && g_nni == nni && g_nmu == nmu) goto apply_common;
+  if (g_grid) x2g_grid_destroy(g_grid);
+  g_grid = nullptr;
+  {
+    // a nominal geometry only fills tables that the sweep then overrides
+    int rc = x2g_grid_create(g_ctx, nni, nmu, 1.0, 40.0, 1.0, 1.0, 4, &g_grid);
+    if (rc) return rc;
+  }
+  g_nni = nni;
+  g_nmu = nmu;
+apply_common : {
+  GridDev &d = g_grid->d;
+  std::memcpy(d.dmu1, c_interface_40_.v, sizeof d.dmu1);
+  std::memcpy(d.dmu2, c_interface_41_.v, sizeof d.dmu2);
+  std::memcpy(d.dni1, c_interface_42_.v, sizeof d.dni1);
+  std::memcpy(d.dni2, c_interface_43_.v, sizeof d.dni2);
+  std::memcpy(d.exeven, c_interface_44_.v, sizeof d.exeven);
+  const double *sup = c_supplptr_.p;
+  const int *i4 = c_i4b_.i4barr;
+  std::vector<double> borb(nmu), bpot(nmu), dnu(nni);
+  for (int i = 0; i < nmu; i++) {
+    borb[i] = sup[i4[0] - 1 + i * nni];
+    bpot[i] = sup[i4[1] - 1 + i * nni];
+  }
+  for (int j = 0; j < nni; j++) dnu[j] = sup[i4[2] - 1 + nni + j];
+  cudaMemcpy(const_cast<double *>(d.borb_mu), borb.data(), nmu * sizeof(double), cudaMemcpyHostToDevice);
+  cudaMemcpy(const_cast<double *>(d.bpot_mu), bpot.data(), nmu * sizeof(double), cudaMemcpyHostToDevice);
+  cudaMemcpy(const_cast<double *>(d.d_nu), dnu.data(), nni * sizeof(double), cudaMemcpyHostToDevice);
+}
+  return X2G_OK;
+}
+
+void mcsor_common(int *isym, double *wk2, double *lhs, double *rhs) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!have_common()) {
+    set_status(X2G_ERR_NO_COMMON, "x2dhf COMMON blocks are not linked");
+    return;
+  }
+  if (ensure_grid()) return;
+  x2g_mcsor_host(g_ctx, g_grid, *isym, 0, c_interface_45_.omegac, c_interface_17_.maxsor2c, wk2, lhs, rhs);
+}
+
+// coulExch_pthread_: every potential of orbital iorbc in one launch, with
+// relax_single_pot_pthread.c:74-92's lhs/rhs and putinc/putoutc embedding
+void coulexch_common() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!have_common() || !&c_interface_46_ || !&c_interface_8_ || !&c_orbptr_ || !&c_exchptr_ ||
+      !&c_interface_1_ || !&c_interface_7_) {
+    set_status(X2G_ERR_NO_COMMON, "x2dhf COMMON blocks are not linked");
+    return;
+  }
+  if (ensure_grid()) return;
+  const int iorb = c_interface_46_.iorbc;
+  const int n = c_interface_8_.nexchpotsc[iorb - 1];
+  const int nni = g_nni, nmu = g_nmu, mx = nni * nmu;
+  const GridDev &g = g_grid->d;
+  const double *sup = c_supplptr_.p;
+  const int *i4 = c_i4b_.i4barr;
+  const double *f3 = sup + i4[7] - 1, *ef = sup + i4[3] - 1, *gf = sup + i4[9] - 1;
+  const double *psi = c_orbptr_.p;
+  double *excp = c_exchptr_.p;
+  const int maxsor1 = c_interface_17_.maxsor1c, maxsor2 = c_interface_17_.maxsor2c;
+  const double omega = c_interface_45_.omegac;
+  double *buf = nullptr;
+  const size_t per = size_t(g.next) + 3 * size_t(mx);
+  if (cudaMalloc(&buf, per * n * sizeof(double)) != cudaSuccess) {
+    set_status(X2G_ERR_ALLOC, "coulExch buffers");
+    return;
+  }
+  std::vector<double> h(size_t(3) * mx);
+  std::vector<x2g_job> jobs(n);
+  for (int k = 0; k < n; k++) {
+    const int in1 = c_interface_1_.v[k][iorb - 1], in2 = c_interface_2_.v[k][iorb - 1];
+    const int ib1 = c_interface_7_.i1bc[in1 - 1], ib2 = c_interface_7_.i1bc[in2 - 1];
+    const int ibexc = c_interface_3_.v[k][iorb - 1];
+    const int idel = c_interface_4_.v[k][iorb - 1];
+    const int isym = c_interface_6_.v[k][iorb - 1];
+    const double deltam2 = double(idel * idel);
+    double *rhsh = h.data(), *lhsh = h.data() + mx, *funh = h.data() + 2 * size_t(mx);
+    for (int i = 0; i < mx; i++) rhsh[i] = psi[ib1 + i - 1] * psi[ib2 + i - 1] * gf[i];
+    for (int i = 0; i < mx; i++) lhsh[i] = (deltam2 == 0.0) ? f3[i] : f3[i] + ef[i] * deltam2;
+    std::memcpy(funh, excp + ibexc - 1, mx * sizeof(double));
+    double *base = buf + per * k;
+    cudaMemcpyAsync(base + g.next, h.data(), 3 * size_t(mx) * sizeof(double), cudaMemcpyHostToDevice, g_ctx->stream);
+    launch_putin(g_ctx, g, isym, base + g.next + 2 * size_t(mx), base);
+    cudaStreamSynchronize(g_ctx->stream);
+    x2g_job &j = jobs[k];
+    j.u = base;
+    j.rhs = base + g.next;
+    j.lhs = base + g.next + mx;
+    j.omega = omega;
+    j.isym = isym;
+    j.idel = idel;
+    j.kind = 1;
+  }
+  for (int it = 0; it < maxsor1; it++) launch_relax(g_ctx, g_grid, jobs.data(), n, maxsor2, X2G_FP64);
+  std::vector<double> out(mx);
+  for (int k = 0; k < n; k++) {
+    const int ibexc = c_interface_3_.v[k][iorb - 1];
+    double *base = buf + per * k;
+    launch_putout(g_ctx, g, base, base + g.next + 2 * size_t(mx));
+    cudaMemcpyAsync(out.data(), base + g.next + 2 * size_t(mx), mx * sizeof(double), cudaMemcpyDeviceToHost,
+                    g_ctx->stream);
+    if (x2g_synchronize(g_ctx)) break;
+    std::memcpy(excp + ibexc - 1, out.data(), mx * sizeof(double));
+  }
+  cudaFree(buf);
+}
+
+}  // namespace
+
+extern "C" {
+
+void mcsor_pthread_(int *isym, int *nthreads, double *wk2, double *lhs, double *rhs) {
+  (void)nthreads;
+  mcsor_common(isym, wk2, lhs, rhs);
+}
+
+void mcsor_tpool_(int *isym, int *nthreads, double *wk2, double *lhs, double *rhs) {
+  (void)nthreads;
+  mcsor_common(isym, wk2, lhs, rhs);
+}
+
+void coulExch_pthread_(void) { coulexch_common(); }
+
+void coulExch_tpool_(void) { coulexch_common(); }
+
+static void release() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (g_grid) x2g_grid_destroy(g_grid);
+  if (g_ctx) x2g_destroy(g_ctx);
+  g_grid = nullptr;
+  g_ctx = nullptr;
+}
+
+void tpoolStop4mcsor_(int *nthreads) {
+  (void)nthreads;
+  release();
+}
+
+void tpoolStop4pots_(int *nthreads) {
+  (void)nthreads;
+  release();
+}
+
+}  // extern "C"

@@ -1,0 +1,111 @@
+// Internal structures of the x2dhf GB300 relaxation library.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/x2dhf_gpu.h"
+
+namespace x2g {
+
+constexpr double kPrecis = 2.220446049250313080847263336181640625e-16;  // epsilon(1d0), initVariables.F90:397
+constexpr double kPi = 3.14159265358979323846264338327950;                // params.F90:94
+constexpr int kMaxLevels = 8;
+
+// ----------------------------------------------------------------------
+// Host-side grid: every table the relaxation path reads, built with the
+// reference's formulas (initCBAllocArrays.F90 initCBlocks:813-858,
+// initSuppl:1636-2051).  Indices are 0-based: nu j in [0,nni), mu i in
+// [0,nmu); plain index i*nni+j; extended index (i+4)*n8+(j+4).
+// ----------------------------------------------------------------------
+struct HostGrid {
+  int nni = 0, nmu = 0, n8 = 0, m8 = 0, next = 0, mxsize = 0, mpole = 4;
+  double r = 0, r2 = 0, z1 = 0, z2 = 0, rinf = 0, hni = 0, hmu = 0, diag = 0;
+  std::vector<double> vxi, vxisq, vxi1, vxi2, veta, vetasq, veta1, veta2, wmu, wni;
+  double dmu1[4], dmu2[4], dni1[4], dni2[4], exeven[5];
+  std::vector<double> dmu9, dni9;              // 9-point derivative weights (diffmu/diffnu)
+  std::vector<double> borb_mu, bpot_mu, f3_mu;  // mu-only coefficient tables
+  std::vector<double> d_nu;                     // nu-only
+  std::vector<double> e, f0, f1, f2, f4, g, wgt1, wgt2;  // plain 2-D tables
+  std::vector<double> leg;                      // mpole tables P_k(cos th) r^k, plain
+  // "middle" ordering of interior points (ext indices, reference list order)
+  std::vector<int> order;
+  // sweep schedule: tiles = bands of ext rows [row0,row1)
+  int ntiles = 0, nlev = 0;
+  std::vector<int> tile_row0, tile_row1;
+  std::vector<int> pts;  // ext indices grouped [tile][colour][level]
+  std::vector<int> off;  // (ntiles*5*nlev + 1) offsets into pts
+};
+
+std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf, double z1, double z2, int mpole);
+
+// ----------------------------------------------------------------------
+// Device view of a grid, passed by value to kernels.
+// ----------------------------------------------------------------------
+struct GridDev {
+  int nni, nmu, n8, m8, next, mxsize, ntiles, nlev, mpole;
+  double r2;
+  double dmu1[4], dmu2[4], dni1[4], dni2[4], exeven[5], diag;
+  const double *borb_mu, *bpot_mu, *f3_mu, *d_nu;
+  const double *e, *f0, *f1, *f2, *f4, *g, *wgt1, *wgt2, *leg;
+  const double *dmu9, *dni9;
+  const double *vxi, *vxisq, *veta, *vetasq;
+  const int *tile_row0, *tile_row1, *pts, *off;
+  // FP32 copies of the coefficient tables for the mixed form
+  const float *borb_mu32, *bpot_mu32, *d_nu32;
+};
+
+// Device job (one function to relax), built from x2g_job.
+struct JobDev {
+  double *u;
+  const double *lhs;
+  const double *rhs;
+  const double *psa, *psb;
+  double *rhs_buf;  // materialised rhs for potentials
+  float *e32;       // mixed: FP32 extended correction
+  float *r32, *l32; // mixed: FP32 residual and diagonal
+  double omega;
+  double idel2;
+  int isym, kind;
+};
+
+// Grid barrier state in device memory.
+struct BarrierDev {
+  unsigned int *count;
+  unsigned int *gen;
+  int *err;  // first error code (0 = none), phase where it happened
+};
+
+}  // namespace x2g
+
+struct x2g_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  // barrier words + error flag (4 ints)
+  unsigned int *bar = nullptr;
+  // reusable device workspace
+  void *work = nullptr;
+  size_t work_bytes = 0;
+  void *red = nullptr;  // reduction partials
+  size_t red_bytes = 0;
+  double *host_red = nullptr;  // pinned host buffer for small readbacks
+  long launches = 0;
+};
+
+struct x2g_grid {
+  x2g_ctx *ctx = nullptr;
+  x2g::HostGrid h;
+  x2g::GridDev d{};
+  std::vector<void *> allocs;
+};
+
+namespace x2g {
+// status helpers (x2g_capi.cu)
+int set_status(int code, const std::string &msg);
+int cuda_status(cudaError_t e, const char *where);
+void *ctx_workspace(x2g_ctx *ctx, size_t bytes);
+}  // namespace x2g

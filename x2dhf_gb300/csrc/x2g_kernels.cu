@@ -1,0 +1,1104 @@
+// CUDA kernels of the x2dhf GB300 relaxation library (sm_103a).
+//
+// Layout: every function lives in the reference's extended layout
+// ((nni+8) x (nmu+8) doubles, nu fastest), so putin reduces to a ghost
+// refresh and putout to nothing.  Plain 2-D tables are nni x nmu.
+//
+// FP64 arithmetic that must reproduce the reference bit for bit is written
+// with __dadd_rn/__dmul_rn/__ddiv_rn, which the compiler never contracts
+// into FMAs (the reference was built without FMA contraction).
+#include <cooperative_groups.h>
+#include <cstdio>
+
+#include "x2g_kernels.cuh"
+
+namespace x2g {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
+
+__device__ __forceinline__ double A(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double S(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double M(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double D(double a, double b) { return __ddiv_rn(a, b); }
+
+template <typename T>
+__device__ __forceinline__ T ldcg(const T *p) {
+  return __ldcg(p);
+}
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Grid-wide barrier for a cooperative launch.  Every wait is bounded: after
+// kBarrierTimeoutNs the block records X2G_ERR_TIMEOUT and all blocks leave
+// the kernel at their next barrier.  Returns false when the kernel must stop.
+__device__ bool grid_barrier(const BarrierDev &b, unsigned nblocks) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned *vgen = b.gen;
+    volatile int *verr = b.err;
+    const unsigned g0 = *vgen;
+    __threadfence();
+    const unsigned arrived = atomicAdd(b.count, 1u);
+    if (arrived == nblocks - 1) {
+      atomicExch(b.count, 0u);
+      __threadfence();
+      atomicAdd(b.gen, 1u);
+    } else {
+      const unsigned long long t0 = globaltimer();
+      unsigned spins = 0;
+      while (*vgen == g0) {
+        if (*verr) {
+          ok = 0;
+          break;
+        }
+        if ((++spins & 255u) == 0 && globaltimer() - t0 > kBarrierTimeoutNs) {
+          atomicCAS(b.err, 0, X2G_ERR_TIMEOUT);
+          ok = 0;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    if (*verr) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// ----------------------------------------------------------------------
+// One point update, FP64, reference arithmetic order (sormcsor.F90:46-71).
+// ----------------------------------------------------------------------
+__device__ __forceinline__ void relax_f64(double *__restrict__ u, int ij, const GridDev &g, double b, double d,
+                                          double lhs, double rhs, double omega, double omega1) {
+  const int n1 = g.n8, n2 = 2 * g.n8, n3 = 3 * g.n8, n4 = 4 * g.n8;
+  const double m4 = ldcg(u + ij - n4), p4 = ldcg(u + ij + n4);
+  const double m3 = ldcg(u + ij - n3), p3 = ldcg(u + ij + n3);
+  const double m2 = ldcg(u + ij - n2), p2 = ldcg(u + ij + n2);
+  const double m1 = ldcg(u + ij - n1), p1 = ldcg(u + ij + n1);
+  const double l4 = ldcg(u + ij - 4), r4 = ldcg(u + ij + 4);
+  const double l3 = ldcg(u + ij - 3), r3 = ldcg(u + ij + 3);
+  const double l2 = ldcg(u + ij - 2), r2 = ldcg(u + ij + 2);
+  const double l1 = ldcg(u + ij - 1), r1 = ldcg(u + ij + 1);
+  const double uc = ldcg(u + ij);
+  const double ddmi2 =
+      A(A(A(M(g.dmu2[0], A(m4, p4)), M(g.dmu2[1], A(m3, p3))), M(g.dmu2[2], A(m2, p2))), M(g.dmu2[3], A(m1, p1)));
+  const double ddmi1 =
+      A(A(A(M(g.dmu1[0], S(m4, p4)), M(g.dmu1[1], S(m3, p3))), M(g.dmu1[2], S(m2, p2))), M(g.dmu1[3], S(m1, p1)));
+  const double ddni2 =
+      A(A(A(M(g.dni2[0], A(l4, r4)), M(g.dni2[1], A(l3, r3))), M(g.dni2[2], A(l2, r2))), M(g.dni2[3], A(l1, r1)));
+  const double ddni1 =
+      A(A(A(M(g.dni1[0], S(l4, r4)), M(g.dni1[1], S(l3, r3))), M(g.dni1[2], S(l2, r2))), M(g.dni1[3], S(l1, r1)));
+  const double cc = A(A(A(ddmi2, M(b, ddmi1)), ddni2), M(d, ddni1));
+  u[ij] = A(D(M(omega, S(rhs, cc)), lhs), M(omega1, uc));
+}
+
+struct CoefF {
+  float dmu1[4], dmu2[4], dni1[4], dni2[4];
+};
+
+// FP32 correction sweep point update (same operator, FMA allowed).
+__device__ __forceinline__ void relax_f32(float *__restrict__ e, int ij, int n8, const CoefF &c, float b, float d,
+                                          float lhs, float r, float omega, float omega1) {
+  const int n1 = n8, n2 = 2 * n8, n3 = 3 * n8, n4 = 4 * n8;
+  const float m4 = ldcg(e + ij - n4), p4 = ldcg(e + ij + n4);
+  const float m3 = ldcg(e + ij - n3), p3 = ldcg(e + ij + n3);
+  const float m2 = ldcg(e + ij - n2), p2 = ldcg(e + ij + n2);
+  const float m1 = ldcg(e + ij - n1), p1 = ldcg(e + ij + n1);
+  const float l4 = ldcg(e + ij - 4), r4 = ldcg(e + ij + 4);
+  const float l3 = ldcg(e + ij - 3), r3 = ldcg(e + ij + 3);
+  const float l2 = ldcg(e + ij - 2), r2 = ldcg(e + ij + 2);
+  const float l1 = ldcg(e + ij - 1), r1 = ldcg(e + ij + 1);
+  const float ec = ldcg(e + ij);
+  float dm2 = c.dmu2[0] * (m4 + p4);
+  dm2 = __fmaf_rn(c.dmu2[1], m3 + p3, dm2);
+  dm2 = __fmaf_rn(c.dmu2[2], m2 + p2, dm2);
+  dm2 = __fmaf_rn(c.dmu2[3], m1 + p1, dm2);
+  float dm1 = c.dmu1[0] * (m4 - p4);
+  dm1 = __fmaf_rn(c.dmu1[1], m3 - p3, dm1);
+  dm1 = __fmaf_rn(c.dmu1[2], m2 - p2, dm1);
+  dm1 = __fmaf_rn(c.dmu1[3], m1 - p1, dm1);
+  float dn2 = c.dni2[0] * (l4 + r4);
+  dn2 = __fmaf_rn(c.dni2[1], l3 + r3, dn2);
+  dn2 = __fmaf_rn(c.dni2[2], l2 + r2, dn2);
+  dn2 = __fmaf_rn(c.dni2[3], l1 + r1, dn2);
+  float dn1 = c.dni1[0] * (l4 - r4);
+  dn1 = __fmaf_rn(c.dni1[1], l3 - r3, dn1);
+  dn1 = __fmaf_rn(c.dni1[2], l2 - r2, dn1);
+  dn1 = __fmaf_rn(c.dni1[3], l1 - r1, dn1);
+  const float cc = __fmaf_rn(d, dn1, __fmaf_rn(b, dm1, dm2) + dn2);
+  e[ij] = __fmaf_rn(omega1, ec, __fdividef(omega * (r - cc), lhs));
+}
+
+// ----------------------------------------------------------------------
+// Tile-local pieces of one relaxation call.  A tile is a band of ext rows
+// [row0,row1) over the full nu width.
+// ----------------------------------------------------------------------
+
+// putin ghosts for the tile's rows (src/inout.F90:47-80): ghost columns copy
+// nu = 2..5 / nni-1..nni-4, tile 0 also fills the mu ghost rows.
+__device__ void tile_ghosts(const GridDev &g, double *u, int t, int isym) {
+  const int row0 = g.tile_row0[t], row1 = g.tile_row1[t], n8 = g.n8, nni = g.nni;
+  const bool neg = (isym != 1);
+  const int nr = row1 - row0;
+  for (int k = threadIdx.x; k < nr * 8; k += blockDim.x) {
+    const int r = row0 + k / 8, q = k % 8;
+    const int base = r * n8;
+    if (q < 4) {
+      const int j = q + 1;  // ghost col 4-j <- col 4+j
+      const double v = ldcg(u + base + 4 + j);
+      u[base + 4 - j] = neg ? -v : v;
+    } else {
+      const int j = q - 3;  // ghost col nni+3+j <- col nni+3-j
+      const double v = ldcg(u + base + nni + 3 - j);
+      u[base + nni + 3 + j] = neg ? -v : v;
+    }
+  }
+  if (t == 0) {
+    for (int k = threadIdx.x; k < 4 * nni; k += blockDim.x) {
+      const int i = k / nni + 1, col = 4 + k % nni;  // ghost row 4-i <- row 4+i
+      const double v = ldcg(u + (4 + i) * n8 + col);
+      u[(4 - i) * n8 + col] = neg ? -v : v;
+    }
+  }
+}
+
+// Axis extrapolation after a micro-sweep (sormcsor.F90:94-129): mu=1 row
+// (tile 0), nu=1 and nu=nni columns of the tile's rows; the two corners at
+// mu=1 read the freshly extrapolated mu=1 row, so they follow a sync.
+template <typename T>
+__device__ void tile_boundary(const GridDev &g, T *u, int t, int isym) {
+  const int row0 = g.tile_row0[t], row1 = g.tile_row1[t], n8 = g.n8, nni = g.nni;
+  const int n1 = n8, n2 = 2 * n8, n3 = 3 * n8, n4 = 4 * n8, n5 = 5 * n8;
+  const bool even = (isym == 1);
+  const int nrow7 = (t == 0) ? nni - 2 : 0;
+  const int r0 = (t == 0) ? 5 : row0;
+  const int nside = 2 * (row1 - r0);
+  for (int k = threadIdx.x; k < nrow7 + nside; k += blockDim.x) {
+    if (k < nrow7) {
+      const int ij = 4 * n8 + 5 + k;
+      T v = T(0);
+      if (even) {
+        if constexpr (sizeof(T) == 8) {
+          v = A(A(A(A(M(g.exeven[0], ldcg(u + ij + n1)), M(g.exeven[1], ldcg(u + ij + n2))),
+                    M(g.exeven[2], ldcg(u + ij + n3))),
+                  M(g.exeven[3], ldcg(u + ij + n4))),
+                M(g.exeven[4], ldcg(u + ij + n5)));
+        } else {
+          v = T(g.exeven[0]) * ldcg(u + ij + n1) + T(g.exeven[1]) * ldcg(u + ij + n2) +
+              T(g.exeven[2]) * ldcg(u + ij + n3) + T(g.exeven[3]) * ldcg(u + ij + n4) +
+              T(g.exeven[4]) * ldcg(u + ij + n5);
+        }
+      }
+      u[ij] = v;
+    } else {
+      const int q = k - nrow7;
+      const int r = r0 + q / 2;
+      const int side = q % 2;
+      const int ij = r * n8 + (side == 0 ? 4 : nni + 3);
+      const int s = (side == 0) ? 1 : -1;
+      T v = T(0);
+      if (even) {
+        if constexpr (sizeof(T) == 8) {
+          v = A(A(A(A(M(g.exeven[0], ldcg(u + ij + s)), M(g.exeven[1], ldcg(u + ij + 2 * s))),
+                    M(g.exeven[2], ldcg(u + ij + 3 * s))),
+                  M(g.exeven[3], ldcg(u + ij + 4 * s))),
+                M(g.exeven[4], ldcg(u + ij + 5 * s)));
+        } else {
+          v = T(g.exeven[0]) * ldcg(u + ij + s) + T(g.exeven[1]) * ldcg(u + ij + 2 * s) +
+              T(g.exeven[2]) * ldcg(u + ij + 3 * s) + T(g.exeven[3]) * ldcg(u + ij + 4 * s) +
+              T(g.exeven[4]) * ldcg(u + ij + 5 * s);
+        }
+      }
+      u[ij] = v;
+    }
+  }
+  if (t == 0) {
+    __syncthreads();
+    if (threadIdx.x < 2) {
+      const int ij = 4 * n8 + (threadIdx.x == 0 ? 4 : nni + 3);
+      const int s = (threadIdx.x == 0) ? 1 : -1;
+      T v = T(0);
+      if (even) {
+        if constexpr (sizeof(T) == 8) {
+          v = A(A(A(A(M(g.exeven[0], ldcg(u + ij + s)), M(g.exeven[1], ldcg(u + ij + 2 * s))),
+                    M(g.exeven[2], ldcg(u + ij + 3 * s))),
+                  M(g.exeven[3], ldcg(u + ij + 4 * s))),
+                M(g.exeven[4], ldcg(u + ij + 5 * s)));
+        } else {
+          v = T(g.exeven[0]) * ldcg(u + ij + s) + T(g.exeven[1]) * ldcg(u + ij + 2 * s) +
+              T(g.exeven[2]) * ldcg(u + ij + 3 * s) + T(g.exeven[3]) * ldcg(u + ij + 4 * s) +
+              T(g.exeven[4]) * ldcg(u + ij + 5 * s);
+        }
+      }
+      u[ij] = v;
+    }
+  }
+}
+
+// Potential right-hand side for the tile's interior points
+// (relaxPots.F90:81-82: rhs = psi_a psi_b g, two successive products).
+__device__ void tile_rhs(const GridDev &g, const JobDev &J, int t) {
+  const int b0 = g.off[(t * 5) * g.nlev], b1 = g.off[(t * 5 + 5) * g.nlev];
+  for (int k = b0 + threadIdx.x; k < b1; k += blockDim.x) {
+    const int ij = g.pts[k];
+    const int row = ij / g.n8, col = ij - row * g.n8;
+    const int ik = (row - 4) * g.nni + (col - 4);
+    J.rhs_buf[ik] = M(M(J.psa[ij], J.psb[ij]), g.g[ik]);
+  }
+}
+
+// ----------------------------------------------------------------------
+// Persistent cooperative MCSOR kernel: all jobs x tiles, 5 colour phases
+// per micro-sweep, grid barrier between phases.
+// ----------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_mcsor_f64(GridDev g, const JobDev *__restrict__ jobs, int njobs,
+                                                        int nsweeps, BarrierDev bar, unsigned nblocks) {
+  const int nitems = njobs * g.ntiles;
+  for (int s = 0; s < nsweeps; ++s) {
+    for (int c = 0; c < 5; ++c) {
+      for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const int jb = item / g.ntiles, t = item - jb * g.ntiles;
+        const JobDev &J = jobs[jb];
+        double *u = J.u;
+        if (c == 0) {
+          if (s == 0) {
+            tile_ghosts(g, u, t, J.isym);
+            if (J.kind == 1) tile_rhs(g, J, t);  // kind 2: explicit rhs
+          } else {
+            tile_boundary<double>(g, u, t, J.isym);
+          }
+          __syncthreads();
+        }
+        const double omega = J.omega, omega1 = 1.0 - J.omega;  // omega1 = 1 - omega (relaxOrbs.F90:83)
+        const double *bt = (J.kind >= 1) ? g.bpot_mu : g.borb_mu;
+        const double *rhsv = (J.kind == 1) ? J.rhs_buf : J.rhs;
+        for (int l = 0; l < g.nlev; ++l) {
+          const int o = (t * 5 + c) * g.nlev + l;
+          const int b0 = g.off[o], b1 = g.off[o + 1];
+          if (b0 == b1) continue;
+          for (int k = b0 + threadIdx.x; k < b1; k += blockDim.x) {
+            const int ij = g.pts[k];
+            const int row = ij / g.n8, col = ij - row * g.n8;
+            const int mu = row - 4, nu = col - 4, ik = mu * g.nni + nu;
+            double lhs;
+            if (J.kind == 1)
+              lhs = (J.idel2 == 0.0) ? g.f3_mu[mu] : A(g.f3_mu[mu], M(J.idel2, g.e[ik]));
+            else
+              lhs = J.lhs[ik];
+            relax_f64(u, ij, g, bt[mu], g.d_nu[nu], lhs, rhsv[ik], omega, omega1);
+          }
+          __syncthreads();
+        }
+      }
+      if (!(s == nsweeps - 1 && c == 4)) {
+        if (!grid_barrier(bar, nblocks)) return;
+      }
+    }
+  }
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+    const int jb = item / g.ntiles, t = item - jb * g.ntiles;
+    tile_boundary<double>(g, jobs[jb].u, t, jobs[jb].isym);
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_mcsor_f32(GridDev g, const JobDev *__restrict__ jobs, int njobs,
+                                                        int nsweeps, BarrierDev bar, unsigned nblocks) {
+  const int nitems = njobs * g.ntiles;
+  CoefF cf;
+  for (int k = 0; k < 4; ++k) {
+    cf.dmu1[k] = float(g.dmu1[k]);
+    cf.dmu2[k] = float(g.dmu2[k]);
+    cf.dni1[k] = float(g.dni1[k]);
+    cf.dni2[k] = float(g.dni2[k]);
+  }
+  for (int s = 0; s < nsweeps; ++s) {
+    for (int c = 0; c < 5; ++c) {
+      for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const int jb = item / g.ntiles, t = item - jb * g.ntiles;
+        const JobDev &J = jobs[jb];
+        float *e = J.e32;
+        if (c == 0 && s > 0) {
+          tile_boundary<float>(g, e, t, J.isym);
+          __syncthreads();
+        }
+        const float omega = float(J.omega), omega1 = float(1.0 - J.omega);
+        const float *bt = (J.kind >= 1) ? g.bpot_mu32 : g.borb_mu32;
+        for (int l = 0; l < g.nlev; ++l) {
+          const int o = (t * 5 + c) * g.nlev + l;
+          const int b0 = g.off[o], b1 = g.off[o + 1];
+          if (b0 == b1) continue;
+          for (int k = b0 + threadIdx.x; k < b1; k += blockDim.x) {
+            const int ij = g.pts[k];
+            const int row = ij / g.n8, col = ij - row * g.n8;
+            const int mu = row - 4, nu = col - 4, ik = mu * g.nni + nu;
+            relax_f32(e, ij, g.n8, cf, bt[mu], g.d_nu32[nu], J.l32[ik], J.r32[ik], omega, omega1);
+          }
+          __syncthreads();
+        }
+      }
+      if (!(s == nsweeps - 1 && c == 4)) {
+        if (!grid_barrier(bar, nblocks)) return;
+      }
+    }
+  }
+  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+    const int jb = item / g.ntiles, t = item - jb * g.ntiles;
+    tile_boundary<float>(g, jobs[jb].e32, t, jobs[jb].isym);
+    __syncthreads();
+  }
+}
+
+// ----------------------------------------------------------------------
+// Mixed form: ghost refresh, FP64 residual, FP32 correction, FP64 update.
+// ----------------------------------------------------------------------
+__device__ __forceinline__ void ghost_point(const GridDev &g, double *u, int k, int isym) {
+  // k indexes (rows 4..nmu+3) x 8 ghost columns, then 4 ghost rows x nni
+  const int nrows = g.nmu;
+  const bool neg = (isym != 1);
+  if (k < nrows * 8) {
+    const int r = 4 + k / 8, q = k % 8, base = r * g.n8;
+    if (q < 4) {
+      const int j = q + 1;
+      const double v = u[base + 4 + j];
+      u[base + 4 - j] = neg ? -v : v;
+    } else {
+      const int j = q - 3;
+      const double v = u[base + g.nni + 3 - j];
+      u[base + g.nni + 3 + j] = neg ? -v : v;
+    }
+  } else {
+    k -= nrows * 8;
+    const int i = k / g.nni + 1, col = 4 + k % g.nni;
+    const double v = u[(4 + i) * g.n8 + col];
+    u[(4 - i) * g.n8 + col] = neg ? -v : v;
+  }
+}
+
+__global__ void k_ghost_jobs(GridDev g, const JobDev *__restrict__ jobs) {
+  const JobDev &J = jobs[blockIdx.y];
+  const int n = g.nmu * 8 + 4 * g.nni;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) ghost_point(g, J.u, k, J.isym);
+}
+
+__global__ void k_residual(GridDev g, const JobDev *__restrict__ jobs) {
+  const JobDev &J = jobs[blockIdx.y];
+  const int nint = (g.nni - 2) * (g.nmu - 5);
+  const int n1 = g.n8, n2 = 2 * g.n8, n3 = 3 * g.n8, n4 = 4 * g.n8;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.next; k += gridDim.x * blockDim.x) J.e32[k] = 0.0f;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nint; k += gridDim.x * blockDim.x) {
+    const int mu = 1 + k / (g.nni - 2), nu = 1 + k % (g.nni - 2);
+    const int ik = mu * g.nni + nu, ij = (mu + 4) * g.n8 + nu + 4;
+    const double *u = J.u;
+    double rhs, lhs, b;
+    if (J.kind == 1) {
+      rhs = (J.psa[ij] * J.psb[ij]) * g.g[ik];
+      lhs = (J.idel2 == 0.0) ? g.f3_mu[mu] : g.f3_mu[mu] + J.idel2 * g.e[ik];
+      b = g.bpot_mu[mu];
+    } else {
+      rhs = J.rhs[ik];
+      lhs = J.lhs[ik];
+      b = (J.kind == 2) ? g.bpot_mu[mu] : g.borb_mu[mu];
+    }
+    const double d = g.d_nu[nu];
+    double dm2 = 0, dm1 = 0, dn2 = 0, dn1 = 0;
+    const int offs[4] = {n4, n3, n2, n1};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const double a = u[ij - offs[q]], c = u[ij + offs[q]];
+      dm2 = fma(g.dmu2[q], a + c, dm2);
+      dm1 = fma(g.dmu1[q], a - c, dm1);
+      const double l = u[ij - (4 - q)], r = u[ij + (4 - q)];
+      dn2 = fma(g.dni2[q], l + r, dn2);
+      dn1 = fma(g.dni1[q], l - r, dn1);
+    }
+    const double cc = fma(d, dn1, fma(b, dm1, dm2) + dn2);
+    const double res = rhs - cc - lhs * u[ij];
+    J.r32[ik] = float(res);
+    J.l32[ik] = float(lhs);
+  }
+}
+
+__global__ void k_update(GridDev g, const JobDev *__restrict__ jobs) {
+  const JobDev &J = jobs[blockIdx.y];
+  const int nint = (g.nni - 2) * (g.nmu - 5);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nint; k += gridDim.x * blockDim.x) {
+    const int mu = 1 + k / (g.nni - 2), nu = 1 + k % (g.nni - 2);
+    const int ij = (mu + 4) * g.n8 + nu + 4;
+    J.u[ij] += double(J.e32[ij]);
+  }
+}
+
+// Axis extrapolation of the FP64 function after the update (one block per job).
+__global__ void k_extrap_jobs(GridDev g, const JobDev *__restrict__ jobs) {
+  const JobDev &J = jobs[blockIdx.x];
+  double *u = J.u;
+  const int n8 = g.n8, nni = g.nni;
+  const bool even = (J.isym == 1);
+  const int nrow7 = nni - 2, nside = 2 * (g.nmu - 5);
+  auto ex = [&](int ij, int s) {
+    return A(A(A(A(M(g.exeven[0], u[ij + s]), M(g.exeven[1], u[ij + 2 * s])), M(g.exeven[2], u[ij + 3 * s])),
+               M(g.exeven[3], u[ij + 4 * s])),
+             M(g.exeven[4], u[ij + 5 * s]));
+  };
+  for (int k = threadIdx.x; k < nrow7 + nside; k += blockDim.x) {
+    if (k < nrow7) {
+      const int ij = 4 * n8 + 5 + k;
+      u[ij] = even ? ex(ij, n8) : 0.0;
+    } else {
+      const int q = k - nrow7, r = 5 + q / 2, side = q % 2;
+      const int ij = r * n8 + (side == 0 ? 4 : nni + 3);
+      u[ij] = even ? ex(ij, side == 0 ? 1 : -1) : 0.0;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    const int ij = 4 * n8 + (threadIdx.x == 0 ? 4 : nni + 3);
+    u[ij] = even ? ex(ij, threadIdx.x == 0 ? 1 : -1) : 0.0;
+  }
+}
+
+// ----------------------------------------------------------------------
+// Elementwise kernels of the SCF path
+// ----------------------------------------------------------------------
+__global__ void k_ghost(GridDev g, double *u, int isym) {
+  const int n = g.nmu * 8 + 4 * g.nni;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) ghost_point(g, u, k, isym);
+}
+
+__global__ void k_putin_interior(GridDev g, const double *plain, double *ext) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+    const int mu = k / g.nni, nu = k - mu * g.nni;
+    ext[(mu + 4) * g.n8 + nu + 4] = plain[k];
+  }
+}
+
+__global__ void k_putout(GridDev g, const double *ext, double *plain) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+    const int mu = k / g.nni, nu = k - mu * g.nni;
+    plain[k] = ext[(mu + 4) * g.n8 + nu + 4];
+  }
+}
+
+// fockHF (src/fock.F90:57-186), per grid point in the reference's order.
+__global__ void k_fock(GridDev g, FockArgs a) {
+  const double ee = *a.ee;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+    const int mu = k / g.nni, nu = k - mu * g.nni;
+    const int ij = (mu + 4) * g.n8 + nu + 4;
+    double fock1 = g.f0[k];
+    fock1 = A(M(ee, g.f1[k]), fock1);
+    if (a.m != 0) fock1 = A(M(double(a.m * a.m), g.e[k]), fock1);
+    double fock2 = 0.0;
+    if (!a.nel1) {
+      double wk1 = 0.0;
+      for (int q = 0; q < a.nterms; ++q) {
+        const FockTerm &T = a.t[q];
+        wk1 = A(M(T.coo, T.coul[ij]), wk1);
+        if (T.mode == 0) {
+          double wk2 = M(T.gec, T.ex[ij]);
+          if (T.ex2) wk2 = A(M(T.gec2, T.ex2[ij]), wk2);
+          wk2 = M(wk2, T.psi[ij]);
+          fock2 = A(fock2, wk2);
+        } else if (T.mode == 1) {
+          const double wk2 = M(T.ex[ij], T.psi[ij]);
+          fock2 = A(M(T.gec, wk2), fock2);
+        }
+      }
+      a.coulp[k] = wk1;
+      a.exchp[k] = fock2;
+      wk1 = M(wk1, g.f2[k]);
+      fock2 = M(fock2, g.f2[k]);
+      fock1 = A(fock1, wk1);
+    }
+    a.lhs[k] = A(fock1, g.diag);
+    a.rhs[k] = fock2;
+    if (mu >= g.nmu - 5) {
+      const double f1 = g.f1[k];
+      a.fa[(mu - (g.nmu - 5)) * g.nni + nu] = (fabs(f1) <= kPrecis) ? 0.0 : D(fock1, f1);
+    }
+  }
+}
+
+// orbAsymptGet (relaxOrbs.F90:415-437): edecay for mu = nmu-4..nmu-1 (0-based)
+__global__ void k_asympt_get(GridDev g, const double *fa, double *edecay) {
+  const int n = 4 * g.nni;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int jj = k / g.nni, i = k - jj * g.nni;
+    const int j = g.nmu - 4 + jj;  // 0-based mu
+    const double raiq1 = sqrt(g.vxisq[j - 1] + g.vetasq[i] - 1.0);
+    const double raiq = sqrt(g.vxisq[j] + g.vetasq[i] - 1.0);
+    const double fj = fa[(jj + 1) * g.nni + i], fjm = fa[jj * g.nni + i];
+    edecay[k] = pow(fabs(fj / fjm), 0.250) * exp(sqrt(fabs(fjm)) * (raiq1 - raiq));
+  }
+}
+
+// orbAsymptSet (relaxOrbs.F90:444-462), rows in order
+__global__ void k_asympt_set(GridDev g, double *psi, const double *edecay) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.nni; i += gridDim.x * blockDim.x) {
+    for (int jj = 0; jj < 4; ++jj) {
+      const int j = g.nmu - 4 + jj;
+      const int ij = (j + 4) * g.n8 + i + 4;
+      psi[ij] = M(psi[ij - g.n8], edecay[jj * g.nni + i]);
+    }
+  }
+}
+
+// setCiOrb (scfUtils.F90:380-434)
+__global__ void k_setci(GridDev g, double *psi, int ihomo) {
+  const int n2 = g.nni / 2 + 1;
+  const int n = (n2 - 1) * g.nmu;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int mu = k / (n2 - 1), ni = k - mu * (n2 - 1);  // ni 0-based = reference ni-1
+    const int row = (mu + 4) * g.n8 + 4;
+    const double v = psi[row + ni];
+    psi[row + (g.nni - 1 - ni)] = (ihomo == 1) ? v : -v;
+  }
+  if (ihomo != 1) {
+    for (int mu = blockIdx.x * blockDim.x + threadIdx.x; mu < g.nmu; mu += gridDim.x * blockDim.x)
+      psi[(mu + 4) * g.n8 + 4 + (n2 - 1)] = 0.0;
+  }
+}
+
+// norm scaling: psi = (1/sqrt(xnorm)) psi over the plain region (normOrtho.F90:50-52)
+__global__ void k_scale(GridDev g, double *psi, const double *xnorm) {
+  const double zarea = D(1.0, sqrt(*xnorm));
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+    const int mu = k / g.nni, nu = k - mu * g.nni;
+    const int ij = (mu + 4) * g.n8 + nu + 4;
+    psi[ij] = M(zarea, psi[ij]);
+  }
+}
+
+struct PtrList {
+  const double *p[kMaxTerms];
+};
+
+// Gram-Schmidt step of ortho (normOrtho.F90:175-188)
+__global__ void k_ortho_apply(GridDev g, double *psi, PtrList others, int n, const double *ovl) {
+  double ano = 0.0;
+  for (int q = 0; q < n; ++q) ano = A(ano, M(ovl[q], ovl[q]));
+  ano = D(sqrt(A(1.0, ano)), S(1.0, M(ano, ano)));
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+    const int mu = k / g.nni, nu = k - mu * g.nni;
+    const int ij = (mu + 4) * g.n8 + nu + 4;
+    double v = psi[ij];
+    for (int q = 0; q < n; ++q) v = A(M(-ovl[q], others.p[q][ij]), v);
+    psi[ij] = M(ano, v);
+  }
+}
+
+// vexch/mulex normalised associated Legendre functions P_k^q(cos th) for
+// k = 1..mpole (scfUtils.F90:856-1270).  legacy_m3 reproduces vexch's m=3
+// branch, which uses sin^2 in place of sin.
+__device__ void assoc_legendre(int mt, int mpole, double costh, double *dome, bool legacy_m3) {
+  for (int k = 0; k < 10; ++k) dome[k] = 0.0;
+  if (mt > 4) return;
+  double c2, c4, c6, c8, si, si2, si3;
+  if (mt == 0) {
+    dome[1] = costh;
+    dome[2] = (3.0 * costh * costh - 1.0) * 0.50;
+    for (int n = 2; n <= mpole - 1; n++)
+      dome[n + 1] = (double(2 * n + 1) * costh * dome[n] - double(n) * dome[n - 1]) / double(n + 1);
+  } else if (mt == 1) {
+    c2 = costh * costh;
+    si2 = fabs(1.0 - c2);
+    si = sqrt(si2);
+    c4 = c2 * c2;
+    c6 = c4 * c2;
+    dome[1] = -si / sqrt(2.0);
+    dome[2] = -3.0 * si * costh / sqrt(6.0);
+    dome[3] = (3.0 / 2.0) * si * (1.0 - 5.0 * c2) / sqrt(12.0);
+    dome[4] = (5.0 / 2.0) * si * costh * (3.0 - 7.0 * c2) / sqrt(20.0);
+    dome[5] = (15.0 / 8.0) * si * (-1.0 + 14.0 * c2 - 21.0 * c4) / sqrt(30.0);
+    dome[6] = (21.0 / 8.0) * si * costh * (-5.0 + 30.0 * c2 - 33.0 * c4) / sqrt(42.0);
+    dome[7] = (7.0 / 16.0) * si * (5.0 - 135.0 * c2 + 495.0 * c4 - 429.0 * c6) / sqrt(56.0);
+    dome[8] = (9.0 / 16.0) * si * costh * (35.0 - 385.0 * c2 + 1001.0 * c4 - 715.0 * c6) / sqrt(72.0);
+  } else if (mt == 2) {
+    c2 = costh * costh;
+    si2 = fabs(1.0 - c2);
+    c4 = c2 * c2;
+    c6 = c4 * c2;
+    c8 = c6 * c2;
+    dome[2] = 3.0 * si2 / sqrt(24.0);
+    dome[3] = 15.0 * costh * si2 / sqrt(120.0);
+    dome[4] = (15.0 / 2.0) * (-1.0 + 8.0 * c2 - 7.0 * c4) / sqrt(360.0);
+    dome[5] = (105.0 / 2.0) * costh * (-1.0 + 4.0 * c2 - 3.0 * c4) / sqrt(840.0);
+    dome[6] = (105.0 / 8.0) * (1.0 - 19.0 * c2 + 51.0 * c4 - 33.0 * c6) / sqrt(1680.0);
+    dome[7] = (63.0 / 8.0) * costh * (15.0 - 125.0 * c2 + 253.0 * c4 - 143.0 * c6) / sqrt(3024.0);
+    dome[8] = (315.0 / 8.0) * (-1.0 + 34.0 * c2 - 176.0 * c4 + 286.0 * c6 - 143.0 * c8) / sqrt(5040.0);
+  } else if (mt == 3) {
+    c2 = costh * costh;
+    si2 = fabs(1.0 - c2);
+    si = legacy_m3 ? si2 : sqrt(si2);
+    si3 = si2 * si;
+    c4 = c2 * c2;
+    dome[3] = -15.0 * si3 / sqrt(720.0);
+    dome[4] = -105.0 * si3 * costh / sqrt(5040.0);
+    dome[5] = -(105.0 / 2.0) * si3 * (-1.0 + 9.0 * c2) / sqrt(20160.0);
+    dome[6] = -(315.0 / 2.0) * si3 * costh * (-3.0 + 11.0 * c2) / sqrt(60480.0);
+    dome[7] = -(315.0 / 8.0) * si3 * (3.0 - 66.0 * c2 + 143.0 * c4) / sqrt(151200.0);
+    dome[8] = -(3465.0 / 8.0) * si3 * costh * (3.0 - 26.0 * c2 + 39.0 * c4) / sqrt(332640.0);
+  } else if (mt == 4) {
+    c2 = costh * costh;
+    c4 = c2 * c2;
+    c6 = c4 * c2;
+    c8 = c6 * c2;
+    dome[4] = 105.0 * (1.0 - 2.0 * c2 + c4) / sqrt(40320.0);
+    dome[5] = 945.0 * costh * (1.0 - 2.0 * c2 + c4) / sqrt(362880.0);
+    dome[6] = (945.0 / 2.0) * (-1.0 + 13 * c2 - 23.0 * c4 + 11.0 * c6) / sqrt(1814400.0);
+    dome[7] = (3465.0 / 2.0) * costh * (-3.0 + 19 * c2 - 29.0 * c4 + 13.0 * c6) / sqrt(6652800.0);
+    dome[8] = (10395.0 / 8.0) * (1.0 - 28.0 * c2 + 118.0 * c4 - 156.0 * c6 + 65.0 * c8) / sqrt(19958400.0);
+  }
+  for (int k = mpole + 1; k <= 8; ++k) dome[k] = 0.0;
+}
+
+// potAsympt: Coulomb (coulAsympt/vcoul) and exchange (exchAsympt/vexch)
+// boundary values on mu = nmu-4..nmu-1 (0-based).
+__global__ void k_asympt(GridDev g, AsymptArgs a) {
+  const AsymptItem &it = a.it[blockIdx.y];
+  const int n = 4 * g.nni;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int jj = k / g.nni, i = k - jj * g.nni;
+    const int j = g.nmu - 4 + jj;
+    const int ij = (j + 4) * g.n8 + i + 4;
+    double rr = sqrt(g.vxisq[j] + g.vetasq[i] - 1.0);
+    if (it.type == 0) {
+      const double rr1 = 1.0 / (rr * g.r2);
+      const double costh = g.veta[i] * g.vxi[j] / rr;
+      double dome[10];
+      dome[1] = costh;
+      dome[2] = (3.0 * costh * costh - 1.0) * 0.5;
+      for (int m = 2; m <= g.mpole - 1; m++)
+        dome[m + 1] = (double(2 * m + 1) * costh * dome[m] - double(m) * dome[m - 1]) / double(m + 1);
+      double pe = 0.0;
+      for (int m = 1; m <= g.mpole; m++)
+        pe = pe + a.cmulti[it.idx * 8 + (m - 1)] * dome[m] * pow(rr1, double(m + 1));
+      it.pot[ij] = g.r2 * g.vxi[j] * (rr1 + pe);
+    } else {
+      double pe = 0.0;
+      if (it.idel <= 4) {
+        const double costh = (fabs(rr) > kPrecis) ? g.veta[i] * g.vxi[j] / rr : 0.0;
+        rr = rr * g.r2;
+        double dome[10];
+        assoc_legendre(it.idel, g.mpole, costh, dome, true);
+        double xrn = rr * rr;
+        pe = dome[1] * a.excm[it.idx * 8 + 0] / xrn;
+        for (int m = 2; m <= g.mpole; m++) {
+          xrn = xrn * rr;
+          pe = pe + dome[m] * a.excm[it.idx * 8 + (m - 1)] / xrn;
+        }
+      }
+      it.pot[ij] = g.r2 * g.vxi[j] * pe;
+    }
+  }
+}
+
+__global__ void k_zero(double *p, size_t n) {
+  for (size_t k = blockIdx.x * size_t(blockDim.x) + threadIdx.x; k < n; k += size_t(gridDim.x) * blockDim.x) p[k] = 0.0;
+}
+
+// ----------------------------------------------------------------------
+// Deterministic reductions: fixed grid -> per-block partials -> one block
+// sums the partials in block order.
+// ----------------------------------------------------------------------
+constexpr int kRedBlocks = 160;
+constexpr int kMaxK = 16;
+
+template <int K>
+__device__ void block_sum_store(double (&v)[K], double *partials) {
+  __shared__ double sh[kThreads / 32][K];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < K; ++q) {
+    double x = v[q];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[w][q] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double s = 0.0;
+    for (int i = 0; i < kThreads / 32; ++i) s += sh[i][threadIdx.x];
+    partials[blockIdx.x * K + threadIdx.x] = s;
+  }
+}
+
+// final pass: out[q] = sum over blocks, then an optional epilogue
+template <int K>
+__global__ void k_reduce_final(const double *partials, int nblocks, double *out, int nout) {
+  __shared__ double sh[kThreads / 32];
+  for (int q = 0; q < nout; ++q) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partials[b * K + q];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int i = 0; i < kThreads / 32; ++i) t += sh[i];
+      out[q] = t;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_norm(GridDev g, const double *psi, double *partials) {
+  double v[1] = {0.0};
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+    const int mu = k / g.nni, nu = k - mu * g.nni;
+    const double p = psi[(mu + 4) * g.n8 + nu + 4];
+    v[0] += g.wgt2[k] * M(M(p, p), g.f4[k]);
+  }
+  block_sum_store<1>(v, partials);
+}
+
+__global__ void k_overlaps(GridDev g, const double *psi, PtrList o, int n, double *partials) {
+  double v[kMaxK];
+  for (int q = 0; q < kMaxK; ++q) v[q] = 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+    const int mu = k / g.nni, nu = k - mu * g.nni;
+    const int ij = (mu + 4) * g.n8 + nu + 4;
+    const double p = psi[ij], w = g.wgt2[k], f4 = g.f4[k];
+    for (int q = 0; q < n; ++q) v[q] += w * M(M(p, o.p[q][ij]), f4);
+  }
+  block_sum_store<kMaxK>(v, partials);
+}
+
+// EaHF = oneelij(i,i) + (J + K): per point terms of integrals.F90:406-480
+// and lagrangeMultipliers.F90:67-72.  psi has its ghosts filled.
+__global__ void k_eahf(GridDev g, const double *psi, int m, const double *coulp, const double *exchp,
+                       double *partials) {
+  double v[5] = {0, 0, 0, 0, 0};
+  const int n8 = g.n8;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+    const int mu = k / g.nni, nu = k - mu * g.nni;
+    const int ij = (mu + 4) * n8 + nu + 4;
+    // diffnu: sum_k f(nu+k-4) dni(k,nu); diffmu: sum_k f(mu+k-4) dmu(k,mu) (dgemv order)
+    double sn = 0.0, sm = 0.0;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) sn = A(sn, M(psi[ij + q - 4], g.dni9[9 * nu + q]));
+#pragma unroll
+    for (int q = 0; q < 9; ++q) sm = A(sm, M(psi[ij + (q - 4) * n8], g.dmu9[9 * mu + q]));
+    double kin = A(sn, sm);
+    const double p = psi[ij];
+    if (m != 0) kin = A(M(M(double(m * m), g.e[k]), p), kin);
+    const double t = M(A(M(p, g.f0[k]), kin), p);
+    v[0] += g.wgt1[k] * t;                   // oneel
+    v[1] += g.wgt1[k] * M(kin, p);           // kinetic (+ m^2 e term)
+    v[2] += g.wgt1[k] * M(M(p, g.f0[k]), p);  // nuclear
+    v[3] += g.wgt2[k] * M(M(p, coulp[k]), p);
+    v[4] += g.wgt2[k] * M(p, exchp[k]);
+  }
+  block_sum_store<5>(v, partials);
+}
+
+__global__ void k_eahf_final(const double *sums, double *ee_out, double *parts) {
+  if (threadIdx.x == 0) {
+    const double woneel = sums[0], wc = sums[3], wx = -sums[4];
+    *ee_out = woneel + (wc + wx);
+    if (parts) {
+      parts[0] = sums[1];
+      parts[1] = sums[2];
+      parts[2] = woneel;
+      parts[3] = wc;
+      parts[4] = wx;
+    }
+  }
+}
+
+struct TripleList {
+  TripleItem it[kMaxK];
+};
+
+__global__ void k_triples(GridDev g, TripleList L, int n, double *partials) {
+  double v[kMaxK];
+  for (int q = 0; q < kMaxK; ++q) v[q] = 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+    const int mu = k / g.nni, nu = k - mu * g.nni;
+    const int ij = (mu + 4) * g.n8 + nu + 4;
+    const double w = g.wgt2[k];
+    for (int q = 0; q < n; ++q) {
+      double t = M(L.it[q].a[ij], L.it[q].b[ij]);
+      if (L.it[q].c) t = M(t, L.it[q].c[ij]);
+      v[q] += w * t;
+    }
+  }
+  block_sum_store<kMaxK>(v, partials);
+}
+
+// coulMom (scfUtils.F90:490-603)
+__global__ void k_coulmom(GridDev g, const double *psi, int homo, double *partials) {
+  double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+    const int mu = k / g.nni, nu = k - mu * g.nni;
+    const double p = psi[(mu + 4) * g.n8 + nu + 4];
+    const double wk1 = M(M(p, p), g.f4[k]);
+    for (int q = 0; q < g.mpole; ++q) {
+      if (homo && (q % 2 == 0)) continue;
+      v[q] += g.wgt2[k] * M(g.leg[size_t(q) * g.mxsize + k], wk1);
+    }
+  }
+  block_sum_store<8>(v, partials);
+}
+
+// exchMom (scfUtils.F90:615-844): normalised P_k^q r^k evaluated on the fly
+__global__ void k_exchmom(GridDev g, const double *psa, const double *psb, int idel, double *partials) {
+  double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+    const int mu = k / g.nni, nu = k - mu * g.nni;
+    const int ij = (mu + 4) * g.n8 + nu + 4;
+    const double rr = sqrt(g.vxisq[mu] + g.vetasq[nu] - 1.0);
+    const double xrr = g.r2 * rr;
+    const double costh = (fabs(rr) > kPrecis) ? g.veta[nu] * g.vxi[mu] / rr : 0.0;
+    double dome[10];
+    assoc_legendre(idel, g.mpole, costh, dome, false);
+    const double wk1 = M(M(psa[ij], psb[ij]), g.f4[k]);
+    double xw = xrr;
+    for (int q = 0; q < g.mpole; ++q) {
+      if (q > 0) xw = xw * xrr;
+      v[q] += g.wgt2[k] * M(dome[q + 1] * xw, wk1);
+    }
+  }
+  block_sum_store<8>(v, partials);
+}
+
+inline int grid_blocks(int n) {
+  int b = (n + kThreads - 1) / kThreads;
+  return b < 1 ? 1 : (b > 1184 ? 1184 : b);
+}
+
+}  // namespace
+
+// ======================================================================
+// launchers
+// ======================================================================
+
+static double *reduction_partials(x2g_ctx *ctx, int K) {
+  size_t need = size_t(kRedBlocks) * K * sizeof(double) + 64 * sizeof(double);
+  if (ctx->red_bytes < need) {
+    if (ctx->red) cudaFree(ctx->red);
+    ctx->red = nullptr;
+    ctx->red_bytes = 0;
+    if (cudaMalloc(&ctx->red, need) != cudaSuccess) return nullptr;
+    ctx->red_bytes = need;
+  }
+  return static_cast<double *>(ctx->red);
+}
+
+int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, int nsweeps, int precision) {
+  if (njobs <= 0) return X2G_OK;
+  if (nsweeps <= 0) return set_status(X2G_ERR_ARG, "nsweeps must be positive");
+  const GridDev &g = grid->d;
+  const bool mixed = (precision == X2G_MIXED);
+  // device job table + per-job scratch
+  const size_t ext_bytes = size_t(g.next) * sizeof(double);
+  const size_t plain_bytes = size_t(g.mxsize) * sizeof(double);
+  const size_t per_job = mixed ? (size_t(g.next) * sizeof(float) + 2 * size_t(g.mxsize) * sizeof(float) + 256)
+                               : (plain_bytes + 256);
+  const size_t jobs_bytes = (sizeof(JobDev) * njobs + 255) / 256 * 256;
+  char *ws = static_cast<char *>(ctx_workspace(ctx, jobs_bytes + per_job * njobs + 256));
+  if (!ws) return set_status(X2G_ERR_ALLOC, "workspace allocation failed");
+  (void)ext_bytes;
+  std::vector<JobDev> h(njobs);
+  char *scratch = ws + jobs_bytes;
+  for (int i = 0; i < njobs; ++i) {
+    const x2g_job &x = jobs[i];
+    const bool explicit_lr = (x.lhs && x.rhs);
+    if (!x.u || (x.kind != 0 && x.kind != 1) || (x.kind == 0 && !explicit_lr) ||
+        (x.kind == 1 && !explicit_lr && (!x.psa || !x.psb)) || (x.isym != 1 && x.isym != -1))
+      return set_status(X2G_ERR_ARG, "bad relaxation job");
+    JobDev &d = h[i];
+    d.u = x.u;
+    d.lhs = x.lhs;
+    d.rhs = x.rhs;
+    d.psa = x.psa;
+    d.psb = x.psb;
+    d.omega = x.omega;
+    d.idel2 = double(x.idel * x.idel);
+    d.isym = x.isym;
+    // kind 0 orbital (borb); 1 potential built from psa/psb; 2 potential
+    // given explicit lhs/rhs arrays (bpot)
+    d.kind = (x.kind == 1 && explicit_lr) ? 2 : x.kind;
+    char *p = scratch + per_job * i;
+    if (mixed) {
+      d.e32 = reinterpret_cast<float *>(p);
+      d.r32 = reinterpret_cast<float *>(p + (size_t(g.next) * sizeof(float) + 127) / 128 * 128);
+      d.l32 = d.r32 + g.mxsize;
+      d.rhs_buf = nullptr;
+    } else {
+      d.rhs_buf = reinterpret_cast<double *>(p);
+      d.e32 = nullptr;
+      d.r32 = d.l32 = nullptr;
+    }
+  }
+  JobDev *djobs = reinterpret_cast<JobDev *>(ws);
+  cudaError_t err = cudaMemcpyAsync(djobs, h.data(), sizeof(JobDev) * njobs, cudaMemcpyHostToDevice, ctx->stream);
+  if (err != cudaSuccess) return cuda_status(err, "job table upload");
+  BarrierDev bar{ctx->bar, ctx->bar + 1, reinterpret_cast<int *>(ctx->bar + 2)};
+  err = cudaMemsetAsync(ctx->bar, 0, 4 * sizeof(unsigned), ctx->stream);
+  if (err != cudaSuccess) return cuda_status(err, "barrier reset");
+  const int nitems = njobs * g.ntiles;
+  if (mixed) {
+    dim3 gg(grid_blocks(g.nmu * 8 + 4 * g.nni), njobs);
+    k_ghost_jobs<<<gg, kThreads, 0, ctx->stream>>>(g, djobs);
+    dim3 gr(grid_blocks((g.nni - 2) * (g.nmu - 5)), njobs);
+    k_residual<<<gr, kThreads, 0, ctx->stream>>>(g, djobs);
+    ctx->launches += 2;
+  }
+  static int max_f64 = -1, max_f32 = -1;
+  int *pmax = mixed ? &max_f32 : &max_f64;
+  if (*pmax < 0) {
+    int per_sm = 0;
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, mixed ? (const void *)k_mcsor_f32 : (const void *)k_mcsor_f64, kThreads, 0);
+    if (err != cudaSuccess) return cuda_status(err, "occupancy query");
+    *pmax = per_sm * ctx->num_sms;
+  }
+  unsigned nblocks = unsigned(nitems < *pmax ? nitems : *pmax);
+  if (nblocks < 1) nblocks = 1;
+  int nj = njobs, ns = nsweeps;
+  GridDev gd = g;
+  void *args[] = {&gd, &djobs, &nj, &ns, &bar, &nblocks};
+  err = cudaLaunchCooperativeKernel(mixed ? (const void *)k_mcsor_f32 : (const void *)k_mcsor_f64, dim3(nblocks),
+                                    dim3(kThreads), args, 0, ctx->stream);
+  if (err != cudaSuccess) return cuda_status(err, "cooperative MCSOR launch");
+  ctx->launches += 1;
+  if (mixed) {
+    dim3 gu(grid_blocks((g.nni - 2) * (g.nmu - 5)), njobs);
+    k_update<<<gu, kThreads, 0, ctx->stream>>>(g, djobs);
+    k_extrap_jobs<<<njobs, kThreads, 0, ctx->stream>>>(g, djobs);
+    ctx->launches += 2;
+  }
+  // barrier error word: checked by the caller at its next synchronisation
+  return X2G_OK;
+}
+
+void launch_ghost_fill(x2g_ctx *ctx, const GridDev &g, double *u, int isym) {
+  k_ghost<<<grid_blocks(g.nmu * 8 + 4 * g.nni), kThreads, 0, ctx->stream>>>(g, u, isym);
+  ctx->launches++;
+}
+
+void launch_putin(x2g_ctx *ctx, const GridDev &g, int isym, const double *plain, double *ext) {
+  k_putin_interior<<<grid_blocks(g.mxsize), kThreads, 0, ctx->stream>>>(g, plain, ext);
+  k_ghost<<<grid_blocks(g.nmu * 8 + 4 * g.nni), kThreads, 0, ctx->stream>>>(g, ext, isym);
+  ctx->launches += 2;
+}
+
+void launch_putout(x2g_ctx *ctx, const GridDev &g, const double *ext, double *plain) {
+  k_putout<<<grid_blocks(g.mxsize), kThreads, 0, ctx->stream>>>(g, ext, plain);
+  ctx->launches++;
+}
+
+void launch_fock(x2g_ctx *ctx, const GridDev &g, const FockArgs &a) {
+  k_fock<<<grid_blocks(g.mxsize), kThreads, 0, ctx->stream>>>(g, a);
+  ctx->launches++;
+}
+
+void launch_asympt_get(x2g_ctx *ctx, const GridDev &g, const double *fa, double *edecay) {
+  k_asympt_get<<<grid_blocks(4 * g.nni), kThreads, 0, ctx->stream>>>(g, fa, edecay);
+  ctx->launches++;
+}
+
+void launch_asympt_set(x2g_ctx *ctx, const GridDev &g, double *psi, const double *edecay) {
+  k_asympt_set<<<grid_blocks(g.nni), kThreads, 0, ctx->stream>>>(g, psi, edecay);
+  ctx->launches++;
+}
+
+void launch_setci(x2g_ctx *ctx, const GridDev &g, double *psi, int ihomo) {
+  k_setci<<<grid_blocks((g.nni / 2) * g.nmu), kThreads, 0, ctx->stream>>>(g, psi, ihomo);
+  ctx->launches++;
+}
+
+void launch_scale(x2g_ctx *ctx, const GridDev &g, double *psi, const double *norm_dev) {
+  k_scale<<<grid_blocks(g.mxsize), kThreads, 0, ctx->stream>>>(g, psi, norm_dev);
+  ctx->launches++;
+}
+
+void launch_ortho_apply(x2g_ctx *ctx, const GridDev &g, double *psi, const double *const *others, int n,
+                        const double *ovl_dev) {
+  PtrList L{};
+  for (int q = 0; q < n && q < kMaxTerms; ++q) L.p[q] = others[q];
+  k_ortho_apply<<<grid_blocks(g.mxsize), kThreads, 0, ctx->stream>>>(g, psi, L, n, ovl_dev);
+  ctx->launches++;
+}
+
+void launch_asympt(x2g_ctx *ctx, const GridDev &g, const AsymptArgs &a) {
+  if (a.n <= 0) return;
+  dim3 gg(grid_blocks(4 * g.nni), a.n);
+  k_asympt<<<gg, kThreads, 0, ctx->stream>>>(g, a);
+  ctx->launches++;
+}
+
+void launch_zero(x2g_ctx *ctx, double *p, size_t n) {
+  k_zero<<<grid_blocks(int(n < (1u << 30) ? n : (1u << 30))), kThreads, 0, ctx->stream>>>(p, n);
+  ctx->launches++;
+}
+
+void launch_norm(x2g_ctx *ctx, const GridDev &g, const double *psi, double *out) {
+  double *part = reduction_partials(ctx, 1);
+  k_norm<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psi, part);
+  k_reduce_final<1><<<1, kThreads, 0, ctx->stream>>>(part, kRedBlocks, out, 1);
+  ctx->launches += 2;
+}
+
+void launch_overlaps(x2g_ctx *ctx, const GridDev &g, const double *psi, const double *const *others, int n,
+                     double *out) {
+  double *part = reduction_partials(ctx, kMaxK);
+  for (int b = 0; b < n; b += kMaxK) {
+    const int m = (n - b < kMaxK) ? n - b : kMaxK;
+    PtrList L{};
+    for (int q = 0; q < m; ++q) L.p[q] = others[b + q];
+    k_overlaps<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psi, L, m, part);
+    k_reduce_final<kMaxK><<<1, kThreads, 0, ctx->stream>>>(part, kRedBlocks, out + b, m);
+    ctx->launches += 2;
+  }
+}
+
+void launch_eahf(x2g_ctx *ctx, const GridDev &g, const double *psi, int m, const double *coulp,
+                 const double *exchp, double *ee_out, double *parts) {
+  double *part = reduction_partials(ctx, 5);
+  double *sums = part + size_t(kRedBlocks) * 5;
+  k_eahf<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psi, m, coulp, exchp, part);
+  k_reduce_final<5><<<1, kThreads, 0, ctx->stream>>>(part, kRedBlocks, sums, 5);
+  k_eahf_final<<<1, 32, 0, ctx->stream>>>(sums, ee_out, parts);
+  ctx->launches += 3;
+}
+
+void launch_triples(x2g_ctx *ctx, const GridDev &g, const TripleItem *items, int n, double *out) {
+  double *part = reduction_partials(ctx, kMaxK);
+  for (int b = 0; b < n; b += kMaxK) {
+    const int m = (n - b < kMaxK) ? n - b : kMaxK;
+    TripleList L{};
+    for (int q = 0; q < m; ++q) L.it[q] = items[b + q];
+    k_triples<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, L, m, part);
+    k_reduce_final<kMaxK><<<1, kThreads, 0, ctx->stream>>>(part, kRedBlocks, out + b, m);
+    ctx->launches += 2;
+  }
+}
+
+void launch_coulmom(x2g_ctx *ctx, const GridDev &g, const double *psi, int homo, double *out) {
+  double *part = reduction_partials(ctx, 8);
+  k_coulmom<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psi, homo, part);
+  k_reduce_final<8><<<1, kThreads, 0, ctx->stream>>>(part, kRedBlocks, out, g.mpole);
+  ctx->launches += 2;
+}
+
+void launch_exchmom(x2g_ctx *ctx, const GridDev &g, const double *psa, const double *psb, int idel, double *out) {
+  double *part = reduction_partials(ctx, 8);
+  k_exchmom<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psa, psb, idel, part);
+  k_reduce_final<8><<<1, kThreads, 0, ctx->stream>>>(part, kRedBlocks, out, g.mpole);
+  ctx->launches += 2;
+}
+
+}  // namespace x2g

@@ -1,0 +1,90 @@
+// Kernel launchers of the x2dhf GB300 library (implemented in x2g_kernels.cu).
+#pragma once
+
+#include "x2g_internal.h"
+
+namespace x2g {
+
+constexpr int kMaxTerms = 36;  // orbitals in one Fock build (MAXORB)
+
+// One term of the Fock potential of orbital iorb (src/fock.F90:102-160).
+struct FockTerm {
+  const double *coul;  // Coulomb potential of orbital iorb1 (ext)
+  const double *ex;    // exchange potential K(iorb,iorb1) (ext), or null
+  const double *ex2;   // second exchange potential (ilc2 == 2), or null
+  const double *psi;   // orbital iorb1 (ext)
+  double coo;          // occupation weight of the Coulomb term
+  double gec, gec2;    // exchange weights (initExWeights)
+  int mode;            // 0: iorb1 != iorb, 1: self term with m > 0 exchange, 2: self, no exchange
+  int pad;
+};
+
+struct FockArgs {
+  int nterms;
+  int m;        // |lambda| of iorb
+  int nel1;     // one-electron case: fockHF returns before the two-electron part
+  int pad;
+  const double *ee;  // device: diagonal Lagrange multiplier of iorb
+  double *lhs, *rhs; // plain outputs: fock1 + diag, fock2
+  double *coulp, *exchp;  // plain: coulombptr, exchangeptr of iorb
+  double *fa;        // 5 x nni: fock1/f1 on mu = nmu-5..nmu-1
+  FockTerm t[kMaxTerms];
+};
+
+// Asymptotic boundary values (potAsympt, src/scfUtils.F90:179-329).
+struct AsymptItem {
+  double *pot;  // ext array
+  int type;     // 0 Coulomb (cmulti of orbital `idx`), 1 exchange (moments slot `idx`)
+  int idx;
+  int idel;
+  int pad;
+};
+constexpr int kMaxAsympt = 80;
+struct AsymptArgs {
+  int n;
+  int norb;
+  const double *cmulti;  // [norb][8] Coulomb moments
+  const double *excm;    // [nslots][8] exchange moments
+  int nslots;
+  int pad;
+  AsymptItem it[kMaxAsympt];
+};
+
+// ---- sweeps ----
+int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, int nsweeps, int precision);
+
+// ---- elementwise ----
+void launch_ghost_fill(x2g_ctx *ctx, const GridDev &g, double *u, int isym);           // putin ghosts, all rows
+void launch_putin(x2g_ctx *ctx, const GridDev &g, int isym, const double *plain, double *ext);
+void launch_putout(x2g_ctx *ctx, const GridDev &g, const double *ext, double *plain);
+void launch_fock(x2g_ctx *ctx, const GridDev &g, const FockArgs &a);
+void launch_asympt_get(x2g_ctx *ctx, const GridDev &g, const double *fa, double *edecay);
+void launch_asympt_set(x2g_ctx *ctx, const GridDev &g, double *psi, const double *edecay);
+void launch_setci(x2g_ctx *ctx, const GridDev &g, double *psi, int ihomo);
+void launch_scale(x2g_ctx *ctx, const GridDev &g, double *psi, const double *norm_dev);
+void launch_ortho_apply(x2g_ctx *ctx, const GridDev &g, double *psi, const double *const *others, int n,
+                        const double *ovl_dev);
+void launch_asympt(x2g_ctx *ctx, const GridDev &g, const AsymptArgs &a);
+void launch_zero(x2g_ctx *ctx, double *p, size_t n);
+
+// ---- reductions (deterministic two-pass; results in device memory) ----
+// norm: out[0] = sum wgt2 psi psi f4
+void launch_norm(x2g_ctx *ctx, const GridDev &g, const double *psi, double *out);
+// overlaps with n other orbitals: out[k] = sum wgt2 psi o_k f4
+void launch_overlaps(x2g_ctx *ctx, const GridDev &g, const double *psi, const double *const *others, int n,
+                     double *out);
+// EaHF: out = woneel + (wcoul + wexch); psi must have ghosts filled.
+// Also writes parts[0..4] = kinetic, nuclear, oneel, coul, exch.
+void launch_eahf(x2g_ctx *ctx, const GridDev &g, const double *psi, int m, const double *coulp,
+                 const double *exchp, double *ee_out, double *parts);
+// generic weighted triple products: out[k] = sum w * a_k * b_k * c_k (c may be null), w = wgt2
+struct TripleItem {
+  const double *a, *b, *c;  // a,b ext arrays; c ext or null
+};
+void launch_triples(x2g_ctx *ctx, const GridDev &g, const TripleItem *items, int n, double *out);
+// multipole moments
+void launch_coulmom(x2g_ctx *ctx, const GridDev &g, const double *psi, int homo, double *out /*[mpole]*/);
+void launch_exchmom(x2g_ctx *ctx, const GridDev &g, const double *psa, const double *psb, int idel,
+                    double *out /*[mpole]*/);
+
+}  // namespace x2g

@@ -1,0 +1,952 @@
+// Device-resident closed-shell HF SCF of x2dhf (src/doSCF.F90 prepSCF:24,
+// scf:211, relaxDriver:943).  Orbitals, Coulomb and exchange potentials live
+// on the GPU in the extended layout for the whole run; the host keeps only
+// the scalar control of the reference's SCF loop and reads back a few
+// scalars (orbital energies, norms, overlaps) once per SCF iteration.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "x2g_kernels.cuh"
+
+using namespace x2g;
+
+namespace {
+
+constexpr int MAXO = X2G_MAXORB;
+
+struct Rec {
+  int iscf, iorb;
+  double ee, dee, dnorm;
+};
+
+// one potential of an orbital's relaxation batch (initAddr:1339-1461)
+struct PotSlot {
+  int in1, in2, idel, isym;
+  double *target;  // ext array
+};
+
+}  // namespace
+
+struct x2g_scf {
+  x2g_ctx *ctx = nullptr;
+  x2g_grid *grid = nullptr;
+  x2g_case cs{};
+  int norb = 0, nel = 0, mpole = 4, nslots = 0;
+  int m[MAXO + 1]{}, isymOrb[MAXO + 1]{}, ihomo[MAXO + 1]{}, ige[MAXO + 1]{};
+  double occ[MAXO + 1]{};
+  double gec[2 * MAXO * MAXO + 1]{};
+  int k2[MAXO + 1][MAXO + 1]{}, ilc2[MAXO + 1][MAXO + 1]{};
+  std::vector<int> ilc;
+  std::vector<double *> orb, coul, coulp, exchp, exch;  // device arrays
+  double *lhs = nullptr, *rhs = nullptr, *fa = nullptr, *edecay = nullptr;
+  double *sc = nullptr;  // device scalars
+  // scalar block offsets (doubles)
+  enum { O_EE = 0, O_NORM = 64, O_OVL = 128, O_CM = 128 + 64 * 64, O_EX = O_CM + 64 * 8 };
+  size_t sc_count = 0;
+  std::vector<double> hsc;
+  std::vector<std::vector<PotSlot>> pots;
+  // exchange-moment list (initLP:1592-1626)
+  std::vector<int> mm_i1, mm_i2, mm_idel, mm_ipc;
+  std::vector<void *> allocs;
+  double omega_orb = 0, omega_pot = 0;
+  // SCF control (doSCF.F90:211-886)
+  int started = 0, done = 0, iscf = 0, converged = 0;
+  int ifixorb[MAXO + 1]{}, itouch[MAXO + 1]{};
+  int lfixorb = 0, lfixorb4init = 0;
+  double ee[MAXO + 1]{}, eeOld[MAXO + 1]{}, deltaee[MAXO + 1]{}, orbNorm[MAXO + 1]{}, wst[MAXO + 1]{};
+  double deltaeeMax = 100, deltaNormMax = 100, eeconv = 10, eeconvprev = 1e35, dnmaxprev = 1e35, demax1 = 100;
+  double orbEnergyThld = 0, orbNormThld = 0, thren4init = 0;
+  int nresets = 0, nresets4no = 0, nOrbEnergyThld = 0, nOrbNormThld = 0, noenergydec = 0, nonormdec = 0;
+  int lenergyThld = 0, lnormThld = 0;
+  long nsor4orb = 0, nsor4pot = 0;
+  double etot = 0, evt = 0, virial = 0;
+  std::vector<Rec> recs;
+  int last_error = 0;
+};
+
+namespace {
+
+double *dalloc(x2g_scf *s, size_t n) {
+  void *p = nullptr;
+  if (cudaMalloc(&p, n * sizeof(double)) != cudaSuccess) return nullptr;
+  cudaMemset(p, 0, n * sizeof(double));
+  s->allocs.push_back(p);
+  return static_cast<double *>(p);
+}
+
+// ---------------------------------------------------------------------
+// hydrogenic start (initOrbitalsPotentials.F90:714-934) and initial
+// potentials (coulombExchangePotentials.f90:14-239), evaluated on the host
+// ---------------------------------------------------------------------
+double factorial(int n) {
+  double f = 1.0;
+  for (int i = 1; i <= n; i++) f = double(i) * f;
+  return f;
+}
+
+double hyp1f1(int np, int lp, double x) {  // utils.f90:265-282
+  double h = 1.0;
+  if (-np == 0) return h;
+  double t = double(np) * x / double(lp);
+  h = h + t;
+  for (int i = 2; i <= -np; i++) {
+    t = t * x * double(np + i - 1) / double(lp + i - 1) / double(i);
+    h = h + t;
+  }
+  return h;
+}
+
+double hyp2f1(int na, int nb, int nc, double x) {  // utils.f90:289-309
+  double h = 1.0;
+  if (na == 0) return h;
+  double a = na, b = nb, c = nc;
+  double t = a * b * x / c;
+  h = h + t;
+  for (int i = 2; i <= -na; i++) {
+    t = t * x * (a + double(i - 1)) * (b + double(i - 1)) / (c + double(i - 1)) / double(i);
+    h = h + t;
+  }
+  return h;
+}
+
+// associated Legendre as evaluated by plegendg (utils.f90:315-335); its
+// prefactor is written (-one**m), i.e. always -1 in Fortran precedence
+double plegendre(int l, int m, double c) {
+  double ct = std::fabs(1.0 - c * c);
+  if (m == 0) return hyp2f1(-l, l + 1, 1, (1.0 - c) / 2.0);
+  if (ct < kPrecis) return 0.0;
+  double fn0 = -std::pow(1.0, double(m)) * factorial(l + m) / factorial(l - m) / factorial(m) / std::pow(2.0, double(m));
+  return hyp2f1(m - l, m + l + 1, m + 1, (1.0 - c) / 2.0) * (fn0 * std::pow(ct, double(m) / 2.0));
+}
+
+double hydrogenic(const HostGrid &g, int n, int l, int m, double z, bool centre_b, int i, int j) {
+  const double r = g.r;
+  double fn = std::pow(2.0 * z / double(n), 3.0 / 2.0 + double(l)) *
+              std::sqrt(factorial(n + l) / (2.0 * double(n) * factorial(n - l - 1))) / factorial(2 * l + 1);
+  double shn = (m == 0 ? 1.0 : std::pow(-1.0, double(m))) / std::sqrt(4.0 * kPi) *
+               std::sqrt((2.0 * l + 1.0) * factorial(l - m) / factorial(l + m));
+  double z0 = (r / 2.0) * g.vxi[i] * g.veta[j];
+  double rt, c;
+  if (!centre_b) {
+    rt = (r / 2.0) * (g.vxi[i] + g.veta[j]);
+    c = (rt < kPrecis) ? -1.0 : std::min(1.0, std::max(-1.0, (z0 + r / 2.0) / rt));
+  } else {
+    rt = (r / 2.0) * (g.vxi[i] - g.veta[j]);
+    c = (rt < kPrecis) ? -1.0 : std::min(1.0, std::max(-1.0, -(z0 - r / 2.0) / rt));
+  }
+  int np = n - l - 1, lp = 2 * l + 2;
+  double x = z * rt / double(n);
+  double lag = std::pow(rt, double(l)) * std::exp(-x) * hyp1f1(-np, lp, x + x);
+  return fn * lag * shn * plegendre(l, m, c);
+}
+
+double thomas_fermi(double r, double veta, double vxi) {  // pottf, coulombExchangePotentials.f90:222-239
+  if (std::fabs(vxi + veta) < kPrecis) return 0.0;
+  double rab = r * (vxi + veta) / 2.0;
+  double w = std::sqrt(rab / 0.885340);
+  double t = w * (0.6011200 * w + 1.8106100) + 1.0;
+  w = w * (w * (w * (w * (0.0479300 * w + 0.2146500) + 0.7711200) + 1.3951500) + 1.8106100) + 1.0;
+  return (1.0 - (t / w) * (t / w)) / rab;
+}
+
+int upload_ext(x2g_scf *s, double *dst, const std::vector<double> &plain) {
+  const HostGrid &g = s->grid->h;
+  std::vector<double> ext(g.next, 0.0);
+  for (int i = 0; i < g.nmu; i++)
+    for (int j = 0; j < g.nni; j++) ext[(i + 4) * g.n8 + j + 4] = plain[i * g.nni + j];
+  cudaError_t e = cudaMemcpy(dst, ext.data(), ext.size() * sizeof(double), cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? X2G_OK : cuda_status(e, "initial guess upload");
+}
+
+int initial_guess(x2g_scf *s) {
+  const HostGrid &g = s->grid->h;
+  const x2g_case &c = s->cs;
+  const int mx = g.mxsize;
+  std::vector<double> psi(mx), tmp(mx);
+  for (int o = 1; o <= s->norb; o++) {
+    const int k = o - 1;
+    std::fill(psi.begin(), psi.end(), 0.0);
+    for (int pass = 0; pass < 2; pass++) {
+      double co = pass ? c.co2[k] : c.co1[k];
+      if (!(std::fabs(co) > kPrecis)) continue;
+      int n = pass ? c.n2[k] : c.n1[k], l = pass ? c.l2[k] : c.l1[k];
+      double z = pass ? c.zb[k] : c.za[k];
+      for (int i = 0; i < g.nmu; i++)
+        for (int j = 0; j < g.nni; j++) tmp[i * g.nni + j] = hydrogenic(g, n, l, s->m[o], z, pass == 1, i, j);
+      for (int q = 0; q < mx; q++) psi[q] = co * tmp[q] + psi[q];
+    }
+    int rc = upload_ext(s, s->orb[o], psi);
+    if (rc) return rc;
+  }
+  const int iz1 = int(std::lround(g.z1)), iz2 = int(std::lround(g.z2));
+  for (int o = 1; o <= s->norb; o++) {
+    const int k = o - 1;
+    double crt1 = std::fabs(c.co1[k]), crt2 = std::fabs(c.co2[k]);
+    for (int i = 0; i < g.nmu; i++)
+      for (int j = 0; j < g.nni; j++) {
+        double v;
+        if (i == 0 && (j == 0 || j == g.nni - 1))
+          v = 0.0;
+        else if (iz1 != 0 && iz2 != 0)
+          v = -1.0 * thomas_fermi(g.r, g.veta[j], g.vxi[i]) * crt1 + -1.0 * thomas_fermi(g.r, -g.veta[j], g.vxi[i]) * crt2;
+        else
+          v = -1.0 * thomas_fermi(g.r, g.veta[j], g.vxi[i]) * crt1;
+        psi[i * g.nni + j] = v * g.f4[i * g.nni + j];
+      }
+    int rc = upload_ext(s, s->coul[o], psi);
+    if (rc) return rc;
+  }
+  for (int i1 = 1; i1 <= s->norb; i1++)
+    for (int i2 = i1; i2 <= s->norb; i2++) {
+      if (i1 == i2 && s->m[i2] == 0) continue;
+      const int kk = s->k2[i1][i2];
+      std::fill(psi.begin(), psi.end(), 0.0);
+      for (int i = 1; i < g.nmu; i++)
+        for (int j = 1; j < g.nni - 1; j++) {
+          double ra1 = (g.r / 2.0) * (g.vxi[i] + g.veta[j]), ra2 = (g.r / 2.0) * (g.vxi[i] - g.veta[j]);
+          double v = (ra1 > 1.0e-8) ? c.co1[i1 - 1] / ra1 : 0.0;
+          if (ra2 > 1.0e-8) v = v + c.co2[i1 - 1] / ra2;
+          psi[i * g.nni + j] = v;
+        }
+      for (int q = 0; q < mx; q++) psi[q] = psi[q] * g.f4[q];
+      int rc = upload_ext(s, s->exch[2 * kk], psi);
+      if (rc) return rc;
+      if (i1 != i2 && s->m[i1] != 0 && s->m[i2] != 0) {
+        rc = upload_ext(s, s->exch[2 * kk + 1], psi);
+        if (rc) return rc;
+      }
+    }
+  return X2G_OK;
+}
+
+// exchange weights of a closed-shell configuration (initExWeights:3303-3436)
+void exchange_weights(x2g_scf *s) {
+  const int norb = s->norb, isu2 = norb * norb;
+  char spn[4 * MAXO + 1];
+  int iloop[MAXO + 1], iqm[4 * MAXO + 1];
+  for (int i = 1; i <= norb; i++) {
+    int is = 4 * (i - 1);
+    iloop[i] = 2;
+    iqm[1 + is] = 1;
+    iqm[2 + is] = 1;
+    spn[is + 1] = '+';
+    spn[is + 2] = '-';
+    spn[is + 3] = ' ';
+    spn[is + 4] = ' ';
+    if (s->m[i] > 0) {
+      iloop[i] = 4;
+      iqm[3 + is] = -1;
+      iqm[4 + is] = -1;
+      spn[is + 3] = '+';
+      spn[is + 4] = '-';
+    }
+  }
+  std::fill(std::begin(s->gec), std::end(s->gec), 0.0);
+  for (int i = 1; i <= norb; i++) {
+    int ixx = 4 * (i - 1);
+    double div = 0.0;
+    for (int ii = 1; ii <= iloop[i]; ii++) {
+      int ix = ii + ixx;
+      div += 1.0;
+      for (int j = 1; j <= norb; j++) {
+        int jxx = 4 * (j - 1), kk = i + norb * (j - 1);
+        int mpl = std::abs(s->m[i] - s->m[j]), mmi = std::abs(s->m[i] + s->m[j]);
+        for (int jj = 1; jj <= iloop[j]; jj++) {
+          int jx = jxx + jj;
+          if (mpl == mmi && spn[ix] == spn[jx] && i != j) s->gec[kk] += 1.0;
+          if (mpl != mmi && spn[ix] == spn[jx]) {
+            if (i == j && iqm[ix] != iqm[jx]) s->gec[kk] += 1.0;
+            if (i != j && iqm[ix] == iqm[jx]) s->gec[kk] += 1.0;
+            if (i != j && iqm[ix] != iqm[jx]) s->gec[kk + isu2] += 1.0;
+          }
+        }
+      }
+    }
+    for (int idiv = 1; idiv <= norb; idiv++) {
+      int kk = i + norb * (idiv - 1);
+      s->gec[kk] = s->gec[kk] / div;
+      s->gec[kk + isu2] = s->gec[kk + isu2] / div;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------
+// device operations of one SCF step
+// ---------------------------------------------------------------------
+int fock(x2g_scf *s, int iorb) {
+  const GridDev &g = s->grid->d;
+  FockArgs a{};
+  a.m = s->m[iorb];
+  a.nel1 = (s->nel == 1);
+  a.ee = s->sc + x2g_scf::O_EE + iorb;
+  a.lhs = s->lhs;
+  a.rhs = s->rhs;
+  a.coulp = s->coulp[iorb];
+  a.exchp = s->exchp[iorb];
+  a.fa = s->fa;
+  int n = 0;
+  for (int j = 1; j <= s->norb; j++) {
+    FockTerm &t = a.t[n++];
+    t.coul = s->coul[j];
+    t.coo = s->occ[j] - (j == iorb ? 1.0 : 0.0);
+    const int kex = iorb + (j - 1) * s->norb;
+    t.psi = s->orb[j];
+    t.gec = s->gec[kex];
+    t.gec2 = s->gec[kex + s->norb * s->norb];
+    const int kp = s->k2[iorb][j];
+    if (j != iorb) {
+      t.mode = 0;
+      t.ex = s->exch[2 * kp];
+      t.ex2 = (s->ilc2[iorb][j] == 2) ? s->exch[2 * kp + 1] : nullptr;
+    } else if (s->m[iorb] > 0 && s->ilc2[iorb][j] > 0) {
+      t.mode = 1;
+      t.ex = s->exch[2 * kp];
+      t.ex2 = nullptr;
+    } else {
+      t.mode = 2;
+      t.ex = t.ex2 = nullptr;
+    }
+  }
+  a.nterms = n;
+  launch_fock(s->ctx, g, a);
+  return X2G_OK;
+}
+
+int relax_potentials(x2g_scf *s, int iorb) {
+  const auto &P = s->pots[iorb];
+  std::vector<x2g_job> jobs(P.size());
+  for (size_t k = 0; k < P.size(); k++) {
+    x2g_job &j = jobs[k];
+    j.u = P[k].target;
+    j.psa = s->orb[P[k].in1];
+    j.psb = s->orb[P[k].in2];
+    j.omega = s->omega_pot;
+    j.isym = P[k].isym;
+    j.idel = P[k].idel;
+    j.kind = 1;
+  }
+  s->nsor4pot += long(P.size()) * s->cs.maxsor_pot;
+  return launch_relax(s->ctx, s->grid, jobs.data(), int(jobs.size()), s->cs.maxsor_pot, s->cs.precision);
+}
+
+int relax_orbital(x2g_scf *s, int iorb) {
+  const GridDev &g = s->grid->d;
+  fock(s, iorb);
+  launch_asympt_get(s->ctx, g, s->fa, s->edecay);
+  x2g_job j{};
+  j.u = s->orb[iorb];
+  j.lhs = s->lhs;
+  j.rhs = s->rhs;
+  j.omega = s->omega_orb;
+  j.isym = s->isymOrb[iorb];
+  j.kind = 0;
+  s->nsor4orb += s->cs.maxsor_orb;
+  int rc = launch_relax(s->ctx, s->grid, &j, 1, s->cs.maxsor_orb, s->cs.precision);
+  if (rc) return rc;
+  launch_asympt_set(s->ctx, g, s->orb[iorb], s->edecay);
+  return X2G_OK;
+}
+
+void norm(x2g_scf *s, int iorb) {
+  double *out = s->sc + x2g_scf::O_NORM + iorb;
+  launch_norm(s->ctx, s->grid->d, s->orb[iorb], out);
+  launch_scale(s->ctx, s->grid->d, s->orb[iorb], out);
+}
+
+// lower orbitals of the same symmetry (normOrtho.F90:124-131)
+std::vector<int> ortho_partners(x2g_scf *s, int iorb1) {
+  std::vector<int> v;
+  for (int iorb2 = 1; iorb2 <= s->norb; iorb2++) {
+    int iorb3 = s->norb - iorb2 + 1;
+    if (iorb3 <= iorb1) continue;
+    if (s->m[iorb3] != s->m[iorb1]) continue;
+    if (s->ige[iorb3] != s->ige[iorb1] && !(s->cs.homonuclear == 0 && false)) {
+      if (s->ige[iorb3] != s->ige[iorb1]) continue;
+    }
+    v.push_back(iorb3);
+  }
+  return v;
+}
+
+void ortho(x2g_scf *s, int iorb) {
+  std::vector<int> p = ortho_partners(s, iorb);
+  if (p.empty()) return;
+  std::vector<const double *> o;
+  for (int q : p) o.push_back(s->orb[q]);
+  double *ovl = s->sc + x2g_scf::O_OVL + 64 * iorb;
+  launch_overlaps(s->ctx, s->grid->d, s->orb[iorb], o.data(), int(o.size()), ovl);
+  launch_ortho_apply(s->ctx, s->grid->d, s->orb[iorb], o.data(), int(o.size()), ovl);
+}
+
+void eahf(x2g_scf *s, int iorb, double *ee_out, double *parts) {
+  const GridDev &g = s->grid->d;
+  launch_ghost_fill(s->ctx, g, s->orb[iorb], s->isymOrb[iorb]);
+  launch_eahf(s->ctx, g, s->orb[iorb], s->m[iorb], s->coulp[iorb], s->exchp[iorb], ee_out, parts);
+}
+
+void mpole_moments(x2g_scf *s) {
+  if (s->nel == 1) return;
+  const GridDev &g = s->grid->d;
+  const int homo = s->cs.homonuclear;
+  for (int i = 1; i <= s->norb; i++) {
+    if (!s->itouch[i]) continue;
+    launch_coulmom(s->ctx, g, s->orb[i], homo, s->sc + x2g_scf::O_CM + 8 * (i - 1));
+  }
+  for (size_t q = 0; q < s->mm_i1.size(); q++)
+    launch_exchmom(s->ctx, g, s->orb[s->mm_i1[q]], s->orb[s->mm_i2[q]], s->mm_idel[q],
+                   s->sc + x2g_scf::O_EX + 8 * s->mm_ipc[q]);
+}
+
+void pot_asympt(x2g_scf *s, int iorb1) {
+  AsymptArgs a{};
+  a.norb = s->norb;
+  a.cmulti = s->sc + x2g_scf::O_CM;
+  a.excm = s->sc + x2g_scf::O_EX;
+  a.nslots = s->nslots;
+  int n = 0;
+  if (s->itouch[iorb1] == 1) a.it[n++] = AsymptItem{s->coul[iorb1], 0, iorb1 - 1, 0, 0};
+  for (int iorb2 = 1; iorb2 <= s->norb; iorb2++) {
+    if (!s->itouch[iorb1] && !s->itouch[iorb2]) continue;
+    int k = s->k2[iorb1][iorb2];
+    if (k == 0 || s->ilc[k] == 0) continue;
+    int idel = std::abs(s->m[iorb1] - s->m[iorb2]);
+    if (iorb1 == iorb2) idel = 2 * s->m[iorb1];
+    a.it[n++] = AsymptItem{s->exch[2 * k], 1, k, idel, 0};
+    if (s->ilc[k] == 2)
+      a.it[n++] = AsymptItem{s->exch[2 * k + 1], 1, k + s->norb * (s->norb + 1) / 2,
+                             s->m[iorb2] + s->m[iorb1], 0};
+  }
+  a.n = n;
+  launch_asympt(s->ctx, s->grid->d, a);
+}
+
+// total energy (totalEnergy.F90:13-245)
+int etotal(x2g_scf *s) {
+  const GridDev &g = s->grid->d;
+  const int norb = s->norb;
+  double *parts = s->sc + x2g_scf::O_OVL + 64 * 40;  // scratch region after the overlaps
+  double *eedummy = parts + 5 * (MAXO + 1);
+  for (int i = 1; i <= norb; i++) eahf(s, i, eedummy, parts + 5 * i);
+  std::vector<TripleItem> items;
+  std::vector<int> kind;  // 0 coulij(i,i) 1 coulij(i2,i1) 2 exch self 3 exch type0 4 exch type1
+  std::vector<std::pair<int, int>> who;
+  for (int i = 1; i <= norb; i++)
+    if (s->occ[i] > 1.0) {
+      items.push_back({s->orb[i], s->coul[i], s->orb[i]});
+      kind.push_back(0);
+      who.push_back({i, i});
+    }
+  for (int i1 = 1; i1 <= norb; i1++) {
+    if (s->m[i1] > 0 && std::fabs(s->occ[i1] - 1.0) > 1e-7) {
+      int k = s->k2[i1][i1];
+      items.push_back({s->orb[i1], s->exch[2 * k], s->orb[i1]});
+      kind.push_back(2);
+      who.push_back({i1, i1});
+    }
+    for (int i2 = i1 + 1; i2 <= norb; i2++) {
+      items.push_back({s->orb[i1], s->coul[i2], s->orb[i1]});
+      kind.push_back(1);
+      who.push_back({i1, i2});
+      int k = s->k2[i1][i2];
+      items.push_back({s->orb[i1], s->exch[2 * k], s->orb[i2]});
+      kind.push_back(3);
+      who.push_back({i1, i2});
+      if (s->ilc2[i1][i2] == 2) {
+        items.push_back({s->orb[i1], s->exch[2 * k + 1], s->orb[i2]});
+        kind.push_back(4);
+        who.push_back({i1, i2});
+      }
+    }
+  }
+  double *out = s->sc + s->sc_count - 1024;
+  if (!items.empty()) launch_triples(s->ctx, g, items.data(), int(items.size()), out);
+  std::vector<double> hp(5 * (MAXO + 1)), ho(items.size() + 1);
+  cudaMemcpyAsync(hp.data(), parts, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, s->ctx->stream);
+  if (!items.empty())
+    cudaMemcpyAsync(ho.data(), out, items.size() * sizeof(double), cudaMemcpyDeviceToHost, s->ctx->stream);
+  int rc = x2g_synchronize(s->ctx);
+  if (rc) return rc;
+  // spin-pair counts for closed shells (exchContribs.f90 excont/exint)
+  auto excont = [&](int a, int b, double &ox1, double &ox2) {
+    int pa = s->m[a], pb = s->m[b];
+    ox1 = ox2 = 0;
+    if (pa == 0 || pb == 0) {
+      ox1 = (pa == 0 && pb == 0) ? 2.0 : 4.0;
+    } else {
+      ox1 = 2.0 + 2.0;
+      ox2 = 2.0 + 2.0;
+    }
+  };
+  double woneel = 0, vkt = 0, vnt = 0, wdcoul = 0, wndc = 0, wex1 = 0, wex2 = 0;
+  for (int i = 1; i <= norb; i++) {
+    woneel = woneel + s->occ[i] * hp[5 * i + 2];
+    vkt = vkt + s->occ[i] * hp[5 * i + 0];
+    vnt = vnt + s->occ[i] * hp[5 * i + 1];
+  }
+  size_t q = 0;
+  for (int i = 1; i <= norb; i++)
+    if (s->occ[i] > 1.0) {
+      wdcoul = wdcoul + s->occ[i] * (s->occ[i] - 1.0) * ho[q] / 2.0;
+      q++;
+    }
+  for (; q < items.size(); q++) {
+    int i1 = who[q].first, i2 = who[q].second;
+    if (kind[q] == 2) {
+      wex1 = wex1 + 2.0 * ho[q];  // exint: 2 same-spin pairs in a closed non-sigma shell
+    } else if (kind[q] == 1) {
+      wndc = wndc + s->occ[i1] * s->occ[i2] * ho[q];
+    } else if (kind[q] == 3) {
+      double ox1, ox2;
+      excont(i1, i2, ox1, ox2);
+      wex1 = wex1 + ox1 * ho[q];
+    } else if (kind[q] == 4) {
+      double ox1, ox2;
+      excont(i1, i2, ox1, ox2);
+      wex2 = wex2 + ox2 * ho[q];
+    }
+  }
+  const double z1 = s->grid->h.z1, z2 = s->grid->h.z2, r = s->grid->h.r;
+  s->evt = woneel + wdcoul + wndc - wex1 - wex2;
+  double epott = vnt + wdcoul + wndc - wex1 - wex2;
+  s->virial = (epott + z1 * z2 / r) / vkt;
+  s->etot = s->evt + z1 * z2 / r;
+  return X2G_OK;
+}
+
+int read_scalars(x2g_scf *s) {
+  cudaError_t e = cudaMemcpyAsync(s->hsc.data(), s->sc, size_t(x2g_scf::O_CM) * sizeof(double),
+                                  cudaMemcpyDeviceToHost, s->ctx->stream);
+  if (e != cudaSuccess) return cuda_status(e, "scalar readback");
+  int rc = x2g_synchronize(s->ctx);
+  if (rc) return rc;
+  for (int i = 1; i <= s->norb; i++) {
+    s->ee[i] = s->hsc[x2g_scf::O_EE + i];
+    s->orbNorm[i] = s->hsc[x2g_scf::O_NORM + i];
+    if (std::isnan(s->ee[i]) || std::isnan(s->orbNorm[i])) return set_status(X2G_ERR_NAN, "NaN in orbital energy");
+  }
+  return X2G_OK;
+}
+
+void update_wst(x2g_scf *s, int iorb) {
+  std::vector<int> p = ortho_partners(s, iorb);
+  double w = 0;
+  for (size_t q = 0; q < p.size(); q++) w = std::max(w, std::fabs(s->hsc[x2g_scf::O_OVL + 64 * iorb + q]));
+  if (!p.empty()) s->wst[iorb] = w;
+}
+
+int prep_scf(x2g_scf *s) {
+  // prepSCF (doSCF.F90:24-174), hydrogenic start
+  for (int i = 1; i <= s->norb; i++) fock(s, i);
+  for (int i = 1; i <= s->norb; i++) {
+    int j = s->norb + 1 - i;
+    norm(s, j);
+    ortho(s, j);
+  }
+  for (int i = 1; i <= s->norb; i++) s->itouch[i] = 1;
+  mpole_moments(s);
+  for (int i = s->norb; i >= 1; i--) eahf(s, i, s->sc + x2g_scf::O_EE + i, nullptr);
+  int rc = read_scalars(s);
+  if (rc) return rc;
+  for (int i = 1; i <= s->norb; i++) s->eeOld[i] = s->ee[i];
+  return etotal(s);
+}
+
+// one SCF iteration (doSCF.F90:342-786); returns 1 when the loop ends
+int scf_iteration(x2g_scf *s, int *rc) {
+  const int norb = s->norb;
+  const int iscf = ++s->iscf;
+  int iasympt = norb;
+  *rc = X2G_OK;
+  for (int i = 1; i <= norb; i++) {
+    const int iorb = norb - i + 1;
+    s->itouch[iorb] = 1;
+    if (iasympt != 0 && s->ifixorb[iorb] == 0) {
+      pot_asympt(s, iorb);
+      iasympt--;
+    }
+    // relaxDriver (doSCF.F90:943-1011)
+    if ((*rc = relax_potentials(s, iorb))) return 1;
+    if (!s->lfixorb)
+      if ((*rc = relax_orbital(s, iorb))) return 1;
+    if (s->ifixorb[iorb] == 0) norm(s, iorb);
+    if (s->cs.homonuclear) launch_setci(s->ctx, s->grid->d, s->orb[iorb], s->ihomo[iorb]);
+    if (norb > 1 && s->ifixorb[iorb] == 0) ortho(s, iorb);
+    if (s->ifixorb[iorb] != 0) fock(s, iorb);
+    eahf(s, iorb, s->sc + x2g_scf::O_EE + iorb, nullptr);
+  }
+  if ((*rc = read_scalars(s))) return 1;
+  for (int i = 1; i <= norb; i++) {
+    const int iorb = norb - i + 1;
+    if (norb > 1 && s->ifixorb[iorb] == 0) update_wst(s, iorb);
+    s->deltaee[iorb] = s->ee[iorb] - s->eeOld[iorb];
+    if (std::fabs(s->deltaee[iorb]) < kPrecis) s->deltaee[iorb] = 2.0 * s->orbEnergyThld;
+    s->eeOld[iorb] = s->ee[iorb];
+    s->recs.push_back({iscf, iorb, s->ee[iorb], s->deltaee[iorb], s->orbNorm[iorb] - 1.0});
+  }
+  // convergence logic (doSCF.F90:540-723)
+  s->deltaeeMax = 0.0;
+  s->deltaNormMax = 0.0;
+  for (int n = 1; n <= norb; n++)
+    if (std::fabs(s->deltaee[n]) >= std::fabs(s->deltaeeMax)) s->deltaeeMax = s->deltaee[n];
+  for (int n = 1; n <= norb; n++) {
+    double dn = std::fabs(s->orbNorm[n] - 1.0);
+    if (s->ifixorb[n] == 0 && dn >= s->deltaNormMax) {
+      s->deltaNormMax = dn;
+      if (std::fabs(s->deltaNormMax) < kPrecis) s->deltaNormMax = kPrecis;
+    }
+  }
+  if (std::fabs(s->eeconv) < kPrecis) s->eeconv = s->deltaeeMax;
+  if (iscf > s->cs.nscf2skip) {
+    if (std::fabs(s->deltaeeMax) >= std::fabs(s->eeconvprev)) s->noenergydec++;
+    else {
+      s->eeconvprev = s->deltaeeMax;
+      s->noenergydec = 0;
+    }
+    if (std::fabs(s->deltaNormMax) >= std::fabs(s->dnmaxprev)) s->nonormdec++;
+    else {
+      s->dnmaxprev = s->deltaNormMax;
+      s->nonormdec = 0;
+    }
+    if (s->noenergydec > s->cs.nenlast || s->nonormdec > s->cs.nnolast) return 1;
+  } else {
+    s->eeconvprev = s->demax1;
+    s->dnmaxprev = s->deltaNormMax;
+  }
+  if (iscf == s->cs.maxscf) return 1;
+  if (s->lfixorb4init && std::fabs(s->deltaeeMax) < s->thren4init) {
+    if (s->nOrbEnergyThld == 3) {
+      for (int i = 1; i <= norb; i++) s->ifixorb[i] = 0;
+      s->lfixorb = 0;
+      s->lfixorb4init = 0;
+      s->eeconv = 10.0;
+      s->deltaeeMax = 100.0;
+    } else
+      s->nOrbEnergyThld++;
+  }
+  if (!s->lenergyThld) {
+    if (std::fabs(s->deltaeeMax) < s->orbEnergyThld) {
+      s->lenergyThld = 1;
+      s->eeconv = s->deltaeeMax;
+      for (int i = 1; i <= norb; i++) s->itouch[i] = 0;
+      s->nOrbEnergyThld = 0;
+    }
+  } else {
+    if (std::fabs(s->deltaeeMax) < s->orbEnergyThld) {
+      if (s->nOrbEnergyThld == 3) {
+        s->converged = 1;
+        return 1;
+      }
+      s->nOrbEnergyThld++;
+    } else if (std::fabs(s->deltaNormMax) < s->orbNormThld) {
+      if (s->nOrbNormThld == 3) {
+        s->converged = 2;
+        return 1;
+      }
+      s->nOrbNormThld++;
+    } else {
+      s->lenergyThld = 0;
+      if (s->nresets > 5) return 1;
+      s->nresets++;
+    }
+  }
+  if (!s->lfixorb) {
+    if (!s->lnormThld) {
+      if (std::fabs(s->deltaNormMax) < s->orbNormThld) {
+        s->lnormThld = 1;
+        for (int i = 1; i <= norb; i++) s->itouch[i] = 0;
+        s->nOrbNormThld = 0;
+      }
+    } else {
+      if (std::fabs(s->deltaNormMax) < s->orbNormThld) {
+        if (s->nOrbNormThld == 3) {
+          s->converged = 2;
+          return 1;
+        }
+        s->nOrbNormThld++;
+      } else {
+        s->lnormThld = 0;
+        if (s->nresets4no > 5) return 1;
+        s->nresets4no++;
+      }
+    }
+  }
+  if (std::fabs(s->eeconv / s->deltaeeMax) > s->cs.recalc_mm) {
+    s->eeconv = s->deltaeeMax;
+    mpole_moments(s);
+  }
+  for (int i = 1; i <= norb; i++) s->itouch[i] = 0;
+  return 0;
+}
+
+int scf_finish(x2g_scf *s) {
+  // end of scf (doSCF.F90:790-860)
+  if (s->norb > 1) {
+    for (int i = 1; i <= s->norb; i++) {
+      int j = s->norb + 1 - i;
+      double *keep = s->sc + x2g_scf::O_OVL + 64 * 50 + j;  // norm kept for the report
+      (void)keep;
+      launch_norm(s->ctx, s->grid->d, s->orb[j], s->sc + x2g_scf::O_OVL + 64 * 50 + j);
+      launch_scale(s->ctx, s->grid->d, s->orb[j], s->sc + x2g_scf::O_OVL + 64 * 50 + j);
+      ortho(s, j);
+    }
+  }
+  for (int i = s->norb; i >= 1; i--) eahf(s, i, s->sc + x2g_scf::O_EE + i, nullptr);
+  mpole_moments(s);
+  int rc = read_scalars(s);
+  if (rc) return rc;
+  return etotal(s);
+}
+
+}  // namespace
+
+extern "C" {
+
+int x2g_case_defaults(x2g_case *c) {
+  if (!c) return set_status(X2G_ERR_ARG, "null case");
+  std::memset(c, 0, sizeof *c);
+  c->maxscf = 1000;
+  c->ienterm = 10;
+  c->inoterm = 10;
+  c->ienterm4init = 1;
+  c->nscf2skip = 600;
+  c->nenlast = 20;
+  c->nnolast = 20;
+  c->maxsor_orb = 10;
+  c->maxsor_pot = 10;
+  c->omega_orb = -1;
+  c->omega_pot = -1;
+  c->recalc_mm = 1.15;
+  c->mpole = 4;
+  c->precision = X2G_FP64;
+  for (int i = 0; i < X2G_MAXORB; i++) c->gu[i] = ' ';
+  return X2G_OK;
+}
+
+int x2g_scf_destroy(x2g_scf *s) {
+  if (!s) return X2G_OK;
+  if (s->ctx) cudaStreamSynchronize(s->ctx->stream);
+  for (void *p : s->allocs) cudaFree(p);
+  if (s->grid) x2g_grid_destroy(s->grid);
+  delete s;
+  return X2G_OK;
+}
+
+int x2g_scf_create(x2g_ctx *ctx, const x2g_case *c, x2g_scf **out) {
+  if (!ctx || !c || !out) return set_status(X2G_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (c->norb < 1 || c->norb > X2G_MAXORB) return set_status(X2G_ERR_ARG, "norb out of range");
+  for (int i = 0; i < c->norb; i++) {
+    double full = (c->m[i] == 0) ? 2.0 : 4.0;
+    if (c->m[i] < 0 || c->m[i] > 3) return set_status(X2G_ERR_ARG, "orbital |lambda| must be 0..3");
+    if (std::fabs(c->occ[i] - full) > 1e-6)
+      return set_status(X2G_ERR_UNSUPPORTED, "open-shell configurations are not supported");
+  }
+  if (c->precision != X2G_FP64 && c->precision != X2G_MIXED) return set_status(X2G_ERR_ARG, "unknown precision");
+  if (c->maxsor_orb < 1 || c->maxsor_pot < 1) return set_status(X2G_ERR_ARG, "sweep counts must be positive");
+  auto *s = new x2g_scf();
+  s->ctx = ctx;
+  s->cs = *c;
+  int mpole = c->mpole > 0 ? c->mpole : 4;
+  // initCBlocks:781-806: mpole raised for delta/phi orbitals listed first
+  if (c->m[0] == 2 && mpole < 4) mpole = 4;
+  if (c->m[0] == 3 && mpole <= 4) mpole = 8;
+  s->mpole = mpole;
+  int rc = x2g_grid_create(ctx, c->nnu, c->nmu, c->r, c->rinf, c->z1, c->z2, mpole, &s->grid);
+  if (rc) {
+    delete s;
+    return rc;
+  }
+  const int norb = c->norb;
+  s->norb = norb;
+  for (int i = 1; i <= norb; i++) {
+    s->m[i] = c->m[i - 1];
+    s->occ[i] = c->occ[i - 1];
+    s->nel += int(std::lround(s->occ[i]));
+    s->isymOrb[i] = (s->m[i] % 2 == 0) ? 1 : -1;
+    char gu = c->gu[i - 1];
+    s->ihomo[i] = 1;
+    if (gu == 'u' && (s->m[i] == 0 || s->m[i] == 2)) s->ihomo[i] = -1;
+    if (gu == 'g' && (s->m[i] == 1 || s->m[i] == 3)) s->ihomo[i] = -1;
+    s->ige[i] = (gu == 'u') ? 1 : 2;
+  }
+  x2g_default_omega(c->nnu, c->nmu, c->z1, c->z2, &s->omega_orb, &s->omega_pot);
+  if (c->omega_orb > 0) s->omega_orb = c->omega_orb;
+  if (c->omega_pot > 0) s->omega_pot = c->omega_pot;
+  exchange_weights(s);
+  // storage (initAddr:1189-1296)
+  const size_t next = size_t(s->grid->h.next), mx = size_t(s->grid->h.mxsize);
+  s->orb.assign(norb + 1, nullptr);
+  s->coul.assign(norb + 1, nullptr);
+  s->coulp.assign(norb + 1, nullptr);
+  s->exchp.assign(norb + 1, nullptr);
+  const int nk = norb * (norb + 1) / 2 + 1;
+  s->exch.assign(2 * nk + 2, nullptr);
+  s->ilc.assign(nk + 1, 0);
+  bool ok = true;
+  for (int i = 1; i <= norb; i++) {
+    ok &= (s->orb[i] = dalloc(s, next)) != nullptr;
+    ok &= (s->coul[i] = dalloc(s, next)) != nullptr;
+    ok &= (s->coulp[i] = dalloc(s, mx)) != nullptr;
+    ok &= (s->exchp[i] = dalloc(s, mx)) != nullptr;
+  }
+  for (int i1 = 1; i1 <= norb; i1++)
+    for (int i2 = i1; i2 <= norb; i2++) {
+      int k = i1 + i2 * (i2 - 1) / 2;
+      if (i1 == i2 && s->m[i1] == 0) continue;
+      s->ilc[k] = 1;
+      s->ilc2[i1][i2] = s->ilc2[i2][i1] = 1;
+      s->k2[i1][i2] = s->k2[i2][i1] = k;
+      ok &= (s->exch[2 * k] = dalloc(s, next)) != nullptr;
+      if (i1 != i2 && s->m[i1] != 0 && s->m[i2] != 0) {
+        s->ilc[k] = 2;
+        s->ilc2[i1][i2] = s->ilc2[i2][i1] = 2;
+        ok &= (s->exch[2 * k + 1] = dalloc(s, next)) != nullptr;
+      }
+    }
+  ok &= (s->lhs = dalloc(s, mx)) != nullptr;
+  ok &= (s->rhs = dalloc(s, mx)) != nullptr;
+  ok &= (s->fa = dalloc(s, 5 * size_t(s->grid->h.nni))) != nullptr;
+  ok &= (s->edecay = dalloc(s, 4 * size_t(s->grid->h.nni))) != nullptr;
+  s->nslots = norb * (norb + 1) + 2;
+  s->sc_count = size_t(x2g_scf::O_EX) + 8 * size_t(s->nslots) + 2048;
+  ok &= (s->sc = dalloc(s, s->sc_count)) != nullptr;
+  s->hsc.assign(s->sc_count, 0.0);
+  if (!ok) {
+    x2g_scf_destroy(s);
+    return set_status(X2G_ERR_ALLOC, "device allocation failed");
+  }
+  // relaxation batches: exchange potentials K(iorb, j>=iorb) then J(iorb)
+  s->pots.assign(norb + 1, {});
+  for (int iorb = 1; iorb <= norb; iorb++) {
+    auto &P = s->pots[iorb];
+    for (int j = iorb; j <= norb; j++) {
+      if (iorb == j && s->m[iorb] == 0) continue;
+      if (iorb == j && s->ilc2[iorb][iorb] == 0) continue;
+      int in1 = std::min(iorb, j), in2 = std::max(iorb, j);
+      int idel = std::abs(s->m[in1] - s->m[in2]);
+      if (in1 == in2) idel = 2 * s->m[in1];
+      int ipc = in1 + in2 * (in2 - 1) / 2;
+      P.push_back({in1, in2, idel, (idel % 2 == 0) ? 1 : -1, s->exch[2 * ipc]});
+      if (s->ilc2[in1][in2] == 2) {
+        int id2 = s->m[in1] + s->m[in2];
+        P.push_back({in1, in2, id2, (id2 % 2 == 0) ? 1 : -1, s->exch[2 * ipc + 1]});
+      }
+    }
+    P.push_back({iorb, iorb, 0, 1, s->coul[iorb]});
+  }
+  for (int i1 = 1; i1 <= norb; i1++)
+    for (int i2 = i1; i2 <= norb; i2++) {
+      if (i1 == i2 && s->m[i2] == 0) continue;
+      int idel = std::abs(s->m[i2] - s->m[i1]);
+      if (i1 == i2) idel = 2 * s->m[i2];
+      int ipc = s->k2[i1][i2];
+      s->mm_i1.push_back(i1);
+      s->mm_i2.push_back(i2);
+      s->mm_idel.push_back(idel);
+      s->mm_ipc.push_back(ipc);
+      if (s->ilc2[i1][i2] == 2) {
+        s->mm_i1.push_back(i1);
+        s->mm_i2.push_back(i2);
+        s->mm_idel.push_back(s->m[i2] + s->m[i1]);
+        s->mm_ipc.push_back(ipc + norb * (norb + 1) / 2);
+      }
+    }
+  if ((rc = initial_guess(s))) {
+    x2g_scf_destroy(s);
+    return rc;
+  }
+  // orbpot hydrogen [ienterm4init] (inputInterface.F90:2257-2305)
+  if (c->ienterm4init > 0) {
+    s->lfixorb4init = s->lfixorb = 1;
+    for (int i = 1; i <= norb; i++) s->ifixorb[i] = 1;
+  }
+  *out = s;
+  return set_status(X2G_OK, "");
+}
+
+int x2g_scf_run(x2g_scf *s, int max_iterations, x2g_result *res) {
+  if (!s) return set_status(X2G_ERR_ARG, "null scf");
+  cudaSetDevice(s->ctx->device);
+  int rc = X2G_OK;
+  if (!s->started) {
+    if ((rc = prep_scf(s))) return rc;
+    s->orbEnergyThld = std::pow(10.0, double(-s->cs.ienterm));
+    s->orbNormThld = std::pow(10.0, double(-s->cs.inoterm));
+    s->thren4init = std::pow(10.0, double(-s->cs.ienterm4init));
+    for (int i = 1; i <= s->norb; i++) {
+      s->itouch[i] = 0;
+      s->deltaee[i] = 0;
+      s->eeOld[i] = s->ee[i];
+    }
+    if (s->cs.homonuclear)
+      for (int i = 1; i <= s->norb; i++) launch_setci(s->ctx, s->grid->d, s->orb[i], s->ihomo[i]);
+    s->started = 1;
+  }
+  for (int k = 0; k < max_iterations && !s->done; k++) {
+    if (scf_iteration(s, &rc)) {
+      if (rc) return rc;
+      s->done = 1;
+      if ((rc = scf_finish(s))) return rc;
+    }
+  }
+  if (res) {
+    std::memset(res, 0, sizeof *res);
+    res->iterations = s->iscf;
+    res->converged = s->converged;
+    res->sweeps = s->nsor4orb + s->nsor4pot;
+    res->total_energy = s->etot;
+    res->electronic_energy = s->evt;
+    res->virial = s->virial;
+    for (int i = 1; i <= s->norb; i++) {
+      res->ee[i - 1] = s->ee[i];
+      res->norm_error[i - 1] = s->orbNorm[i] - 1.0;
+    }
+  }
+  return set_status(X2G_OK, "");
+}
+
+int x2g_scf_get_orbital(x2g_scf *s, int iorb, double *host) {
+  if (!s || !host || iorb < 1 || iorb > s->norb) return set_status(X2G_ERR_ARG, "bad argument");
+  const HostGrid &g = s->grid->h;
+  std::vector<double> ext(g.next);
+  cudaError_t e = cudaMemcpyAsync(ext.data(), s->orb[iorb], ext.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                  s->ctx->stream);
+  if (e != cudaSuccess) return cuda_status(e, "orbital readback");
+  int rc = x2g_synchronize(s->ctx);
+  if (rc) return rc;
+  for (int i = 0; i < g.nmu; i++)
+    for (int j = 0; j < g.nni; j++) host[i * g.nni + j] = ext[(i + 4) * g.n8 + j + 4];
+  return X2G_OK;
+}
+
+int x2g_scf_get_coulomb(x2g_scf *s, int iorb, double *host) {
+  if (!s || !host || iorb < 1 || iorb > s->norb) return set_status(X2G_ERR_ARG, "bad argument");
+  const HostGrid &g = s->grid->h;
+  std::vector<double> ext(g.next);
+  cudaError_t e = cudaMemcpyAsync(ext.data(), s->coul[iorb], ext.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                  s->ctx->stream);
+  if (e != cudaSuccess) return cuda_status(e, "potential readback");
+  int rc = x2g_synchronize(s->ctx);
+  if (rc) return rc;
+  for (int i = 0; i < g.nmu; i++)
+    for (int j = 0; j < g.nni; j++) host[i * g.nni + j] = ext[(i + 4) * g.n8 + j + 4];
+  return X2G_OK;
+}
+
+int x2g_scf_nrecords(x2g_scf *s) { return s ? int(s->recs.size()) : 0; }
+
+int x2g_scf_record(x2g_scf *s, int i, int *iscf, int *iorb, double *ee, double *dee, double *dnorm) {
+  if (!s || i < 0 || i >= int(s->recs.size())) return set_status(X2G_ERR_ARG, "record index out of range");
+  const Rec &r = s->recs[i];
+  if (iscf) *iscf = r.iscf;
+  if (iorb) *iorb = r.iorb;
+  if (ee) *ee = r.ee;
+  if (dee) *dee = r.dee;
+  if (dnorm) *dnorm = r.dnorm;
+  return X2G_OK;
+}
+
+}  // extern "C"

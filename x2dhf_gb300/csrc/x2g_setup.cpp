@@ -1,0 +1,348 @@
+// Host-side construction of the grid, operator tables and the GPU sweep
+// schedule.  The formulas are those of x2dhf's src/initCBAllocArrays.F90
+// (initCBlocks:813-858, initSuppl:1636-2051, initLP:1517-1560, mesh:2503-2544)
+// written out in 0-based C++; the schedule (row bands, colour levels) is this
+// library's own.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <numeric>
+
+#include "x2g_internal.h"
+
+namespace x2g {
+
+namespace {
+
+// 7-point Newton-Cotes weights on n = 1 (mod 6) points (initSuppl:1917-1955)
+std::vector<double> newton_cotes(int n, double h) {
+  std::vector<double> w(n + 6, 0.0);
+  double w1 = h / 140.0;
+  w[0] = 0.0 + w1 * 41.0;
+  for (int i = 1; i < n; i += 6) {
+    w[i] = w1 * 216.0;
+    w[i + 1] = w1 * 27.0;
+    w[i + 2] = w1 * 272.0;
+    w[i + 3] = w1 * 27.0;
+    w[i + 4] = w1 * 216.0;
+    w[i + 5] = (i + 5 == n - 1) ? w1 * 41.0 : 2.0 * w1 * 41.0;
+  }
+  w.resize(n);
+  return w;
+}
+
+}  // namespace
+
+std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf, double z1, double z2,
+                            int mpole) {
+  if (nni < 13 || nmu < 13 || (nni - 1) % 6 || (nmu - 1) % 6 || (nni - 6) % 5 || (nmu - 6) % 5)
+    return "grid sizes must be >= 13 and satisfy n = 1 (mod 6), n - 6 = 0 (mod 5)";
+  if (!(r > 0) || !(rinf > r / 2)) return "bond length must be > 0 and R_inf > R/2";
+  if (mpole < 2 || mpole > 8) return "mpole must be in [2,8]";
+  g.nni = nni;
+  g.nmu = nmu;
+  g.n8 = nni + 8;
+  g.m8 = nmu + 8;
+  g.next = g.n8 * g.m8;
+  g.mxsize = nni * nmu;
+  g.r = r;
+  g.r2 = r / 2.0;
+  g.z1 = z1;
+  g.z2 = z2;
+  g.mpole = mpole;
+  // grid steps (initCBlocks:813-858)
+  g.hni = kPi / double(nni - 1);
+  double xmi0 = 2.0 * rinf / r;
+  xmi0 = std::log(xmi0 + std::sqrt(xmi0 * xmi0 - 1.0));
+  g.hmu = xmi0 / double(nmu - 1);
+  g.vxi.assign(nmu, 0);
+  g.vxisq.assign(nmu, 0);
+  g.vxi1.assign(nmu, 0);
+  g.vxi2.assign(nmu, 0);
+  double vmu = 0.0;
+  for (int i = 0; i < nmu; i++) {
+    if (i > 0) vmu = vmu + g.hmu;
+    g.vxi[i] = std::cosh(vmu);
+    g.vxisq[i] = g.vxi[i] * g.vxi[i];
+    g.vxi1[i] = std::sqrt(g.vxi[i] * g.vxi[i] - 1.0);
+    g.vxi2[i] = (i == 0) ? 0.0 : g.vxi[i] / g.vxi1[i];
+  }
+  g.veta.assign(nni, 0);
+  g.vetasq.assign(nni, 0);
+  g.veta1.assign(nni, 0);
+  g.veta2.assign(nni, 0);
+  for (int j = 0; j < nni; j++) {
+    double vni = double(j) * g.hni;
+    g.veta[j] = std::cos(vni);
+    g.vetasq[j] = g.veta[j] * g.veta[j];
+    g.veta1[j] = std::sqrt(1.0 - g.veta[j] * g.veta[j]);
+    g.veta2[j] = (g.veta1[j] < kPrecis) ? 0.0 : g.veta[j] / g.veta1[j];
+  }
+  g.rinf = r * g.vxi[nmu - 1] / 2.0;
+  // supplementary arrays (initSuppl:1759-1911), Coulomb nuclei
+  const int mx = g.mxsize;
+  g.e.assign(mx, 0);
+  g.f0.assign(mx, 0);
+  g.f1.assign(mx, 0);
+  g.f2.assign(mx, 0);
+  g.f4.assign(mx, 0);
+  g.g.assign(mx, 0);
+  g.wgt1.assign(mx, 0);
+  g.wgt2.assign(mx, 0);
+  g.borb_mu.assign(nmu, 0);
+  g.bpot_mu.assign(nmu, 0);
+  g.f3_mu.assign(nmu, 0);
+  g.d_nu = g.veta2;
+  g.diag = -14350.0 / (5040.0) * (1.0 / (g.hmu * g.hmu) + 1.0 / (g.hni * g.hni));
+  std::vector<double> wjac1(mx), wjac2(mx);
+  const double wj1 = -r * kPi / 2.0, wj2 = r * r * kPi / 2.0, xrr = 0.5 * r;
+  for (int i = 0; i < nmu; i++) {
+    double w1 = g.vxi1[i], w2 = g.vxi[i] * g.vxi[i], w9 = xrr * g.vxi[i], w4 = g.vxi2[i];
+    double w5 = 0.0, w6 = 0.0;
+    if (i > 0) {
+      w5 = g.vxi[i] / g.vxi1[i] - 2.0 * g.vxi1[i] / g.vxi[i];
+      w6 = 1.0 / (g.vxi1[i] * g.vxi1[i]);
+    }
+    double w8 = -r * r * r * kPi * g.vxi[i] / 2.0;
+    g.borb_mu[i] = w4;
+    g.bpot_mu[i] = w5;
+    g.f3_mu[i] = -2.0 / w2 + g.diag;
+    for (int j = 0; j < nni; j++) {
+      int ij = i * nni + j;
+      double w10 = g.veta1[j];
+      g.e[ij] = (w10 < kPrecis) ? 0.0 : (-w6 - 1.0 / (w10 * w10));
+      double w7 = w2 - g.veta[j] * g.veta[j];
+      g.f1[ij] = r * r * w7 / 2.0;
+      g.f0[ij] = r * (g.vxi[i] * (z1 + z2) + g.veta[j] * (z2 - z1));
+      g.f2[ij] = (i == 0) ? 0.0 : -r * w7 / g.vxi[i];
+      g.g[ij] = w8 * w7;
+      g.f4[ij] = w9;
+      wjac1[ij] = wj1 * w1 * w10;
+      wjac2[ij] = wj2 * w1 * w10 * (w1 * w1 + w10 * w10) / g.vxi[i];
+    }
+  }
+  g.wmu = newton_cotes(nmu, g.hmu);
+  g.wni = newton_cotes(nni, g.hni);
+  for (int i = 0; i < nmu; i++)
+    for (int j = 0; j < nni; j++) {
+      int ij = i * nni + j;
+      wjac1[ij] = g.wmu[i] * wjac1[ij];
+      wjac2[ij] = g.wmu[i] * wjac2[ij];
+      g.wgt1[ij] = g.wni[j] * wjac1[ij];
+      g.wgt2[ij] = g.wni[j] * wjac2[ij];
+    }
+  // 8th-order Stirling coefficients (initSuppl:1680-1683, 1979-2001)
+  static const double aa1[9] = {3.0, -32.0, 168.0, -672.0, 0.0, 672.0, -168.0, 32.0, -3.0};
+  static const double aa2[9] = {-9.0, 128.0, -1008.0, 8064.0, -14350.0, 8064.0, -1008.0, 128.0, -9.0};
+  const double c1 = 1.0 / (840.0), c2 = 1.0 / (5040.0);
+  for (int k = 0; k < 4; k++) {
+    g.dmu2[k] = c2 * aa2[k] / (g.hmu * g.hmu);
+    g.dmu1[k] = c1 * aa1[k] / g.hmu;
+    g.dni2[k] = c2 * aa2[k] / (g.hni * g.hni);
+    g.dni1[k] = c1 * aa1[k] / g.hni;
+  }
+  g.dmu9.assign(9 * nmu, 0);
+  g.dni9.assign(9 * nni, 0);
+  for (int i = 0; i < nmu; i++)
+    for (int k = 0; k < 9; k++) {
+      double a2 = c2 * aa2[k] / (g.hmu * g.hmu), a1 = c1 * aa1[k] / g.hmu;
+      g.dmu9[9 * i + k] = a2 + g.borb_mu[i] * a1;
+    }
+  for (int j = 0; j < nni; j++)
+    for (int k = 0; k < 9; k++) {
+      double a2 = c2 * aa2[k] / (g.hni * g.hni), a1 = c1 * aa1[k] / g.hni;
+      g.dni9[9 * j + k] = a2 + g.d_nu[j] * a1;
+    }
+  g.exeven[0] = 210.0 / 126.0;
+  g.exeven[1] = -120.0 / 126.0;
+  g.exeven[2] = 45.0 / 126.0;
+  g.exeven[3] = -10.0 / 126.0;
+  g.exeven[4] = 1.0 / 126.0;
+  // Legendre polynomials times (R/2 r)^k (initLP:1531-1589)
+  g.leg.assign(size_t(mpole) * mx, 0.0);
+  for (int i = 0; i < nmu; i++)
+    for (int j = 0; j < nni; j++) {
+      int ij = i * nni + j;
+      double rr = std::sqrt(g.vxisq[i] + g.vetasq[j] - 1.0);
+      double xr = g.r2 * rr;
+      double costh = (std::fabs(rr) < kPrecis) ? 0.0 : g.vxi[i] * g.veta[j] / rr;
+      double dome[10];
+      dome[1] = costh;
+      dome[2] = (3.0 * costh * costh - 1.0) * 0.50;
+      for (int n = 2; n <= mpole - 1; n++)
+        dome[n + 1] = (double(2 * n + 1) * costh * dome[n] - double(n) * dome[n - 1]) / double(n + 1);
+      double xw = xr;
+      g.leg[ij] = dome[1] * xw;
+      for (int k = 2; k <= mpole; k++) {
+        xw = xw * xr;
+        g.leg[size_t(k - 1) * mx + ij] = dome[k] * xw;
+      }
+    }
+
+  // ------------------------------------------------------------------
+  // "middle" ordering of the interior points (mesh:2503-2544), 1-based
+  // ext rows ii in 6..nmu, cols jj in 6..nni+3, middle-outward.
+  // ------------------------------------------------------------------
+  const int nmux = (g.m8 - 1) / 2, nnix = (g.n8 - 1) / 2;
+  g.order.clear();
+  g.order.reserve(size_t(nni - 2) * (nmu - 5));
+  for (int i = 6; i <= nmu; i++) {
+    int ii = (i <= nmux) ? nmux - i + 6 : i;
+    for (int j = 6; j <= nni + 3; j++) {
+      int jj = (j <= nnix) ? nnix - j + 6 : j;
+      g.order.push_back((ii - 1) * g.n8 + (jj - 1));
+    }
+  }
+  const int npts = int(g.order.size());
+  // colour = list position mod 5 (mcsor loops i=c,ngrid1,5)
+  std::vector<int> pos(g.next, -1);
+  for (int p = 0; p < npts; p++) pos[g.order[p]] = p;
+  // colour level: a point waits for every same-colour stencil neighbour
+  // earlier in the list (new value read) and, by symmetry, is waited on by
+  // every same-colour neighbour later in the list (old value read).
+  std::vector<int> lev(npts, 0);
+  std::vector<std::pair<int, int>> deps;
+  int offs[16];
+  for (int k = 1; k <= 4; k++) {
+    offs[4 * (k - 1) + 0] = -k;
+    offs[4 * (k - 1) + 1] = k;
+    offs[4 * (k - 1) + 2] = -k * g.n8;
+    offs[4 * (k - 1) + 3] = k * g.n8;
+  }
+  int maxlev = 0;
+  for (int p = 0; p < npts; p++) {
+    int ij = g.order[p], L = 0;
+    for (int o : offs) {
+      int q = ij + o;
+      if (q < 0 || q >= g.next) continue;
+      int pq = pos[q];
+      if (pq < 0 || pq % 5 != p % 5) continue;
+      if (pq < p) {
+        L = std::max(L, lev[pq] + 1);
+        deps.push_back({pq, p});
+      }
+    }
+    lev[p] = L;
+    maxlev = std::max(maxlev, L);
+  }
+  if (maxlev + 1 > kMaxLevels) return "colour level depth exceeds the schedule limit";
+  g.nlev = maxlev + 1;
+  // row bands: 0-based ext rows [4, nmu); band 0 must hold rows 4..9 (the
+  // mu=1 extrapolation reads rows 5..9), ~4 rows each, merged until every
+  // same-colour dependency lies inside one band.
+  const int H = 4;
+  std::vector<int> bounds;
+  bounds.push_back(4);
+  int b = 10;
+  while (b < nmu) {
+    bounds.push_back(b);
+    b += H;
+  }
+  bounds.push_back(nmu);
+  // a band narrower than 2 rows at the end is merged into its neighbour
+  if (bounds.size() > 2 && bounds[bounds.size() - 1] - bounds[bounds.size() - 2] < 2)
+    bounds.erase(bounds.end() - 2);
+  auto band_of = [&](int row) {
+    return int(std::upper_bound(bounds.begin(), bounds.end(), row) - bounds.begin()) - 1;
+  };
+  for (bool changed = true; changed;) {
+    changed = false;
+    for (auto &d : deps) {
+      int ra = g.order[d.first] / g.n8, rb = g.order[d.second] / g.n8;
+      int ta = band_of(ra), tb = band_of(rb);
+      if (ta != tb) {
+        int lo = std::min(ta, tb), hi = std::max(ta, tb);
+        bounds.erase(bounds.begin() + lo + 1, bounds.begin() + hi + 1);
+        changed = true;
+        break;
+      }
+    }
+  }
+  g.ntiles = int(bounds.size()) - 1;
+  g.tile_row0.assign(bounds.begin(), bounds.end() - 1);
+  g.tile_row1.assign(bounds.begin() + 1, bounds.end());
+  // bucket points by (tile, colour, level), list order inside each bucket
+  const int nb = g.ntiles * 5 * g.nlev;
+  std::vector<int> cnt(nb + 1, 0);
+  for (int p = 0; p < npts; p++) {
+    int t = band_of(g.order[p] / g.n8);
+    cnt[(t * 5 + p % 5) * g.nlev + lev[p] + 1]++;
+  }
+  for (int k = 0; k < nb; k++) cnt[k + 1] += cnt[k];
+  g.off = cnt;
+  g.pts.assign(npts, 0);
+  std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+  for (int p = 0; p < npts; p++) {
+    int t = band_of(g.order[p] / g.n8);
+    g.pts[fill[(t * 5 + p % 5) * g.nlev + lev[p]]++] = g.order[p];
+  }
+  // final check: no two points of one (tile,colour,level) bucket interact,
+  // and every dependency is inside a tile with a strictly larger level
+  for (auto &d : deps) {
+    int ra = g.order[d.first] / g.n8, rb = g.order[d.second] / g.n8;
+    if (band_of(ra) != band_of(rb)) return "schedule check: dependency crosses a tile";
+    if (!(lev[d.second] > lev[d.first])) return "schedule check: level order violated";
+  }
+  return "";
+}
+
+}  // namespace x2g
+
+// ---------------------------------------------------------------------
+// CUDA-free access to the host-side tables (used by CPU tests)
+// ---------------------------------------------------------------------
+extern "C" int x2g_host_table(int nnu, int nmu, double r, double rinf, double z1, double z2, int which,
+                              double *out) {
+  x2g::HostGrid g;
+  std::string msg = x2g::build_host_grid(g, nnu, nmu, r, rinf, z1, z2, 4);
+  if (!msg.empty()) return X2G_ERR_ARG;
+  for (int i = 0; i < nmu; ++i)
+    for (int j = 0; j < nnu; ++j) {
+      const int k = i * nnu + j;
+      double v;
+      switch (which) {
+        case 0: v = g.borb_mu[i]; break;
+        case 1: v = g.bpot_mu[i]; break;
+        case 2: v = g.d_nu[j]; break;
+        case 3: v = g.e[k]; break;
+        case 4: v = g.f0[k]; break;
+        case 5: v = g.f1[k]; break;
+        case 6: v = g.f2[k]; break;
+        case 7: v = g.f3_mu[i]; break;
+        case 8: v = g.f4[k]; break;
+        case 9: v = g.g[k]; break;
+        case 10: v = g.wgt1[k]; break;
+        case 11: v = g.wgt2[k]; break;
+        default: return X2G_ERR_ARG;
+      }
+      out[k] = v;
+    }
+  return X2G_OK;
+}
+
+// Sweep order and schedule of the host grid: order[npoints] (ext indices,
+// 0-based, reference list order), tile/colour/level of every point.
+extern "C" int x2g_host_schedule(int nnu, int nmu, int *npoints, int *ntiles, int *nlevels, int *order,
+                                 int *tile, int *colour, int *level) {
+  x2g::HostGrid g;
+  std::string msg = x2g::build_host_grid(g, nnu, nmu, 2.0, 40.0, 1.0, 1.0, 4);
+  if (!msg.empty()) return X2G_ERR_SCHEDULE;
+  if (npoints) *npoints = int(g.order.size());
+  if (ntiles) *ntiles = g.ntiles;
+  if (nlevels) *nlevels = g.nlev;
+  if (order) std::copy(g.order.begin(), g.order.end(), order);
+  if (tile && colour && level) {
+    for (int t = 0; t < g.ntiles; ++t)
+      for (int c = 0; c < 5; ++c)
+        for (int l = 0; l < g.nlev; ++l) {
+          const int o = (t * 5 + c) * g.nlev + l;
+          for (int k = g.off[o]; k < g.off[o + 1]; ++k) {
+            tile[k] = t;
+            colour[k] = c;
+            level[k] = l;
+            order[k] = g.pts[k];
+          }
+        }
+  }
+  return X2G_OK;
+}
