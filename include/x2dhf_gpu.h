@@ -72,6 +72,12 @@ int x2g_destroy(x2g_ctx *ctx);
 int x2g_synchronize(x2g_ctx *ctx);
 /* The context's cudaStream_t, as an opaque pointer. */
 void *x2g_stream(x2g_ctx *ctx);
+/* Sweep-kernel timing with CUDA events on the context's stream.
+ * enable: 1 on, 0 off, 2 reset counters and switch on, -1 query only.
+ * precision selects the FP64 sweep kernel (0) or the FP32 sweep kernel of
+ * the mixed form (1); outputs are summed over launches resolved at the last
+ * x2g_synchronize: milliseconds, point-updates, launches. */
+int x2g_profile(x2g_ctx *ctx, int enable, int precision, double *ms, double *points, long *launches);
 
 /* ------------------------------------------------------------------ */
 /* grid                                                               */

@@ -21,6 +21,7 @@ CASES = {
     "he_set02": "he/set-02",   # He 91x121, MCSOR (1 thread)
     "ne_set01": "ne/set-01",   # Ne 151x181, 4 orbitals incl. 1pi, SOR
     "h_set04": "h/set-04",     # H 1pi, 131x?, one electron
+    "n2_set01": "n2-elprop/set-01",  # N2 421x781 R_inf=200, 6 orbitals, 22 potentials
 }
 
 LINE = re.compile(r"^\s*(\d+)\s+(\d+)\s+(sigma|pi|delta|phi)\s*([gu]?)\s+"
@@ -54,6 +55,10 @@ def main():
         with open(os.path.join(d, "reference.lst")) as f:
             lst = f.read()
         recs, etot, sweeps = extract(lst)
+        if len(recs) > 2000:
+            # long runs: keep the first 10 SCF iterations only (the final
+            # energy pins the converged result)
+            recs = [r for r in recs if r[0] <= 10]
         with open(os.path.join(out, name + ".input"), "w") as f:
             f.write(deck)
         with open(os.path.join(out, name + ".json"), "w") as f:

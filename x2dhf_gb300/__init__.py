@@ -71,7 +71,7 @@ EXPORTS = [
     "x2g_quadrature", "x2g_case_defaults", "x2g_scf_create", "x2g_scf_destroy", "x2g_scf_run",
     "x2g_scf_get_orbital", "x2g_scf_get_coulomb", "x2g_scf_nrecords", "x2g_scf_record",
     "x2g_kernel_launches", "mcsor_pthread_", "mcsor_tpool_", "coulExch_pthread_", "coulExch_tpool_",
-    "tpoolStop4mcsor_", "tpoolStop4pots_", "x2g_host_table", "x2g_host_schedule",
+    "tpoolStop4mcsor_", "tpoolStop4pots_", "x2g_host_table", "x2g_host_schedule", "x2g_profile",
 ]
 
 _lib = None
@@ -118,6 +118,7 @@ def lib():
     L.x2g_host_table.argtypes = [I, I, D, D, D, D, I, dp]
     ip = C.POINTER(C.c_int)
     L.x2g_host_schedule.argtypes = [I, I, ip, ip, ip, ip, ip, ip, ip]
+    L.x2g_profile.argtypes = [P, I, I, dp, dp, C.POINTER(C.c_long)]
     L.x2g_kernel_launches.restype = C.c_long
     L.x2g_kernel_launches.argtypes = [P]
     _lib = L
@@ -190,12 +191,14 @@ def parse_deck(text, precision=FP64):
                     c.homonuclear = 1
                     rest = rest[1:]
                 spins = [t for t in rest if t != "end"]
+                occ = 2.0 if mt == 0 else 4.0
                 if spins and spins[0][0] in "+-.":
-                    raise ValueError("open-shell configurations are not supported")
+                    # explicit spin occupation (read_config): one electron per + or -
+                    occ = float(sum(1 for t in spins[:4] if t in ("+", "-")))
                 for _ in range(nb):
                     c.m[norb] = mt
                     c.gu[norb] = ord(gu)
-                    c.occ[norb] = 2.0 if mt == 0 else 4.0
+                    c.occ[norb] = occ
                     norb += 1
                 if "end" in rest:
                     break
@@ -308,6 +311,12 @@ class Context:
     def launches(self):
         return self.L.x2g_kernel_launches(self.h)
 
+    def profile(self, enable=-1, precision=FP64):
+        """Sweep-kernel CUDA-event timing: (ms, point_updates, launches)."""
+        ms, pts, n = C.c_double(), C.c_double(), C.c_long()
+        _check(self.L.x2g_profile(self.h, enable, precision, C.byref(ms), C.byref(pts), C.byref(n)))
+        return ms.value, pts.value, n.value
+
     def close(self):
         if getattr(self, "h", None):
             self.L.x2g_destroy(self.h)
@@ -337,9 +346,10 @@ class Grid:
         return out
 
     def close(self):
-        if getattr(self, "h", None):
+        # a grid outliving its context is left to the process teardown
+        if getattr(self, "h", None) and getattr(self.ctx, "h", None):
             self.L.x2g_grid_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         self.close()
@@ -392,9 +402,9 @@ class SCF:
         return out
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and getattr(self.ctx, "h", None):
             self.L.x2g_scf_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         self.close()

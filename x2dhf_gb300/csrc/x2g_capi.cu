@@ -102,6 +102,11 @@ int x2g_destroy(x2g_ctx *c) {
   if (!c) return X2G_OK;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  for (auto &p : c->pending) {
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  for (cudaEvent_t ev : c->event_pool) cudaEventDestroy(ev);
   if (c->work) cudaFree(c->work);
   if (c->red) cudaFree(c->red);
   if (c->bar) cudaFree(c->bar);
@@ -115,6 +120,17 @@ int x2g_synchronize(x2g_ctx *c) {
   if (!c) return set_status(X2G_ERR_ARG, "null context");
   cudaError_t e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_status(e, "stream synchronize");
+  for (auto &p : c->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      c->prof_ms[p.precision] += ms;
+      c->prof_points[p.precision] += p.points;
+      c->prof_launches[p.precision] += 1;
+    }
+    c->event_pool.push_back(p.a);
+    c->event_pool.push_back(p.b);
+  }
+  c->pending.clear();
   int err = 0;
   e = cudaMemcpy(&err, c->bar + 2, sizeof(int), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_status(e, "error word readback");
@@ -126,6 +142,23 @@ int x2g_synchronize(x2g_ctx *c) {
 }
 
 void *x2g_stream(x2g_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int x2g_profile(x2g_ctx *c, int enable, int precision, double *ms, double *points, long *launches) {
+  if (!c || precision < 0 || precision > 1) return set_status(X2G_ERR_ARG, "bad argument");
+  if (enable >= 0) {
+    c->profiling = enable;
+    if (enable == 2) {  // reset counters
+      c->prof_ms[0] = c->prof_ms[1] = 0;
+      c->prof_points[0] = c->prof_points[1] = 0;
+      c->prof_launches[0] = c->prof_launches[1] = 0;
+      c->profiling = 1;
+    }
+  }
+  if (ms) *ms = c->prof_ms[precision];
+  if (points) *points = c->prof_points[precision];
+  if (launches) *launches = c->prof_launches[precision];
+  return X2G_OK;
+}
 
 long x2g_kernel_launches(x2g_ctx *c) { return c ? c->launches : 0; }
 
@@ -244,7 +277,7 @@ int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, doubl
 
 int x2g_grid_destroy(x2g_grid *gr) {
   if (!gr) return X2G_OK;
-  if (gr->ctx) cudaStreamSynchronize(gr->ctx->stream);
+  cudaDeviceSynchronize();
   for (void *p : gr->allocs) cudaFree(p);
   delete gr;
   return X2G_OK;

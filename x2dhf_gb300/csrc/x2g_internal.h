@@ -94,6 +94,18 @@ struct x2g_ctx {
   size_t red_bytes = 0;
   double *host_red = nullptr;  // pinned host buffer for small readbacks
   long launches = 0;
+  // optional per-launch timing of the sweep kernels (CUDA events on stream)
+  int profiling = 0;
+  struct Pending {
+    cudaEvent_t a, b;
+    int precision;
+    double points;  // point-updates performed by the launch
+  };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> event_pool;
+  double prof_ms[2] = {0, 0};      // FP64, mixed (FP32 sweep kernel only)
+  double prof_points[2] = {0, 0};
+  long prof_launches[2] = {0, 0};
 };
 
 struct x2g_grid {

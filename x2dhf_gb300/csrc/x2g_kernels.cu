@@ -970,9 +970,27 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
   int nj = njobs, ns = nsweeps;
   GridDev gd = g;
   void *args[] = {&gd, &djobs, &nj, &ns, &bar, &nblocks};
+  x2g_ctx::Pending pe{};
+  if (ctx->profiling) {
+    for (cudaEvent_t *ev : {&pe.a, &pe.b}) {
+      if (!ctx->event_pool.empty()) {
+        *ev = ctx->event_pool.back();
+        ctx->event_pool.pop_back();
+      } else if ((err = cudaEventCreate(ev)) != cudaSuccess) {
+        return cuda_status(err, "profiling event");
+      }
+    }
+    pe.precision = mixed ? 1 : 0;
+    pe.points = double(njobs) * double(g.nni - 2) * double(g.nmu - 5) * double(nsweeps);
+    cudaEventRecord(pe.a, ctx->stream);
+  }
   err = cudaLaunchCooperativeKernel(mixed ? (const void *)k_mcsor_f32 : (const void *)k_mcsor_f64, dim3(nblocks),
                                     dim3(kThreads), args, 0, ctx->stream);
   if (err != cudaSuccess) return cuda_status(err, "cooperative MCSOR launch");
+  if (ctx->profiling) {
+    cudaEventRecord(pe.b, ctx->stream);
+    ctx->pending.push_back(pe);
+  }
   ctx->launches += 1;
   if (mixed) {
     dim3 gu(grid_blocks((g.nni - 2) * (g.nmu - 5)), njobs);

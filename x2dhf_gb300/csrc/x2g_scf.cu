@@ -363,15 +363,14 @@ std::vector<int> ortho_partners(x2g_scf *s, int iorb1) {
     int iorb3 = s->norb - iorb2 + 1;
     if (iorb3 <= iorb1) continue;
     if (s->m[iorb3] != s->m[iorb1]) continue;
-    if (s->ige[iorb3] != s->ige[iorb1] && !(s->cs.homonuclear == 0 && false)) {
-      if (s->ige[iorb3] != s->ige[iorb1]) continue;
-    }
+    if (s->ige[iorb3] != s->ige[iorb1]) continue;
     v.push_back(iorb3);
   }
   return v;
 }
 
 void ortho(x2g_scf *s, int iorb) {
+  if (s->ifixorb[iorb] != 0) return;  // normOrtho.F90:143
   std::vector<int> p = ortho_partners(s, iorb);
   if (p.empty()) return;
   std::vector<const double *> o;
@@ -741,8 +740,11 @@ int x2g_scf_create(x2g_ctx *ctx, const x2g_case *c, x2g_scf **out) {
   for (int i = 0; i < c->norb; i++) {
     double full = (c->m[i] == 0) ? 2.0 : 4.0;
     if (c->m[i] < 0 || c->m[i] > 3) return set_status(X2G_ERR_ARG, "orbital |lambda| must be 0..3");
-    if (std::fabs(c->occ[i] - full) > 1e-6)
-      return set_status(X2G_ERR_UNSUPPORTED, "open-shell configurations are not supported");
+    if (!(c->occ[i] > 0) || c->occ[i] > full + 1e-6) return set_status(X2G_ERR_ARG, "bad occupation");
+    // one open orbital has neither exchange nor off-diagonal multipliers;
+    // several orbitals must form closed shells
+    if (c->norb > 1 && std::fabs(c->occ[i] - full) > 1e-6)
+      return set_status(X2G_ERR_UNSUPPORTED, "open-shell configurations with several orbitals are not supported");
   }
   if (c->precision != X2G_FP64 && c->precision != X2G_MIXED) return set_status(X2G_ERR_ARG, "unknown precision");
   if (c->maxsor_orb < 1 || c->maxsor_pot < 1) return set_status(X2G_ERR_ARG, "sweep counts must be positive");
