@@ -140,6 +140,24 @@ typedef struct {
  * stream.  `jobs` is a HOST array.  precision: X2G_FP64 or X2G_MIXED. */
 int x2g_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, int nsweeps, int precision);
 
+/* Relaxation that allocates no device memory (this entry point has no
+ * counterpart in the reference).  Same contract and FP64 results as
+ * x2g_relax with precision X2G_FP64, for callers that must not allocate:
+ * x2g_relax grows a context workspace with cudaMalloc, after synchronising
+ * the stream, when a larger batch arrives, which a loop admitting work
+ * against a fixed HBM budget, or a host driver relaxing inside its inner
+ * loop, cannot allow.  Here the scratch is one fixed 32 MiB device array in
+ * the library (held by every GPU that loads it until the process exits),
+ * looked up with cudaGetSymbolAddress on the first call on each device:
+ * make that first call before any stream capture.  A batch needing more
+ * than 32 MiB (256 B + 256 B-aligned job table + one nnu*nmu FP64
+ * right-hand side per job) is rejected with X2G_ERR_ARG.  Every call shares
+ * the array and the call returns only after its kernel has finished; calls
+ * that overlap on the GPU (other threads, other contexts on the same
+ * device) would race on the shared scratch and must be serialised by the
+ * caller. */
+int x2g_relax_noalloc(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, int nsweeps);
+
 /* putin / putout on device buffers (src/inout.F90:23-82, 165-183). */
 int x2g_putin(x2g_ctx *ctx, x2g_grid *grid, int isym, const double *fun_plain, double *work_ext);
 int x2g_putout(x2g_ctx *ctx, x2g_grid *grid, const double *work_ext, double *fun_plain);

@@ -72,6 +72,7 @@ EXPORTS = [
     "x2g_scf_get_orbital", "x2g_scf_get_coulomb", "x2g_scf_nrecords", "x2g_scf_record",
     "x2g_kernel_launches", "mcsor_pthread_", "mcsor_tpool_", "coulExch_pthread_", "coulExch_tpool_",
     "tpoolStop4mcsor_", "tpoolStop4pots_", "x2g_host_table", "x2g_host_schedule", "x2g_profile",
+    "x2g_relax_noalloc",
 ]
 
 _lib = None
@@ -103,6 +104,7 @@ def lib():
     L.x2g_grid_table.argtypes = [P, I, dp]
     L.x2g_grid_info.argtypes = [P] + [C.POINTER(C.c_int)] * 5
     L.x2g_relax.argtypes = [P, P, C.POINTER(Job), I, I, I]
+    L.x2g_relax_noalloc.argtypes = [P, P, C.POINTER(Job), I, I]
     L.x2g_putin.argtypes = [P, P, I, P, P]
     L.x2g_putout.argtypes = [P, P, P, P]
     L.x2g_mcsor_host.argtypes = [P, P, I, I, D, I, dp, dp, dp]
@@ -359,6 +361,13 @@ def relax(ctx, grid, jobs, nsweeps, precision=FP64):
     """Relax a list of Job structures (device pointers) in one launch."""
     arr = (Job * len(jobs))(*jobs)
     _check(lib().x2g_relax(ctx.h, grid.h, arr, len(jobs), nsweeps, precision))
+
+
+def relax_noalloc(ctx, grid, jobs, nsweeps):
+    """FP64 relaxation through the entry point that allocates no device memory
+    (fixed 32 MiB library-resident scratch; returns when the kernel is done)."""
+    arr = (Job * len(jobs))(*jobs)
+    _check(lib().x2g_relax_noalloc(ctx.h, grid.h, arr, len(jobs), nsweeps))
 
 
 def mcsor_host(ctx, grid, isym, kind, omega, nsweeps, wk2, lhs, rhs):

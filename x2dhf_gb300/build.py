@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libx2dhf_gpu.so")
-SOURCES = ["x2g_setup.cpp", "x2g_kernels.cu", "x2g_capi.cu", "x2g_scf.cu", "x2g_compat.cu"]
+SOURCES = ["x2g_setup.cpp", "x2g_kernels.cu", "x2g_capi.cu", "x2g_scf.cu", "x2g_compat.cu", "x2g_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -9,6 +9,7 @@
 // into FMAs (the reference was built without FMA contraction).
 #include <cooperative_groups.h>
 #include <cstdio>
+#include <vector>
 
 #include "x2g_kernels.cuh"
 
@@ -999,6 +1000,66 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
     ctx->launches += 2;
   }
   // barrier error word: checked by the caller at its next synchronisation
+  return X2G_OK;
+}
+
+// Scratch layout of launch_relax_in_scratch: 4 barrier words, the job
+// table, then one plain right-hand-side buffer per job (256-byte aligned).
+size_t relax_scratch_bytes(const GridDev &g, int njobs) {
+  const size_t head = 256;
+  const size_t table = (sizeof(JobDev) * size_t(njobs) + 255) / 256 * 256;
+  const size_t plain = (size_t(g.mxsize) * sizeof(double) + 255) / 256 * 256;
+  return head + table + plain * size_t(njobs);
+}
+
+int launch_relax_in_scratch(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, int nsweeps,
+                            void *scratch, size_t scratch_bytes) {
+  const GridDev &g = grid->d;
+  if (njobs <= 0 || nsweeps <= 0) return set_status(X2G_ERR_ARG, "njobs and nsweeps must be positive");
+  const size_t need = relax_scratch_bytes(g, njobs);
+  if (need > scratch_bytes) return set_status(X2G_ERR_ARG, "batch does not fit the scratch");
+  char *base = static_cast<char *>(scratch);
+  unsigned *barw = reinterpret_cast<unsigned *>(base);
+  JobDev *djobs = reinterpret_cast<JobDev *>(base + 256);
+  char *rhs0 = base + 256 + (sizeof(JobDev) * size_t(njobs) + 255) / 256 * 256;
+  const size_t plain = (size_t(g.mxsize) * sizeof(double) + 255) / 256 * 256;
+  std::vector<JobDev> h(njobs);
+  for (int i = 0; i < njobs; ++i) {
+    const x2g_job &x = jobs[i];
+    const bool explicit_lr = (x.lhs && x.rhs);
+    if (!x.u || (x.kind != 0 && x.kind != 1) || (x.kind == 0 && !explicit_lr) ||
+        (x.kind == 1 && !explicit_lr && (!x.psa || !x.psb)) || (x.isym != 1 && x.isym != -1))
+      return set_status(X2G_ERR_ARG, "bad relaxation job");
+    JobDev &d = h[i];
+    d = JobDev{};
+    d.u = x.u;
+    d.lhs = x.lhs;
+    d.rhs = x.rhs;
+    d.psa = x.psa;
+    d.psb = x.psb;
+    d.omega = x.omega;
+    d.idel2 = double(x.idel * x.idel);
+    d.isym = x.isym;
+    d.kind = (x.kind == 1 && explicit_lr) ? 2 : x.kind;
+    d.rhs_buf = reinterpret_cast<double *>(rhs0 + plain * size_t(i));
+  }
+  cudaError_t err = cudaMemsetAsync(barw, 0, 4 * sizeof(unsigned), ctx->stream);
+  if (err != cudaSuccess) return cuda_status(err, "scratch barrier reset");
+  err = cudaMemcpyAsync(djobs, h.data(), sizeof(JobDev) * njobs, cudaMemcpyHostToDevice, ctx->stream);
+  if (err != cudaSuccess) return cuda_status(err, "scratch job table upload");
+  BarrierDev bar{barw, barw + 1, reinterpret_cast<int *>(barw + 2)};
+  int per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k_mcsor_f64, kThreads, 0);
+  if (err != cudaSuccess) return cuda_status(err, "occupancy query");
+  const int nitems = njobs * g.ntiles, cap = per_sm * ctx->num_sms;
+  unsigned nblocks = unsigned(nitems < cap ? nitems : cap);
+  if (nblocks < 1) nblocks = 1;
+  int nj = njobs, ns = nsweeps;
+  GridDev gd = g;
+  void *args[] = {&gd, &djobs, &nj, &ns, &bar, &nblocks};
+  err = cudaLaunchCooperativeKernel((const void *)k_mcsor_f64, dim3(nblocks), dim3(kThreads), args, 0, ctx->stream);
+  if (err != cudaSuccess) return cuda_status(err, "cooperative MCSOR launch");
+  ctx->launches += 1;
   return X2G_OK;
 }
 

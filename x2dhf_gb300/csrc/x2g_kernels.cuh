@@ -52,6 +52,11 @@ struct AsymptArgs {
 
 // ---- sweeps ----
 int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, int nsweeps, int precision);
+// FP64 sweep whose job table, right-hand-side buffers and barrier words live
+// in caller-provided device scratch (no allocation on this path).
+size_t relax_scratch_bytes(const GridDev &g, int njobs);
+int launch_relax_in_scratch(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, int nsweeps,
+                            void *scratch, size_t scratch_bytes);
 
 // ---- elementwise ----
 void launch_ghost_fill(x2g_ctx *ctx, const GridDev &g, double *u, int isym);           // putin ghosts, all rows
