@@ -79,6 +79,10 @@ struct x2o_state {
   int mm[MAXORB + 1], isymOrb[MAXORB + 1], ihomo[MAXORB + 1], ige[MAXORB + 1];
   int iorn[MAXORB + 1], lock[MAXORB + 1], iloop[MAXORB + 1], iqm[4 * MAXORB + 1];
   char spin[4 * MAXORB + 1];
+  double *orbblock, *potblock; /* contiguous storage (reference orbptr / exchptr) */
+  void (*pot_hook)(void *, int);
+  void (*orb_hook)(void *, int, int, double *, double *, double *);
+  void *hook_ud;
   double **psi;  /* [1..norb] plain */
   double **coul; /* [1..norb] plain Coulomb potential (exchptr(i2b)) */
   /* exchange potential storage by pair index k=k2(i,j), two slots each */
@@ -551,11 +555,15 @@ static void init_addr(x2o_state *s) {
   s->coul = (double **)calloc(norb + 1, sizeof(double *));
   s->coulombptr = (double **)calloc(norb + 1, sizeof(double *));
   s->exchangeptr = (double **)calloc(norb + 1, sizeof(double *));
+  int nk = norb * (norb + 1) / 2 + 1;
+  /* one block per kind, like the reference's orbptr / exchptr */
+  s->orbblock = dalloc((long)norb * mx);
+  s->potblock = dalloc((long)(norb + 2 * nk + 2) * mx);
   for (int i = 1; i <= norb; i++) {
-    s->psi[i] = dalloc(mx); s->coul[i] = dalloc(mx);
+    s->psi[i] = s->orbblock + (long)(i - 1) * mx;
+    s->coul[i] = s->potblock + (long)(i - 1) * mx;
     s->coulombptr[i] = dalloc(mx); s->exchangeptr[i] = dalloc(mx);
   }
-  int nk = norb * (norb + 1) / 2 + 1;
   s->exch = (double **)calloc(2 * nk + 2, sizeof(double *));
   for (int i1 = 1; i1 <= norb; i1++)
     for (int i2 = i1; i2 <= norb; i2++) {
@@ -564,8 +572,8 @@ static void init_addr(x2o_state *s) {
       if (i1 == i2 && s->m[i1] == 0) continue;
       s->ilc[k] = 1; s->ilc2[i1][i2] = 1; s->ilc2[i2][i1] = 1;
       s->k2[i1][i2] = k; s->k2[i2][i1] = k;
-      s->exch[2 * k] = dalloc(mx);
-      s->exch[2 * k + 1] = dalloc(mx);
+      s->exch[2 * k] = s->potblock + (long)(norb + 2 * k) * mx;
+      s->exch[2 * k + 1] = s->potblock + (long)(norb + 2 * k + 1) * mx;
       if (i1 == i2) continue;
       if (s->m[i1] == 0 || s->m[i2] == 0) continue;
       s->ilc[k] = 2; s->ilc2[i1][i2] = 2; s->ilc2[i2][i1] = 2;
@@ -1146,8 +1154,11 @@ void x2o_relax_orb(x2o_state *s, int iorb, int mode) {
       }
     orb_asympt_get(s, wk3, wk1);
     x2o_putin(nni, s->mxnmu, isym, s->psi[iorb], wk2);
-    x2o_sweep(s, mode, isym, s->maxsororb[1], omega, wk2, lhs, rhs, s->sup[0], s->sup[2], s->isstart, s->isstop,
-              s->isstep);
+    if (s->orb_hook)
+      s->orb_hook(s->hook_ud, iorb, isym, wk2, lhs, rhs);
+    else
+      x2o_sweep(s, mode, isym, s->maxsororb[1], omega, wk2, lhs, rhs, s->sup[0], s->sup[2], s->isstart,
+                s->isstop, s->isstep);
     x2o_putout(nni, s->mxnmu, s->psi[iorb], wk2);
     orb_asympt_set(s, s->psi[iorb], wk3);
   }
@@ -1747,8 +1758,14 @@ static const char *bondname(const x2o_state *s, int i) { return s->bond[i]; }
 
 /* relaxDriver: src/doSCF.F90:943-1011 (serial build) */
 static void relax_driver(x2o_state *s, int iorb) {
-  if (s->nexchpots[iorb] != 0 && !s->lfixexch)
-    for (int k = 1; k <= s->nexchpots[iorb]; k++) x2o_relax_pot(s, iorb, k, s->lpotmcsor ? 1 : 0);
+  if (s->nexchpots[iorb] != 0 && !s->lfixexch) {
+    if (s->pot_hook) {
+      s->nsor4pot += (long)s->nexchpots[iorb] * s->maxsorpot[0] * s->maxsorpot[1];
+      s->pot_hook(s->hook_ud, iorb);
+    } else {
+      for (int k = 1; k <= s->nexchpots[iorb]; k++) x2o_relax_pot(s, iorb, k, s->lpotmcsor ? 1 : 0);
+    }
+  }
   if (!s->lfixorb) x2o_relax_orb(s, iorb, s->lorbmcsor ? 1 : 0);
 }
 
@@ -2018,16 +2035,25 @@ void x2o_cmulti(const x2o_state *s, double *out) {
     for (int i = 1; i <= s->norb; i++) out[(k - 1) * s->norb + (i - 1)] = s->cmulti[i + (k - 1) * s->norb];
 }
 
+void x2o_set_hooks(x2o_state *s, void (*pot_hook)(void *, int),
+                   void (*orb_hook)(void *, int, int, double *, double *, double *), void *ud) {
+  s->pot_hook = pot_hook;
+  s->orb_hook = orb_hook;
+  s->hook_ud = ud;
+}
+double *x2o_orbital_block(x2o_state *s) { return s->orbblock; }
+double *x2o_potential_block(x2o_state *s) { return s->potblock; }
+long x2o_pot_offset(const x2o_state *s, int iorb, int k) { return (long)(s->pottarget[iorb][k] - s->potblock) + 1; }
+
 void x2o_free(x2o_state *s) {
   if (!s) return;
   if (s->psi) {
     for (int i = 1; i <= s->norb; i++) {
-      free(s->psi[i]); free(s->coul[i]); free(s->coulombptr[i]); free(s->exchangeptr[i]);
+      free(s->coulombptr[i]); free(s->exchangeptr[i]);
     }
     free(s->psi); free(s->coul); free(s->coulombptr); free(s->exchangeptr);
-    int nk = s->norb * (s->norb + 1) / 2 + 1;
-    for (int k = 0; k < 2 * nk + 2; k++) free(s->exch[k]);
     free(s->exch);
+    free(s->orbblock); free(s->potblock);
   }
   double *arrs[] = {s->vmu, s->vxi, s->vxisq, s->vxi1, s->vxi2, s->vni, s->veta, s->vetasq, s->veta1, s->veta2,
                     s->wmu, s->wni, s->dmu9, s->dni9};

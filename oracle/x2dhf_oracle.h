@@ -109,6 +109,18 @@ void x2o_pot_asympt(x2o_state *s, int iorb);
 /* multipole moments: cmulti[(k-1)*norb + iorb-1], exchange moments by pair */
 void x2o_cmulti(const x2o_state *s, double *out);
 
+/* Replace the relaxations by external kernels (the reference's own C backend
+ * in the timed reference run): pot_hook(ud, iorb) relaxes every potential of
+ * orbital iorb in the potential block; orb_hook(ud, iorb, isym, wk2, lhs,
+ * rhs) sweeps the extended orbital wk2.  Storage: one orbital block (orbital
+ * i at (i-1)*mxsize) and one potential block; x2o_pot_offset is the 1-based
+ * offset of potential k of orbital iorb (the reference's ibexcp). */
+void x2o_set_hooks(x2o_state *s, void (*pot_hook)(void *, int),
+                   void (*orb_hook)(void *, int, int, double *, double *, double *), void *ud);
+double *x2o_orbital_block(x2o_state *s);
+double *x2o_potential_block(x2o_state *s);
+long x2o_pot_offset(const x2o_state *s, int iorb, int k);
+
 #ifdef __cplusplus
 }
 #endif
