@@ -109,6 +109,13 @@ int x2g_grid_table(x2g_grid *grid, int which, double *host_out);
 int x2g_host_table(int nnu, int nmu, double r, double rinf, double z1, double z2, int which, double *out);
 int x2g_host_schedule(int nnu, int nmu, int *npoints, int *ntiles, int *nlevels, int *order, int *tile,
                       int *colour, int *level);
+/* Cluster plan of the on-chip FP32 sweep of the mixed form (no CUDA call):
+ * CTAs per relaxation job (0 = grid too large, grid-barrier kernel used),
+ * rows of the largest band, shared memory per CTA, band starts row0[C+1]. */
+int x2g_host_cluster_plan(int nnu, int nmu, int *csize, int *maxrows, long *smem, int *row0);
+/* Mixed form sweep path: 1 (default) on-chip cluster kernel where the grid
+ * fits, 0 the grid-barrier FP32 kernel. */
+int x2g_set_mixed_on_chip(x2g_ctx *ctx, int on);
 /* Schedule statistics: tiles (row bands), colour levels, points per sweep. */
 int x2g_grid_info(x2g_grid *grid, int *nnu, int *nmu, int *ntiles, int *nlevels, int *npoints);
 

@@ -121,6 +121,36 @@ def test_mixed_relaxation_tracks_fp64(ctx):
     assert np.abs(got - exact).max() <= 1e-5 * change + 1e-14
 
 
+@pytest.mark.parametrize("name", ["he_set01", "ne_set01", "h2_set01"])
+def test_mixed_on_chip_matches_grid_barrier_path(ctx, name):
+    """The cluster (distributed shared memory) FP32 sweep and the grid-barrier
+    FP32 sweep run the same schedule; the on-chip kernel multiplies by a
+    precomputed omega/lhs where the other divides, so they agree to FP32
+    rounding of the correction (the same bound as mixed vs FP64 above)."""
+    torch = pytest.importorskip("torch")
+    deck = golden_deck(name)
+    oc = Case(deck)
+    c, g = _grid(ctx, deck)
+    f1, f2 = oc.fock(1)
+    lhs, rhs = f1 + oc.coeffs()[5], f2.copy()
+    isym = 1 if c.m[0] % 2 == 0 else -1
+    uext = oc.putin(isym, oc.orbital(1))
+    omega = oc.omega()[0]
+    dev = torch.device("cuda:0")
+    dl, dr = torch.tensor(lhs, device=dev), torch.tensor(rhs, device=dev)
+    out = []
+    for on_chip in (True, False):
+        ctx.set_mixed_on_chip(on_chip)
+        u = torch.tensor(uext, device=dev)
+        xg.relax(ctx, g, [xg.Job(u=u.data_ptr(), lhs=dl.data_ptr(), rhs=dr.data_ptr(), omega=omega, isym=isym,
+                                 kind=0)], 10, xg.MIXED)
+        ctx.synchronize()
+        out.append(u.cpu().numpy())
+    ctx.set_mixed_on_chip(True)
+    change = np.abs(out[1] - uext).max()
+    assert np.abs(out[0] - out[1]).max() <= 1e-5 * change
+
+
 def _scf_records_match(name, niter, transform=None, tol=1e-11):
     deck = golden_deck(name)
     if transform:

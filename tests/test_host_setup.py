@@ -62,3 +62,26 @@ def _check_schedule(nnu, nmu):
 def test_schedule_reproduces_single_thread_mcsor_order(nnu, nmu):
     npairs = _check_schedule(nnu, nmu)
     assert npairs > 0  # the "middle" ordering has seam conflicts to order
+
+
+@pytest.mark.parametrize("nnu,nmu", [(31, 31), (91, 121), (151, 211), (151, 241), (331, 481)])
+def test_cluster_plan_bands(nnu, nmu):
+    """On-chip sweep plan: contiguous bands covering ext rows [4, nmu), band 0
+    holds rows 4..9 (the mu=1 extrapolation), every band >= 4 rows (its halo
+    is fed by the adjacent band only), shared memory within one SM."""
+    C, maxrows, smem, row0 = xg.host_cluster_plan(nnu, nmu)
+    assert 2 <= C <= 16
+    assert row0[0] == 4 and row0[-1] == nmu
+    heights = [b - a for a, b in zip(row0[:-1], row0[1:])]
+    assert min(heights) >= 4 and row0[1] >= 10 and max(heights) == maxrows
+    assert smem == ((maxrows + 8) + 2 * maxrows) * (nnu + 8) * 4 <= 200 * 1024
+    # every same-colour dependency lies inside one band (bands are unions of tiles)
+    order, pts, tile, col, lev = xg.host_schedule(nnu, nmu)
+    rows = pts // (nnu + 8)
+    band = np.searchsorted(np.array(row0), rows, side="right") - 1
+    for t in np.unique(tile):
+        assert np.unique(band[tile == t]).size == 1
+
+
+def test_large_grid_has_no_cluster_plan():
+    assert xg.host_cluster_plan(781, 1201)[0] == 0

@@ -72,7 +72,7 @@ EXPORTS = [
     "x2g_scf_get_orbital", "x2g_scf_get_coulomb", "x2g_scf_nrecords", "x2g_scf_record",
     "x2g_kernel_launches", "mcsor_pthread_", "mcsor_tpool_", "coulExch_pthread_", "coulExch_tpool_",
     "tpoolStop4mcsor_", "tpoolStop4pots_", "x2g_host_table", "x2g_host_schedule", "x2g_profile",
-    "x2g_relax_noalloc",
+    "x2g_relax_noalloc", "x2g_host_cluster_plan", "x2g_set_mixed_on_chip",
 ]
 
 _lib = None
@@ -121,6 +121,9 @@ def lib():
     ip = C.POINTER(C.c_int)
     L.x2g_host_schedule.argtypes = [I, I, ip, ip, ip, ip, ip, ip, ip]
     L.x2g_profile.argtypes = [P, I, I, dp, dp, C.POINTER(C.c_long)]
+    L.x2g_host_cluster_plan.argtypes = [I, I, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_long),
+                                        C.POINTER(C.c_int)]
+    L.x2g_set_mixed_on_chip.argtypes = [P, I]
     L.x2g_kernel_launches.restype = C.c_long
     L.x2g_kernel_launches.argtypes = [P]
     _lib = L
@@ -296,6 +299,17 @@ def host_schedule(nnu, nmu):
     return list_order, arrs[0], arrs[1], arrs[2], arrs[3]
 
 
+def host_cluster_plan(nnu, nmu):
+    """(CTAs per job, max band rows, shared bytes per CTA, band starts) of the on-chip sweep."""
+    L = lib()
+    c, m, sm = C.c_int(), C.c_int(), C.c_long()
+    _check(L.x2g_host_cluster_plan(nnu, nmu, C.byref(c), C.byref(m), C.byref(sm), None))
+    rows = (C.c_int * (c.value + 1))()
+    if c.value:
+        _check(L.x2g_host_cluster_plan(nnu, nmu, C.byref(c), C.byref(m), C.byref(sm), rows))
+    return c.value, m.value, sm.value, list(rows)
+
+
 # ---------------------------------------------------------------------------
 # objects
 # ---------------------------------------------------------------------------
@@ -312,6 +326,9 @@ class Context:
     @property
     def launches(self):
         return self.L.x2g_kernel_launches(self.h)
+
+    def set_mixed_on_chip(self, on):
+        _check(self.L.x2g_set_mixed_on_chip(self.h, 1 if on else 0))
 
     def profile(self, enable=-1, precision=FP64):
         """Sweep-kernel CUDA-event timing: (ms, point_updates, launches)."""

@@ -162,6 +162,12 @@ int x2g_profile(x2g_ctx *c, int enable, int precision, double *ms, double *point
 
 long x2g_kernel_launches(x2g_ctx *c) { return c ? c->launches : 0; }
 
+int x2g_set_mixed_on_chip(x2g_ctx *c, int on) {
+  if (!c) return set_status(X2G_ERR_ARG, "null context");
+  c->no_cluster = on ? 0 : 1;
+  return X2G_OK;
+}
+
 int x2g_round_grid(int n) {
   // nnucalc/nmucalc (inputInterface.F90:2961-3095): n = 1 (mod 6) and
   // n - 6 = 0 (mod 5) enforced alternately, always rounding down.
@@ -267,6 +273,17 @@ int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, doubl
   UP(h.tile_row1, tile_row1);
   UP(h.pts, pts);
   UP(h.off, off);
+  UP(h.pts_rc, pts_rc);
+  d.cl_size = h.cl_size;
+  d.cl_maxrows = h.cl_maxrows;
+  if (h.cl_size > 0) {
+    UP(h.cl_tile0, cl_tile0);
+    UP(h.cl_row0, cl_row0);
+    UP(h.cl_pts, cl_pts);
+    UP(h.cl_off, cl_off);
+  } else {
+    d.cl_tile0 = d.cl_row0 = d.cl_pts = d.cl_off = nullptr;
+  }
   UP(b32, borb_mu32);
   UP(p32, bpot_mu32);
   UP(d32, d_nu32);

@@ -38,6 +38,14 @@ struct HostGrid {
   std::vector<int> tile_row0, tile_row1;
   std::vector<int> pts;  // ext indices grouped [tile][colour][level]
   std::vector<int> off;  // (ntiles*5*nlev + 1) offsets into pts
+  std::vector<int> pts_rc;  // same points as (ext row << 16) | ext col
+  // cluster plan of the on-chip FP32 sweep: cl_size CTAs per job, CTA k
+  // owns tiles [cl_tile0[k], cl_tile0[k+1]) = ext rows [cl_row0[k], cl_row0[k+1])
+  int cl_size = 0, cl_maxrows = 0;
+  size_t cl_smem = 0;
+  std::vector<int> cl_tile0, cl_row0;
+  // the CTAs' points regrouped [cta][colour][level], packed (row << 16) | col
+  std::vector<int> cl_pts, cl_off;
 };
 
 std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf, double z1, double z2, int mpole);
@@ -53,7 +61,9 @@ struct GridDev {
   const double *e, *f0, *f1, *f2, *f4, *g, *wgt1, *wgt2, *leg;
   const double *dmu9, *dni9;
   const double *vxi, *vxisq, *veta, *vetasq;
-  const int *tile_row0, *tile_row1, *pts, *off;
+  const int *tile_row0, *tile_row1, *pts, *off, *pts_rc;
+  int cl_size, cl_maxrows;
+  const int *cl_tile0, *cl_row0, *cl_pts, *cl_off;
   // FP32 copies of the coefficient tables for the mixed form
   const float *borb_mu32, *bpot_mu32, *d_nu32;
 };
@@ -94,6 +104,11 @@ struct x2g_ctx {
   size_t red_bytes = 0;
   double *host_red = nullptr;  // pinned host buffer for small readbacks
   long launches = 0;
+  size_t cluster_smem_set = 0;  // dynamic shared memory granted to the cluster kernel
+  int no_cluster = 0;           // 1: mixed form uses the grid-barrier FP32 kernel
+  int cluster_nonportable = 0;  // cluster kernel allowed more than 8 CTAs
+  long cluster_checked_key = -1;  // (shared bytes, cluster size) last checked
+  int cluster_ok = 0;             // that cluster shape is schedulable here
   // optional per-launch timing of the sweep kernels (CUDA events on stream)
   int profiling = 0;
   struct Pending {

@@ -362,6 +362,174 @@ __global__ void __launch_bounds__(kThreads) k_mcsor_f32(GridDev g, const JobDev 
 }
 
 // ----------------------------------------------------------------------
+// On-chip FP32 correction sweep of the mixed form: one relaxation job per
+// thread-block cluster.  CTA k of the cluster keeps ext rows
+// [cl_row0[k]-4, cl_row0[k+1]+4) of the correction e in shared memory for
+// all micro-sweeps; after updating a point within 4 rows of its band edge it
+// also stores the value into the neighbouring CTA's halo through distributed
+// shared memory, and the colour phases are separated by the cluster's
+// hardware barrier.  Ends with u += e (FP64) and the FP64 axis
+// re-extrapolation of u for the CTA's rows.
+// ----------------------------------------------------------------------
+constexpr int kClusterThreads = 512;
+
+__device__ __forceinline__ float ex5f(const float *ex, const float *p, int s) {
+  return ex[0] * p[s] + ex[1] * p[2 * s] + ex[2] * p[3 * s] + ex[3] * p[4 * s] + ex[4] * p[5 * s];
+}
+
+// axis extrapolation of e in shared memory for the CTA's rows
+__device__ void smem_boundary(const GridDev &g, float *E, int R0, int R1, int rank, bool even, const float *ex) {
+  const int n8 = g.n8, nni = g.nni;
+  const int nrow7 = (rank == 0) ? nni - 2 : 0;
+  const int r0 = (rank == 0) ? 5 : R0;
+  const int nside = 2 * (R1 - r0);
+  for (int k = threadIdx.x; k < nrow7 + nside; k += blockDim.x) {
+    if (k < nrow7) {
+      float *p = E + (4 - R0 + 4) * n8 + 5 + k;
+      *p = even ? ex5f(ex, p, n8) : 0.0f;
+    } else {
+      const int q = k - nrow7, r = r0 + q / 2, side = q % 2;
+      float *p = E + (r - R0 + 4) * n8 + (side == 0 ? 4 : nni + 3);
+      *p = even ? ex5f(ex, p, side == 0 ? 1 : -1) : 0.0f;
+    }
+  }
+  __syncthreads();
+  if (rank == 0 && threadIdx.x < 2) {
+    float *p = E + (4 - R0 + 4) * n8 + (threadIdx.x == 0 ? 4 : nni + 3);
+    *p = even ? ex5f(ex, p, threadIdx.x == 0 ? 1 : -1) : 0.0f;
+  }
+}
+
+__global__ void __launch_bounds__(kClusterThreads) k_mixed_cluster(GridDev g, const JobDev *__restrict__ jobs,
+                                                                     int nsweeps) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  const int C = int(cl.num_blocks()), rank = int(cl.block_rank());
+  const JobDev &J = jobs[blockIdx.x / C];
+  double *const u = J.u;
+  const float *const r32 = J.r32, *const l32 = J.l32;
+  const bool even = (J.isym == 1);
+  const float omega = float(J.omega), omega1 = float(1.0 - J.omega);
+  const float *const bt = (J.kind >= 1) ? g.bpot_mu32 : g.borb_mu32;
+  extern __shared__ float E[];
+  const int n8 = g.n8, nni = g.nni;
+  const int R0 = g.cl_row0[rank], R1 = g.cl_row0[rank + 1];
+  const int nloc = (g.cl_maxrows + 8) * n8;
+  float *const RS = E + nloc;                 // residual of the band's points
+  float *const WS = RS + g.cl_maxrows * n8;   // omega / lhs
+  for (int k = threadIdx.x; k < nloc; k += blockDim.x) E[k] = 0.0f;
+  {
+    const int ra = (R0 < 5) ? 5 : R0, ncols = nni - 2, npts = (R1 - ra) * ncols;
+    for (int k = threadIdx.x; k < npts; k += blockDim.x) {
+      const int row = ra + k / ncols, col = 5 + k % ncols;
+      const int ik = (row - 4) * nni + (col - 4), ls = (row - R0) * n8 + col;
+      RS[ls] = r32[ik];
+      WS[ls] = omega / l32[ik];
+    }
+  }
+  CoefF cf;
+  for (int k = 0; k < 4; ++k) {
+    cf.dmu1[k] = float(g.dmu1[k]);
+    cf.dmu2[k] = float(g.dmu2[k]);
+    cf.dni1[k] = float(g.dni1[k]);
+    cf.dni2[k] = float(g.dni2[k]);
+  }
+  float ex[5];
+  for (int k = 0; k < 5; ++k) ex[k] = float(g.exeven[k]);
+  float *up = nullptr, *dn = nullptr;
+  int R0up = 0, R0dn = 0;
+  if (rank > 0) {
+    up = cl.map_shared_rank(E, rank - 1);
+    R0up = g.cl_row0[rank - 1];
+  }
+  if (rank < C - 1) {
+    dn = cl.map_shared_rank(E, rank + 1);
+    R0dn = g.cl_row0[rank + 1];
+  }
+  cl.sync();  // every CTA's band is zeroed before halo values arrive
+  const int *const cpts = g.cl_pts;
+  const int *const coff = g.cl_off + size_t(rank) * 5 * g.nlev;
+  for (int s = 0; s < nsweeps; ++s) {
+    for (int c = 0; c < 5; ++c) {
+      if (c == 0 && s > 0) {
+        smem_boundary(g, E, R0, R1, rank, even, ex);
+        __syncthreads();
+      }
+      for (int l = 0; l < g.nlev; ++l) {
+        const int b0 = coff[c * g.nlev + l], b1 = coff[c * g.nlev + l + 1];
+        if (b0 == b1) continue;
+        for (int k = b0 + threadIdx.x; k < b1; k += blockDim.x) {
+          const int rc = cpts[k];
+          const int row = rc >> 16, col = rc & 0xffff;
+          float *p = E + (row - R0 + 4) * n8 + col;
+          const int ls = (row - R0) * n8 + col;
+          const float m4 = p[-4 * n8], p4 = p[4 * n8], m3 = p[-3 * n8], p3 = p[3 * n8];
+          const float m2 = p[-2 * n8], p2 = p[2 * n8], m1 = p[-n8], p1 = p[n8];
+          const float l4 = p[-4], r4 = p[4], l3 = p[-3], r3 = p[3], l2 = p[-2], r2 = p[2], l1 = p[-1], r1 = p[1];
+          float dm2 = cf.dmu2[0] * (m4 + p4);
+          dm2 = __fmaf_rn(cf.dmu2[1], m3 + p3, dm2);
+          dm2 = __fmaf_rn(cf.dmu2[2], m2 + p2, dm2);
+          dm2 = __fmaf_rn(cf.dmu2[3], m1 + p1, dm2);
+          float dm1 = cf.dmu1[0] * (m4 - p4);
+          dm1 = __fmaf_rn(cf.dmu1[1], m3 - p3, dm1);
+          dm1 = __fmaf_rn(cf.dmu1[2], m2 - p2, dm1);
+          dm1 = __fmaf_rn(cf.dmu1[3], m1 - p1, dm1);
+          float dn2 = cf.dni2[0] * (l4 + r4);
+          dn2 = __fmaf_rn(cf.dni2[1], l3 + r3, dn2);
+          dn2 = __fmaf_rn(cf.dni2[2], l2 + r2, dn2);
+          dn2 = __fmaf_rn(cf.dni2[3], l1 + r1, dn2);
+          float dn1 = cf.dni1[0] * (l4 - r4);
+          dn1 = __fmaf_rn(cf.dni1[1], l3 - r3, dn1);
+          dn1 = __fmaf_rn(cf.dni1[2], l2 - r2, dn1);
+          dn1 = __fmaf_rn(cf.dni1[3], l1 - r1, dn1);
+          const float cc = __fmaf_rn(g.d_nu32[col - 4], dn1, __fmaf_rn(bt[row - 4], dm1, dm2) + dn2);
+          const float v = __fmaf_rn(omega1, *p, WS[ls] * (RS[ls] - cc));
+          *p = v;
+          if (up && row < R0 + 4) up[(row - R0up + 4) * n8 + col] = v;
+          if (dn && row >= R1 - 4) dn[(row - R0dn + 4) * n8 + col] = v;
+        }
+        __syncthreads();
+      }
+      cl.sync();
+    }
+  }
+  smem_boundary(g, E, R0, R1, rank, even, ex);
+  __syncthreads();
+  // u += e on the CTA's interior points, then the FP64 axis of u
+  const int ra = (R0 < 5) ? 5 : R0;
+  const int ncols = nni - 2, npts = (R1 - ra) * ncols;
+  for (int k = threadIdx.x; k < npts; k += blockDim.x) {
+    const int row = ra + k / ncols, col = 5 + k % ncols;
+    u[row * n8 + col] += double(E[(row - R0 + 4) * n8 + col]);
+  }
+  __syncthreads();
+  {
+    const int nrow7 = (rank == 0) ? nni - 2 : 0;
+    const int nside = 2 * (R1 - ra);
+    auto ex64 = [&](int ij, int st) {
+      return A(A(A(A(M(g.exeven[0], u[ij + st]), M(g.exeven[1], u[ij + 2 * st])), M(g.exeven[2], u[ij + 3 * st])),
+                 M(g.exeven[3], u[ij + 4 * st])),
+               M(g.exeven[4], u[ij + 5 * st]));
+    };
+    for (int k = threadIdx.x; k < nrow7 + nside; k += blockDim.x) {
+      if (k < nrow7) {
+        const int ij = 4 * n8 + 5 + k;
+        u[ij] = even ? ex64(ij, n8) : 0.0;
+      } else {
+        const int q = k - nrow7, r = ra + q / 2, side = q % 2;
+        const int ij = r * n8 + (side == 0 ? 4 : nni + 3);
+        u[ij] = even ? ex64(ij, side == 0 ? 1 : -1) : 0.0;
+      }
+    }
+    __syncthreads();
+    if (rank == 0 && threadIdx.x < 2) {
+      const int ij = 4 * n8 + (threadIdx.x == 0 ? 4 : nni + 3);
+      u[ij] = even ? ex64(ij, threadIdx.x == 0 ? 1 : -1) : 0.0;
+    }
+  }
+}
+
+// ----------------------------------------------------------------------
 // Mixed form: ghost refresh, FP64 residual, FP32 correction, FP64 update.
 // ----------------------------------------------------------------------
 __device__ __forceinline__ void ghost_point(const GridDev &g, double *u, int k, int isym) {
@@ -393,11 +561,12 @@ __global__ void k_ghost_jobs(GridDev g, const JobDev *__restrict__ jobs) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) ghost_point(g, J.u, k, J.isym);
 }
 
-__global__ void k_residual(GridDev g, const JobDev *__restrict__ jobs) {
+__global__ void k_residual(GridDev g, const JobDev *__restrict__ jobs, int zero_e) {
   const JobDev &J = jobs[blockIdx.y];
   const int nint = (g.nni - 2) * (g.nmu - 5);
   const int n1 = g.n8, n2 = 2 * g.n8, n3 = 3 * g.n8, n4 = 4 * g.n8;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.next; k += gridDim.x * blockDim.x) J.e32[k] = 0.0f;
+  if (zero_e)
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.next; k += gridDim.x * blockDim.x) J.e32[k] = 0.0f;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nint; k += gridDim.x * blockDim.x) {
     const int mu = 1 + k / (g.nni - 2), nu = 1 + k % (g.nni - 2);
     const int ik = mu * g.nni + nu, ij = (mu + 4) * g.n8 + nu + 4;
@@ -950,12 +1119,98 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
   err = cudaMemsetAsync(ctx->bar, 0, 4 * sizeof(unsigned), ctx->stream);
   if (err != cudaSuccess) return cuda_status(err, "barrier reset");
   const int nitems = njobs * g.ntiles;
+  bool on_chip = mixed && g.cl_size >= 2 && !ctx->no_cluster;
+  if (on_chip) {
+    // the cluster must be schedulable on this device (shared memory per CTA,
+    // non-portable sizes above 8): ask the occupancy calculator once
+    const size_t smem = size_t(g.cl_maxrows + 8) * g.n8 * sizeof(float) + 2 * size_t(g.cl_maxrows) * g.n8 * sizeof(float);
+    const long key = long(smem) * 64 + g.cl_size;
+    if (ctx->cluster_checked_key != key) {
+      ctx->cluster_checked_key = key;
+      ctx->cluster_ok = 0;
+      bool attr_ok = cudaFuncSetAttribute((const void *)k_mixed_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          int(smem)) == cudaSuccess;
+      if (attr_ok && g.cl_size > 8)
+        attr_ok = cudaFuncSetAttribute((const void *)k_mixed_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                                       1) == cudaSuccess;
+      if (attr_ok) {
+        ctx->cluster_smem_set = smem;
+        ctx->cluster_nonportable = (g.cl_size > 8);
+        cudaLaunchConfig_t q = {};
+        q.gridDim = dim3(unsigned(g.cl_size));
+        q.blockDim = dim3(kClusterThreads);
+        q.dynamicSmemBytes = smem;
+        cudaLaunchAttribute qa[1];
+        qa[0].id = cudaLaunchAttributeClusterDimension;
+        qa[0].val.clusterDim.x = unsigned(g.cl_size);
+        qa[0].val.clusterDim.y = 1;
+        qa[0].val.clusterDim.z = 1;
+        q.attrs = qa;
+        q.numAttrs = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, (const void *)k_mixed_cluster, &q) == cudaSuccess &&
+            nclusters > 0)
+          ctx->cluster_ok = 1;
+      }
+      (void)cudaGetLastError();
+    }
+    on_chip = ctx->cluster_ok != 0;
+  }
   if (mixed) {
     dim3 gg(grid_blocks(g.nmu * 8 + 4 * g.nni), njobs);
     k_ghost_jobs<<<gg, kThreads, 0, ctx->stream>>>(g, djobs);
     dim3 gr(grid_blocks((g.nni - 2) * (g.nmu - 5)), njobs);
-    k_residual<<<gr, kThreads, 0, ctx->stream>>>(g, djobs);
+    k_residual<<<gr, kThreads, 0, ctx->stream>>>(g, djobs, on_chip ? 0 : 1);
     ctx->launches += 2;
+  }
+  if (on_chip) {
+    const size_t smem = size_t(g.cl_maxrows + 8) * g.n8 * sizeof(float) + 2 * size_t(g.cl_maxrows) * g.n8 * sizeof(float);
+    if (smem > ctx->cluster_smem_set) {
+      err = cudaFuncSetAttribute((const void *)k_mixed_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(smem));
+      if (err != cudaSuccess) return cuda_status(err, "cluster kernel shared memory");
+      ctx->cluster_smem_set = smem;
+    }
+    if (g.cl_size > 8 && !ctx->cluster_nonportable) {
+      err = cudaFuncSetAttribute((const void *)k_mixed_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+      if (err != cudaSuccess) return cuda_status(err, "non-portable cluster size");
+      ctx->cluster_nonportable = 1;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(unsigned(njobs * g.cl_size));
+    cfg.blockDim = dim3(kClusterThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = unsigned(g.cl_size);
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    x2g_ctx::Pending pe{};
+    if (ctx->profiling) {
+      for (cudaEvent_t *ev : {&pe.a, &pe.b}) {
+        if (!ctx->event_pool.empty()) {
+          *ev = ctx->event_pool.back();
+          ctx->event_pool.pop_back();
+        } else if ((err = cudaEventCreate(ev)) != cudaSuccess) {
+          return cuda_status(err, "profiling event");
+        }
+      }
+      pe.precision = 1;
+      pe.points = double(njobs) * double(g.nni - 2) * double(g.nmu - 5) * double(nsweeps);
+      cudaEventRecord(pe.a, ctx->stream);
+    }
+    GridDev gd = g;
+    err = cudaLaunchKernelEx(&cfg, k_mixed_cluster, gd, (const JobDev *)djobs, nsweeps);
+    if (err != cudaSuccess) return cuda_status(err, "cluster MCSOR launch");
+    if (ctx->profiling) {
+      cudaEventRecord(pe.b, ctx->stream);
+      ctx->pending.push_back(pe);
+    }
+    ctx->launches += 1;
+    return X2G_OK;
   }
   static int max_f64 = -1, max_f32 = -1;
   int *pmax = mixed ? &max_f32 : &max_f64;

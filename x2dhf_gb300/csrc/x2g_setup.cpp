@@ -276,6 +276,60 @@ std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf
     int t = band_of(g.order[p] / g.n8);
     g.pts[fill[(t * 5 + p % 5) * g.nlev + lev[p]]++] = g.order[p];
   }
+  g.pts_rc.resize(g.pts.size());
+  for (size_t k = 0; k < g.pts.size(); ++k) g.pts_rc[k] = ((g.pts[k] / g.n8) << 16) | (g.pts[k] % g.n8);
+  // cluster plan for the on-chip FP32 sweep: contiguous tile ranges, ~30
+  // rows per CTA, 2..16 CTAs; each CTA keeps its FP32 band with 4-row halos
+  // plus the band's residual and omega/lhs in shared memory
+  g.cl_size = 0;
+  {
+    const int rows = nmu - 4;
+    int C = std::max(2, std::min(16, (rows + 29) / 30));
+    C = std::min(C, g.ntiles);
+    if (C >= 2) {
+      std::vector<int> t0(C + 1), r0(C + 1);
+      int t = 0;
+      t0[0] = 0;
+      for (int k = 1; k < C; ++k) {
+        const int target = 4 + (rows * k + C / 2) / C;
+        while (t < g.ntiles - (C - k) && g.tile_row1[t] <= target) ++t;
+        if (t <= t0[k - 1]) t = t0[k - 1] + 1;
+        t0[k] = t;
+      }
+      t0[C] = g.ntiles;
+      bool ok = true;
+      int maxrows = 0;
+      for (int k = 0; k < C; ++k) {
+        if (t0[k + 1] <= t0[k]) ok = false;
+        r0[k] = g.tile_row0[t0[k]];
+        maxrows = std::max(maxrows, g.tile_row1[t0[k + 1] - 1] - g.tile_row0[t0[k]]);
+      }
+      r0[C] = nmu;
+      const size_t smem = size_t(maxrows + 8) * g.n8 * sizeof(float) + 2 * size_t(maxrows) * g.n8 * sizeof(float);
+      // a band must be at least 4 rows (halo pushes go to the next CTA only)
+      for (int k = 0; k < C; ++k)
+        if (r0[k + 1] - r0[k] < 4) ok = false;
+      if (ok && smem <= 200 * 1024) {
+        g.cl_size = C;
+        g.cl_maxrows = maxrows;
+        g.cl_smem = smem;
+        g.cl_tile0 = t0;
+        g.cl_row0 = r0;
+        g.cl_off.assign(size_t(C) * 5 * g.nlev + 1, 0);
+        g.cl_pts.clear();
+        for (int k = 0; k < C; ++k)
+          for (int c = 0; c < 5; ++c)
+            for (int l = 0; l < g.nlev; ++l) {
+              g.cl_off[(size_t(k) * 5 + c) * g.nlev + l] = int(g.cl_pts.size());
+              for (int t = t0[k]; t < t0[k + 1]; ++t) {
+                const int o = (t * 5 + c) * g.nlev + l;
+                for (int q = g.off[o]; q < g.off[o + 1]; ++q) g.cl_pts.push_back(g.pts_rc[q]);
+              }
+            }
+        g.cl_off[size_t(C) * 5 * g.nlev] = int(g.cl_pts.size());
+      }
+    }
+  }
   // final check: no two points of one (tile,colour,level) bucket interact,
   // and every dependency is inside a tile with a strictly larger level
   for (auto &d : deps) {
@@ -344,5 +398,18 @@ extern "C" int x2g_host_schedule(int nnu, int nmu, int *npoints, int *ntiles, in
           }
         }
   }
+  return X2G_OK;
+}
+
+// Cluster plan of the on-chip FP32 sweep (no CUDA call): CTAs per job,
+// rows per CTA, shared memory bytes; row0[C+1] when non-NULL.
+extern "C" int x2g_host_cluster_plan(int nnu, int nmu, int *csize, int *maxrows, long *smem, int *row0) {
+  x2g::HostGrid g;
+  std::string msg = x2g::build_host_grid(g, nnu, nmu, 2.0, 40.0, 1.0, 1.0, 4);
+  if (!msg.empty()) return X2G_ERR_SCHEDULE;
+  if (csize) *csize = g.cl_size;
+  if (maxrows) *maxrows = g.cl_maxrows;
+  if (smem) *smem = long(g.cl_smem);
+  if (row0 && g.cl_size > 0) std::copy(g.cl_row0.begin(), g.cl_row0.end(), row0);
   return X2G_OK;
 }
