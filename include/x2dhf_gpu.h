@@ -113,6 +113,12 @@ int x2g_host_schedule(int nnu, int nmu, int *npoints, int *ntiles, int *nlevels,
  * CTAs per relaxation job (0 = grid too large, grid-barrier kernel used),
  * rows of the largest band, shared memory per CTA, band starts row0[C+1]. */
 int x2g_host_cluster_plan(int nnu, int nmu, int *csize, int *maxrows, long *smem, int *row0);
+/* Chunk lists of the on-chip sweep (host only): chunks of up to 4 points of
+ * one row at stride 5, packed (band row << 19) | (ext col << 2) | (count-1),
+ * and the offsets of each CTA's 5 colours x (levels + 1) segments (level 0
+ * off the shared band edges, level 0 near them, levels 1..), plus the end.
+ * Null arrays: counts only. */
+int x2g_host_cluster_chunks(int nnu, int nmu, int *nchunks, int *noff, int *chunks, int *off);
 /* Mixed form sweep path: 1 (default) on-chip cluster kernel where the grid
  * fits, 0 the grid-barrier FP32 kernel. */
 int x2g_set_mixed_on_chip(x2g_ctx *ctx, int on);

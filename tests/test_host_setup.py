@@ -74,7 +74,11 @@ def test_cluster_plan_bands(nnu, nmu):
     assert row0[0] == 4 and row0[-1] == nmu
     heights = [b - a for a, b in zip(row0[:-1], row0[1:])]
     assert min(heights) >= 4 and row0[1] >= 10 and max(heights) == maxrows
-    assert smem == ((maxrows + 8) + 2 * maxrows) * (nnu + 8) * 4 <= 200 * 1024
+    ch, off = xg.host_cluster_chunks(nnu, nmu)
+    nseg = (off.size - 1) // (5 * C)
+    maxchunks = max(off[(k + 1) * 5 * nseg] - off[k * 5 * nseg] for k in range(C))
+    assert smem == (((maxrows + 8) + 2 * maxrows) * (nnu + 8) + maxrows + nnu + 8 + 5 * nseg + 1 + maxchunks) * 4
+    assert smem <= 200 * 1024
     # every same-colour dependency lies inside one band (bands are unions of tiles)
     order, pts, tile, col, lev = xg.host_schedule(nnu, nmu)
     rows = pts // (nnu + 8)
@@ -85,3 +89,39 @@ def test_cluster_plan_bands(nnu, nmu):
 
 def test_large_grid_has_no_cluster_plan():
     assert xg.host_cluster_plan(781, 1201)[0] == 0
+
+
+@pytest.mark.parametrize("nnu,nmu", [(31, 31), (91, 121), (151, 241), (331, 481)])
+def test_cluster_chunks_cover_schedule(nnu, nmu):
+    """The on-chip sweep's chunks hold every scheduled point exactly once, in
+    its CTA's band and in the segment of its colour and level; a chunk is up
+    to 4 points of one row at stride 5; edge segments hold exactly the rows
+    within 4 of a band edge shared with another CTA."""
+    C, maxrows, smem, row0 = xg.host_cluster_plan(nnu, nmu)
+    ch, off = xg.host_cluster_chunks(nnu, nmu)
+    order, pts, tile, col, lev = xg.host_schedule(nnu, nmu)
+    nlev = int(lev.max()) + 1
+    S = nlev + 1
+    assert off.size == C * 5 * S + 1 and off[-1] == ch.size
+    n8 = nnu + 8
+    want = {int(p): (int(c), int(l)) for p, c, l in zip(pts, col, lev)}
+    seen = set()
+    for k in range(C):
+        for c in range(5):
+            for seg in range(S):
+                o = (k * 5 + c) * S + seg
+                for q in ch[off[o]:off[o + 1]]:
+                    lr, cl, n = int(q >> 19), int((q >> 2) & 0x1FFFF), int(q & 3) + 1
+                    row = row0[k] + lr
+                    assert row0[k] <= row < row0[k + 1]
+                    edge = (k > 0 and row < row0[k] + 4) or (k < C - 1 and row >= row0[k + 1] - 4)
+                    for j in range(n):
+                        p = row * n8 + cl + 5 * j
+                        assert p in want and p not in seen
+                        seen.add(p)
+                        assert want[p][0] == c
+                        if seg < 2:
+                            assert want[p][1] == 0 and edge == (seg == 1)
+                        else:
+                            assert want[p][1] == seg - 1
+    assert len(seen) == len(want)

@@ -72,7 +72,7 @@ EXPORTS = [
     "x2g_scf_get_orbital", "x2g_scf_get_coulomb", "x2g_scf_nrecords", "x2g_scf_record",
     "x2g_kernel_launches", "mcsor_pthread_", "mcsor_tpool_", "coulExch_pthread_", "coulExch_tpool_",
     "tpoolStop4mcsor_", "tpoolStop4pots_", "x2g_host_table", "x2g_host_schedule", "x2g_profile",
-    "x2g_relax_noalloc", "x2g_host_cluster_plan", "x2g_set_mixed_on_chip",
+    "x2g_relax_noalloc", "x2g_host_cluster_plan", "x2g_set_mixed_on_chip", "x2g_host_cluster_chunks",
 ]
 
 _lib = None
@@ -297,6 +297,18 @@ def host_schedule(nnu, nmu):
     _check(L.x2g_host_schedule(nnu, nmu, C.byref(n), C.byref(t), C.byref(l),
                                list_order.ctypes.data_as(C.POINTER(C.c_int)), None, None, None))
     return list_order, arrs[0], arrs[1], arrs[2], arrs[3]
+
+
+def host_cluster_chunks(nnu, nmu):
+    """(packed chunks, segment offsets) of the on-chip sweep (no GPU needed)."""
+    L = lib()
+    nc, no = C.c_int(), C.c_int()
+    _check(L.x2g_host_cluster_chunks(nnu, nmu, C.byref(nc), C.byref(no), None, None))
+    ch = np.zeros(nc.value, np.int32)
+    off = np.zeros(no.value, np.int32)
+    _check(L.x2g_host_cluster_chunks(nnu, nmu, C.byref(nc), C.byref(no),
+                                     ch.ctypes.data_as(C.POINTER(C.c_int)), off.ctypes.data_as(C.POINTER(C.c_int))))
+    return ch.view(np.uint32), off
 
 
 def host_cluster_plan(nnu, nmu):

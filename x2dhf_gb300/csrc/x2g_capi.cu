@@ -237,6 +237,13 @@ int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, doubl
   std::memcpy(d.dni1, h.dni1, sizeof d.dni1);
   std::memcpy(d.dni2, h.dni2, sizeof d.dni2);
   std::memcpy(d.exeven, h.exeven, sizeof d.exeven);
+  for (int k = 0; k < 4; ++k) {
+    d.dmu1f[k] = float(h.dmu1[k]);
+    d.dmu2f[k] = float(h.dmu2[k]);
+    d.dni1f[k] = float(h.dni1[k]);
+    d.dni2f[k] = float(h.dni2[k]);
+  }
+  for (int k = 0; k < 5; ++k) d.exevenf[k] = float(h.exeven[k]);
   d.diag = h.diag;
   std::vector<float> b32(h.borb_mu.begin(), h.borb_mu.end()), p32(h.bpot_mu.begin(), h.bpot_mu.end()),
       d32(h.d_nu.begin(), h.d_nu.end());
@@ -276,6 +283,7 @@ int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, doubl
   UP(h.pts_rc, pts_rc);
   d.cl_size = h.cl_size;
   d.cl_maxrows = h.cl_maxrows;
+  d.cl_maxchunks = h.cl_maxchunks;
   if (h.cl_size > 0) {
     UP(h.cl_tile0, cl_tile0);
     UP(h.cl_row0, cl_row0);

@@ -41,10 +41,14 @@ struct HostGrid {
   std::vector<int> pts_rc;  // same points as (ext row << 16) | ext col
   // cluster plan of the on-chip FP32 sweep: cl_size CTAs per job, CTA k
   // owns tiles [cl_tile0[k], cl_tile0[k+1]) = ext rows [cl_row0[k], cl_row0[k+1])
-  int cl_size = 0, cl_maxrows = 0;
+  int cl_size = 0, cl_maxrows = 0, cl_maxchunks = 0;
   size_t cl_smem = 0;
   std::vector<int> cl_tile0, cl_row0;
-  // the CTAs' points regrouped [cta][colour][level], packed (row << 16) | col
+  // the CTAs' points regrouped [cta][colour][segment] as chunks of up to 4
+  // points of one row at stride 5, packed (band row << 19) | (col << 2) |
+  // (count - 1); segments: level 0 off the band edges, level 0 within 4 rows
+  // of an edge shared with another CTA, then levels 1..nlev-1; cl_off has
+  // cl_size * 5 * (nlev + 1) + 1 chunk offsets
   std::vector<int> cl_pts, cl_off;
 };
 
@@ -62,10 +66,13 @@ struct GridDev {
   const double *dmu9, *dni9;
   const double *vxi, *vxisq, *veta, *vetasq;
   const int *tile_row0, *tile_row1, *pts, *off, *pts_rc;
-  int cl_size, cl_maxrows;
+  int cl_size, cl_maxrows, cl_maxchunks;
   const int *cl_tile0, *cl_row0, *cl_pts, *cl_off;
   // FP32 copies of the coefficient tables for the mixed form
   const float *borb_mu32, *bpot_mu32, *d_nu32;
+  // FP32 stencil weights, rounded on the host: GB300 issues double->float
+  // conversions on its narrow FP64 pipe, so the FP32 kernels never convert
+  float dmu1f[4], dmu2f[4], dni1f[4], dni2f[4], exevenf[5];
 };
 
 // Device job (one function to relax), built from x2g_job.
@@ -76,9 +83,10 @@ struct JobDev {
   const double *psa, *psb;
   double *rhs_buf;  // materialised rhs for potentials
   float *e32;       // mixed: FP32 extended correction
-  float *r32, *l32; // mixed: FP32 residual and diagonal
+  float *r32, *w32; // mixed: FP32 residual and omega / diagonal
   double omega;
   double idel2;
+  float omegaf, omega1f;  // omega and 1 - omega rounded to FP32 on the host
   int isym, kind;
 };
 

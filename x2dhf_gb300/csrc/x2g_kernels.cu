@@ -108,9 +108,10 @@ struct CoefF {
   float dmu1[4], dmu2[4], dni1[4], dni2[4];
 };
 
-// FP32 correction sweep point update (same operator, FMA allowed).
+// FP32 correction sweep point update (same operator, FMA allowed); w is
+// omega / lhs of the point, formed once per relaxation call.
 __device__ __forceinline__ void relax_f32(float *__restrict__ e, int ij, int n8, const CoefF &c, float b, float d,
-                                          float lhs, float r, float omega, float omega1) {
+                                          float w, float r, float omega1) {
   const int n1 = n8, n2 = 2 * n8, n3 = 3 * n8, n4 = 4 * n8;
   const float m4 = ldcg(e + ij - n4), p4 = ldcg(e + ij + n4);
   const float m3 = ldcg(e + ij - n3), p3 = ldcg(e + ij + n3);
@@ -138,7 +139,7 @@ __device__ __forceinline__ void relax_f32(float *__restrict__ e, int ij, int n8,
   dn1 = __fmaf_rn(c.dni1[2], l2 - r2, dn1);
   dn1 = __fmaf_rn(c.dni1[3], l1 - r1, dn1);
   const float cc = __fmaf_rn(d, dn1, __fmaf_rn(b, dm1, dm2) + dn2);
-  e[ij] = __fmaf_rn(omega1, ec, __fdividef(omega * (r - cc), lhs));
+  e[ij] = __fmaf_rn(omega1, ec, w * (r - cc));
 }
 
 // ----------------------------------------------------------------------
@@ -196,9 +197,9 @@ __device__ void tile_boundary(const GridDev &g, T *u, int t, int isym) {
                   M(g.exeven[3], ldcg(u + ij + n4))),
                 M(g.exeven[4], ldcg(u + ij + n5)));
         } else {
-          v = T(g.exeven[0]) * ldcg(u + ij + n1) + T(g.exeven[1]) * ldcg(u + ij + n2) +
-              T(g.exeven[2]) * ldcg(u + ij + n3) + T(g.exeven[3]) * ldcg(u + ij + n4) +
-              T(g.exeven[4]) * ldcg(u + ij + n5);
+          v = g.exevenf[0] * ldcg(u + ij + n1) + g.exevenf[1] * ldcg(u + ij + n2) +
+              g.exevenf[2] * ldcg(u + ij + n3) + g.exevenf[3] * ldcg(u + ij + n4) +
+              g.exevenf[4] * ldcg(u + ij + n5);
         }
       }
       u[ij] = v;
@@ -216,9 +217,9 @@ __device__ void tile_boundary(const GridDev &g, T *u, int t, int isym) {
                   M(g.exeven[3], ldcg(u + ij + 4 * s))),
                 M(g.exeven[4], ldcg(u + ij + 5 * s)));
         } else {
-          v = T(g.exeven[0]) * ldcg(u + ij + s) + T(g.exeven[1]) * ldcg(u + ij + 2 * s) +
-              T(g.exeven[2]) * ldcg(u + ij + 3 * s) + T(g.exeven[3]) * ldcg(u + ij + 4 * s) +
-              T(g.exeven[4]) * ldcg(u + ij + 5 * s);
+          v = g.exevenf[0] * ldcg(u + ij + s) + g.exevenf[1] * ldcg(u + ij + 2 * s) +
+              g.exevenf[2] * ldcg(u + ij + 3 * s) + g.exevenf[3] * ldcg(u + ij + 4 * s) +
+              g.exevenf[4] * ldcg(u + ij + 5 * s);
         }
       }
       u[ij] = v;
@@ -237,9 +238,9 @@ __device__ void tile_boundary(const GridDev &g, T *u, int t, int isym) {
                   M(g.exeven[3], ldcg(u + ij + 4 * s))),
                 M(g.exeven[4], ldcg(u + ij + 5 * s)));
         } else {
-          v = T(g.exeven[0]) * ldcg(u + ij + s) + T(g.exeven[1]) * ldcg(u + ij + 2 * s) +
-              T(g.exeven[2]) * ldcg(u + ij + 3 * s) + T(g.exeven[3]) * ldcg(u + ij + 4 * s) +
-              T(g.exeven[4]) * ldcg(u + ij + 5 * s);
+          v = g.exevenf[0] * ldcg(u + ij + s) + g.exevenf[1] * ldcg(u + ij + 2 * s) +
+              g.exevenf[2] * ldcg(u + ij + 3 * s) + g.exevenf[3] * ldcg(u + ij + 4 * s) +
+              g.exevenf[4] * ldcg(u + ij + 5 * s);
         }
       }
       u[ij] = v;
@@ -319,10 +320,10 @@ __global__ void __launch_bounds__(kThreads) k_mcsor_f32(GridDev g, const JobDev 
   const int nitems = njobs * g.ntiles;
   CoefF cf;
   for (int k = 0; k < 4; ++k) {
-    cf.dmu1[k] = float(g.dmu1[k]);
-    cf.dmu2[k] = float(g.dmu2[k]);
-    cf.dni1[k] = float(g.dni1[k]);
-    cf.dni2[k] = float(g.dni2[k]);
+    cf.dmu1[k] = g.dmu1f[k];
+    cf.dmu2[k] = g.dmu2f[k];
+    cf.dni1[k] = g.dni1f[k];
+    cf.dni2[k] = g.dni2f[k];
   }
   for (int s = 0; s < nsweeps; ++s) {
     for (int c = 0; c < 5; ++c) {
@@ -334,7 +335,7 @@ __global__ void __launch_bounds__(kThreads) k_mcsor_f32(GridDev g, const JobDev 
           tile_boundary<float>(g, e, t, J.isym);
           __syncthreads();
         }
-        const float omega = float(J.omega), omega1 = float(1.0 - J.omega);
+        const float omega1 = J.omega1f;
         const float *bt = (J.kind >= 1) ? g.bpot_mu32 : g.borb_mu32;
         for (int l = 0; l < g.nlev; ++l) {
           const int o = (t * 5 + c) * g.nlev + l;
@@ -344,7 +345,7 @@ __global__ void __launch_bounds__(kThreads) k_mcsor_f32(GridDev g, const JobDev 
             const int ij = g.pts[k];
             const int row = ij / g.n8, col = ij - row * g.n8;
             const int mu = row - 4, nu = col - 4, ik = mu * g.nni + nu;
-            relax_f32(e, ij, g.n8, cf, bt[mu], g.d_nu32[nu], J.l32[ik], J.r32[ik], omega, omega1);
+            relax_f32(e, ij, g.n8, cf, bt[mu], g.d_nu32[nu], J.w32[ik], J.r32[ik], omega1);
           }
           __syncthreads();
         }
@@ -365,11 +366,13 @@ __global__ void __launch_bounds__(kThreads) k_mcsor_f32(GridDev g, const JobDev 
 // On-chip FP32 correction sweep of the mixed form: one relaxation job per
 // thread-block cluster.  CTA k of the cluster keeps ext rows
 // [cl_row0[k]-4, cl_row0[k+1]+4) of the correction e in shared memory for
-// all micro-sweeps; after updating a point within 4 rows of its band edge it
-// also stores the value into the neighbouring CTA's halo through distributed
-// shared memory, and the colour phases are separated by the cluster's
-// hardware barrier.  Ends with u += e (FP64) and the FP64 axis
-// re-extrapolation of u for the CTA's rows.
+// all micro-sweeps, together with the band's residual, omega/lhs, the
+// coefficient rows and its point list; after updating a point within 4 rows
+// of its band edge it also stores the value into the neighbouring CTA's halo
+// through distributed shared memory, and the colour phases are separated by
+// the cluster's hardware barrier.  Ends by writing e of the band's interior
+// points to the job's FP32 correction array (u += e and the FP64 axis
+// extrapolation run afterwards on the whole GPU).
 // ----------------------------------------------------------------------
 constexpr int kClusterThreads = 512;
 
@@ -400,132 +403,183 @@ __device__ void smem_boundary(const GridDev &g, float *E, int R0, int R1, int ra
   }
 }
 
-__global__ void __launch_bounds__(kClusterThreads) k_mixed_cluster(GridDev g, const JobDev *__restrict__ jobs,
-                                                                     int nsweeps) {
+// dynamic shared memory of k_mixed_cluster: (residual, omega/lhs) pairs of
+// the band's points, correction band with 4-row halos, b(mu) of the band's
+// rows, d(nu) by ext column, the CTA's segment offsets, then its chunk list
+size_t cluster_smem_bytes(const GridDev &g) {
+  return 2 * size_t(g.cl_maxrows) * g.n8 * sizeof(float) + size_t(g.cl_maxrows + 8) * g.n8 * sizeof(float) +
+         size_t(g.cl_maxrows + g.n8) * sizeof(float) + size_t(5 * (g.nlev + 1) + 1) * sizeof(int) +
+         size_t(g.cl_maxchunks) * sizeof(int);
+}
+
+// split cluster barrier: arrive releases this thread's earlier shared and
+// distributed-shared writes, wait acquires every CTA's released writes
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
+struct ClusterBand {
+  float *E;               // correction rows [R0-4, R1+4) of the band
+  const float2 *RW;       // (residual, omega/lhs) by band row * n8 + col
+  const float *BT, *DN;   // b(mu) by band row, d(nu) by ext column
+  const unsigned *PL;     // chunks (band row << 19) | (col << 2) | (count-1)
+  float *up, *dn;         // neighbours' halos addressed like E, or null
+  int n8, hdn;            // band rows >= hdn feed the lower neighbour
+  float omega1;
+  CoefF cf;
+};
+
+// One chunk: up to 4 same-colour points of one band row at columns col,
+// col+5, col+10, col+15.  The row values col-4..col+19 are read once (a
+// point's left neighbours are the previous point's right ones); every read
+// precedes every write.  Positions past the chunk's count are computed but
+// not stored: their reads stay inside the CTA's shared allocation (at most
+// 10 elements past the correction band, the pairs or d(nu), each followed
+// by a larger array).
+template <bool halo>
+__device__ __forceinline__ void cluster_chunk(const ClusterBand &B, unsigned q) {
+  const int n8 = B.n8;
+  const int lr = int(q >> 19), col = int((q >> 2) & 0x1ffffu), n = int(q & 3u) + 1;
+  const int ls = lr * n8 + col;
+  float *const p = B.E + ls + 4 * n8;
+  const CoefF &cf = B.cf;
+  float rv[24];
+#pragma unroll
+  for (int i = 0; i < 24; ++i) rv[i] = p[i - 4];
+  const float b = B.BT[lr];
+  float out[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const float *pj = p + 5 * j;
+    const float m4 = pj[-4 * n8], p4 = pj[4 * n8], m3 = pj[-3 * n8], p3 = pj[3 * n8];
+    const float m2 = pj[-2 * n8], p2 = pj[2 * n8], m1 = pj[-n8], p1 = pj[n8];
+    const float l4 = rv[5 * j], l3 = rv[5 * j + 1], l2 = rv[5 * j + 2], l1 = rv[5 * j + 3], ec = rv[5 * j + 4];
+    const float r1 = rv[5 * j + 5], r2 = rv[5 * j + 6], r3 = rv[5 * j + 7], r4 = rv[5 * j + 8];
+    const float2 rw = B.RW[ls + 5 * j];
+    const float d = B.DN[col + 5 * j];
+    float dm2 = cf.dmu2[0] * (m4 + p4);
+    dm2 = __fmaf_rn(cf.dmu2[1], m3 + p3, dm2);
+    dm2 = __fmaf_rn(cf.dmu2[2], m2 + p2, dm2);
+    dm2 = __fmaf_rn(cf.dmu2[3], m1 + p1, dm2);
+    float dm1 = cf.dmu1[0] * (m4 - p4);
+    dm1 = __fmaf_rn(cf.dmu1[1], m3 - p3, dm1);
+    dm1 = __fmaf_rn(cf.dmu1[2], m2 - p2, dm1);
+    dm1 = __fmaf_rn(cf.dmu1[3], m1 - p1, dm1);
+    float dn2 = cf.dni2[0] * (l4 + r4);
+    dn2 = __fmaf_rn(cf.dni2[1], l3 + r3, dn2);
+    dn2 = __fmaf_rn(cf.dni2[2], l2 + r2, dn2);
+    dn2 = __fmaf_rn(cf.dni2[3], l1 + r1, dn2);
+    float dn1 = cf.dni1[0] * (l4 - r4);
+    dn1 = __fmaf_rn(cf.dni1[1], l3 - r3, dn1);
+    dn1 = __fmaf_rn(cf.dni1[2], l2 - r2, dn1);
+    dn1 = __fmaf_rn(cf.dni1[3], l1 - r1, dn1);
+    const float cc = __fmaf_rn(d, dn1, __fmaf_rn(b, dm1, dm2) + dn2);
+    out[j] = __fmaf_rn(B.omega1, ec, rw.y * (rw.x - cc));
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+    if (j < n) p[5 * j] = out[j];
+  if (halo) {
+    if (B.up && lr < 4) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (j < n) B.up[ls + 4 * n8 + 5 * j] = out[j];
+    }
+    if (B.dn && lr >= B.hdn) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (j < n) B.dn[ls + 4 * n8 + 5 * j] = out[j];
+    }
+  }
+}
+
+// update chunks [b0, b1) of the CTA's list (their points are independent)
+template <bool halo>
+__device__ __forceinline__ void cluster_chunks(const ClusterBand &B, int b0, int b1) {
+  for (int k = b0 + threadIdx.x; k < b1; k += blockDim.x) cluster_chunk<halo>(B, B.PL[k]);
+}
+
+__global__ void __launch_bounds__(kClusterThreads, 1) k_mixed_cluster(GridDev g, const JobDev *__restrict__ jobs,
+                                                                        int nsweeps) {
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
   const int C = int(cl.num_blocks()), rank = int(cl.block_rank());
   const JobDev &J = jobs[blockIdx.x / C];
-  double *const u = J.u;
-  const float *const r32 = J.r32, *const l32 = J.l32;
+  const float *const r32 = J.r32, *const w32 = J.w32;
   const bool even = (J.isym == 1);
-  const float omega = float(J.omega), omega1 = float(1.0 - J.omega);
   const float *const bt = (J.kind >= 1) ? g.bpot_mu32 : g.borb_mu32;
-  extern __shared__ float E[];
-  const int n8 = g.n8, nni = g.nni;
+  extern __shared__ float2 smem2[];
+  const int n8 = g.n8, nni = g.nni, nlev = g.nlev, S = nlev + 1;
   const int R0 = g.cl_row0[rank], R1 = g.cl_row0[rank + 1];
   const int nloc = (g.cl_maxrows + 8) * n8;
-  float *const RS = E + nloc;                 // residual of the band's points
-  float *const WS = RS + g.cl_maxrows * n8;   // omega / lhs
+  float2 *const RW = smem2;
+  float *const E = reinterpret_cast<float *>(RW + g.cl_maxrows * n8);
+  float *const BT = E + nloc;
+  float *const DN = BT + g.cl_maxrows;
+  int *const SO = reinterpret_cast<int *>(DN + n8);  // segment offsets into PL
+  unsigned *const PL = reinterpret_cast<unsigned *>(SO + 5 * S + 1);
+  const int *const coff = g.cl_off + size_t(rank) * 5 * S;
+  const int pbase = coff[0], npl = coff[5 * S] - pbase;
+  for (int k = threadIdx.x; k <= 5 * S; k += blockDim.x) SO[k] = coff[k] - pbase;
   for (int k = threadIdx.x; k < nloc; k += blockDim.x) E[k] = 0.0f;
-  {
-    const int ra = (R0 < 5) ? 5 : R0, ncols = nni - 2, npts = (R1 - ra) * ncols;
-    for (int k = threadIdx.x; k < npts; k += blockDim.x) {
-      const int row = ra + k / ncols, col = 5 + k % ncols;
-      const int ik = (row - 4) * nni + (col - 4), ls = (row - R0) * n8 + col;
-      RS[ls] = r32[ik];
-      WS[ls] = omega / l32[ik];
-    }
+  for (int k = threadIdx.x; k < R1 - R0; k += blockDim.x) BT[k] = bt[R0 + k - 4];
+  for (int k = threadIdx.x; k < n8; k += blockDim.x) DN[k] = (k >= 4 && k < nni + 4) ? g.d_nu32[k - 4] : 0.0f;
+  for (int k = threadIdx.x; k < npl; k += blockDim.x) PL[k] = unsigned(g.cl_pts[pbase + k]);
+  const int ra = (R0 < 5) ? 5 : R0, ncols = nni - 2, nband = (R1 - ra) * ncols;
+  for (int k = threadIdx.x; k < nband; k += blockDim.x) {
+    const int row = ra + k / ncols, col = 5 + k % ncols;
+    const int ik = (row - 4) * nni + (col - 4);
+    RW[(row - R0) * n8 + col] = make_float2(r32[ik], w32[ik]);
   }
-  CoefF cf;
+  ClusterBand B;
+  B.E = E;
+  B.RW = RW;
+  B.BT = BT;
+  B.DN = DN;
+  B.PL = PL;
+  B.n8 = n8;
+  B.hdn = R1 - R0 - 4;
+  B.omega1 = J.omega1f;
   for (int k = 0; k < 4; ++k) {
-    cf.dmu1[k] = float(g.dmu1[k]);
-    cf.dmu2[k] = float(g.dmu2[k]);
-    cf.dni1[k] = float(g.dni1[k]);
-    cf.dni2[k] = float(g.dni2[k]);
+    B.cf.dmu1[k] = g.dmu1f[k];
+    B.cf.dmu2[k] = g.dmu2f[k];
+    B.cf.dni1[k] = g.dni1f[k];
+    B.cf.dni2[k] = g.dni2f[k];
   }
   float ex[5];
-  for (int k = 0; k < 5; ++k) ex[k] = float(g.exeven[k]);
-  float *up = nullptr, *dn = nullptr;
-  int R0up = 0, R0dn = 0;
-  if (rank > 0) {
-    up = cl.map_shared_rank(E, rank - 1);
-    R0up = g.cl_row0[rank - 1];
-  }
-  if (rank < C - 1) {
-    dn = cl.map_shared_rank(E, rank + 1);
-    R0dn = g.cl_row0[rank + 1];
-  }
-  cl.sync();  // every CTA's band is zeroed before halo values arrive
-  const int *const cpts = g.cl_pts;
-  const int *const coff = g.cl_off + size_t(rank) * 5 * g.nlev;
+  for (int k = 0; k < 5; ++k) ex[k] = g.exevenf[k];
+  // neighbours' halo rows, addressed by this CTA's band offsets
+  B.up = (rank > 0) ? cl.map_shared_rank(E, rank - 1) + (R0 - g.cl_row0[rank - 1]) * n8 : nullptr;
+  B.dn = (rank < C - 1) ? cl.map_shared_rank(E, rank + 1) + (R0 - R1) * n8 : nullptr;
+  __syncthreads();
+  cluster_arrive();  // this band is zeroed: neighbours may push into its halos
   for (int s = 0; s < nsweeps; ++s) {
     for (int c = 0; c < 5; ++c) {
       if (c == 0 && s > 0) {
         smem_boundary(g, E, R0, R1, rank, even, ex);
         __syncthreads();
       }
-      for (int l = 0; l < g.nlev; ++l) {
-        const int b0 = coff[c * g.nlev + l], b1 = coff[c * g.nlev + l + 1];
-        if (b0 == b1) continue;
-        for (int k = b0 + threadIdx.x; k < b1; k += blockDim.x) {
-          const int rc = cpts[k];
-          const int row = rc >> 16, col = rc & 0xffff;
-          float *p = E + (row - R0 + 4) * n8 + col;
-          const int ls = (row - R0) * n8 + col;
-          const float m4 = p[-4 * n8], p4 = p[4 * n8], m3 = p[-3 * n8], p3 = p[3 * n8];
-          const float m2 = p[-2 * n8], p2 = p[2 * n8], m1 = p[-n8], p1 = p[n8];
-          const float l4 = p[-4], r4 = p[4], l3 = p[-3], r3 = p[3], l2 = p[-2], r2 = p[2], l1 = p[-1], r1 = p[1];
-          float dm2 = cf.dmu2[0] * (m4 + p4);
-          dm2 = __fmaf_rn(cf.dmu2[1], m3 + p3, dm2);
-          dm2 = __fmaf_rn(cf.dmu2[2], m2 + p2, dm2);
-          dm2 = __fmaf_rn(cf.dmu2[3], m1 + p1, dm2);
-          float dm1 = cf.dmu1[0] * (m4 - p4);
-          dm1 = __fmaf_rn(cf.dmu1[1], m3 - p3, dm1);
-          dm1 = __fmaf_rn(cf.dmu1[2], m2 - p2, dm1);
-          dm1 = __fmaf_rn(cf.dmu1[3], m1 - p1, dm1);
-          float dn2 = cf.dni2[0] * (l4 + r4);
-          dn2 = __fmaf_rn(cf.dni2[1], l3 + r3, dn2);
-          dn2 = __fmaf_rn(cf.dni2[2], l2 + r2, dn2);
-          dn2 = __fmaf_rn(cf.dni2[3], l1 + r1, dn2);
-          float dn1 = cf.dni1[0] * (l4 - r4);
-          dn1 = __fmaf_rn(cf.dni1[1], l3 - r3, dn1);
-          dn1 = __fmaf_rn(cf.dni1[2], l2 - r2, dn1);
-          dn1 = __fmaf_rn(cf.dni1[3], l1 - r1, dn1);
-          const float cc = __fmaf_rn(g.d_nu32[col - 4], dn1, __fmaf_rn(bt[row - 4], dm1, dm2) + dn2);
-          const float v = __fmaf_rn(omega1, *p, WS[ls] * (RS[ls] - cc));
-          *p = v;
-          if (up && row < R0 + 4) up[(row - R0up + 4) * n8 + col] = v;
-          if (dn && row >= R1 - 4) dn[(row - R0dn + 4) * n8 + col] = v;
-        }
+      const int *o = SO + c * S;
+      // level-0 points off the shared edges need only this CTA's values
+      cluster_chunks<false>(B, o[0], o[1]);
+      // halos hold the neighbours' previous colour, and the neighbours no
+      // longer read the halo values this colour overwrites
+      cluster_wait();
+      cluster_chunks<true>(B, o[1], o[2]);
+      __syncthreads();
+      for (int l = 1; l < nlev; ++l) {
+        if (o[l + 1] == o[l + 2]) continue;
+        cluster_chunks<true>(B, o[l + 1], o[l + 2]);
         __syncthreads();
       }
-      cl.sync();
+      cluster_arrive();
     }
   }
-  smem_boundary(g, E, R0, R1, rank, even, ex);
-  __syncthreads();
-  // u += e on the CTA's interior points, then the FP64 axis of u
-  const int ra = (R0 < 5) ? 5 : R0;
-  const int ncols = nni - 2, npts = (R1 - ra) * ncols;
-  for (int k = threadIdx.x; k < npts; k += blockDim.x) {
+  cluster_wait();  // no CTA leaves while a neighbour may still write its halo
+  // the band's interior corrections out to the job's FP32 array
+  float *const e32 = J.e32;
+  for (int k = threadIdx.x; k < nband; k += blockDim.x) {
     const int row = ra + k / ncols, col = 5 + k % ncols;
-    u[row * n8 + col] += double(E[(row - R0 + 4) * n8 + col]);
-  }
-  __syncthreads();
-  {
-    const int nrow7 = (rank == 0) ? nni - 2 : 0;
-    const int nside = 2 * (R1 - ra);
-    auto ex64 = [&](int ij, int st) {
-      return A(A(A(A(M(g.exeven[0], u[ij + st]), M(g.exeven[1], u[ij + 2 * st])), M(g.exeven[2], u[ij + 3 * st])),
-                 M(g.exeven[3], u[ij + 4 * st])),
-               M(g.exeven[4], u[ij + 5 * st]));
-    };
-    for (int k = threadIdx.x; k < nrow7 + nside; k += blockDim.x) {
-      if (k < nrow7) {
-        const int ij = 4 * n8 + 5 + k;
-        u[ij] = even ? ex64(ij, n8) : 0.0;
-      } else {
-        const int q = k - nrow7, r = ra + q / 2, side = q % 2;
-        const int ij = r * n8 + (side == 0 ? 4 : nni + 3);
-        u[ij] = even ? ex64(ij, side == 0 ? 1 : -1) : 0.0;
-      }
-    }
-    __syncthreads();
-    if (rank == 0 && threadIdx.x < 2) {
-      const int ij = 4 * n8 + (threadIdx.x == 0 ? 4 : nni + 3);
-      u[ij] = even ? ex64(ij, threadIdx.x == 0 ? 1 : -1) : 0.0;
-    }
+    e32[row * n8 + col] = E[(row - R0 + 4) * n8 + col];
   }
 }
 
@@ -596,7 +650,7 @@ __global__ void k_residual(GridDev g, const JobDev *__restrict__ jobs, int zero_
     const double cc = fma(d, dn1, fma(b, dm1, dm2) + dn2);
     const double res = rhs - cc - lhs * u[ij];
     J.r32[ik] = float(res);
-    J.l32[ik] = float(lhs);
+    J.w32[ik] = J.omegaf / float(lhs);
   }
 }
 
@@ -1095,6 +1149,8 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
     d.psa = x.psa;
     d.psb = x.psb;
     d.omega = x.omega;
+    d.omegaf = float(x.omega);
+    d.omega1f = float(1.0 - x.omega);
     d.idel2 = double(x.idel * x.idel);
     d.isym = x.isym;
     // kind 0 orbital (borb); 1 potential built from psa/psb; 2 potential
@@ -1104,12 +1160,12 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
     if (mixed) {
       d.e32 = reinterpret_cast<float *>(p);
       d.r32 = reinterpret_cast<float *>(p + (size_t(g.next) * sizeof(float) + 127) / 128 * 128);
-      d.l32 = d.r32 + g.mxsize;
+      d.w32 = d.r32 + g.mxsize;
       d.rhs_buf = nullptr;
     } else {
       d.rhs_buf = reinterpret_cast<double *>(p);
       d.e32 = nullptr;
-      d.r32 = d.l32 = nullptr;
+      d.r32 = d.w32 = nullptr;
     }
   }
   JobDev *djobs = reinterpret_cast<JobDev *>(ws);
@@ -1123,7 +1179,7 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
   if (on_chip) {
     // the cluster must be schedulable on this device (shared memory per CTA,
     // non-portable sizes above 8): ask the occupancy calculator once
-    const size_t smem = size_t(g.cl_maxrows + 8) * g.n8 * sizeof(float) + 2 * size_t(g.cl_maxrows) * g.n8 * sizeof(float);
+    const size_t smem = cluster_smem_bytes(g);
     const long key = long(smem) * 64 + g.cl_size;
     if (ctx->cluster_checked_key != key) {
       ctx->cluster_checked_key = key;
@@ -1164,7 +1220,7 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
     ctx->launches += 2;
   }
   if (on_chip) {
-    const size_t smem = size_t(g.cl_maxrows + 8) * g.n8 * sizeof(float) + 2 * size_t(g.cl_maxrows) * g.n8 * sizeof(float);
+    const size_t smem = cluster_smem_bytes(g);
     if (smem > ctx->cluster_smem_set) {
       err = cudaFuncSetAttribute((const void *)k_mixed_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  int(smem));
@@ -1209,7 +1265,11 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
       cudaEventRecord(pe.b, ctx->stream);
       ctx->pending.push_back(pe);
     }
-    ctx->launches += 1;
+    // u += e and the FP64 axis of u, on the whole GPU
+    dim3 gu(grid_blocks((g.nni - 2) * (g.nmu - 5)), njobs);
+    k_update<<<gu, kThreads, 0, ctx->stream>>>(g, djobs);
+    k_extrap_jobs<<<njobs, kThreads, 0, ctx->stream>>>(g, djobs);
+    ctx->launches += 3;
     return X2G_OK;
   }
   static int max_f64 = -1, max_f32 = -1;
@@ -1293,6 +1353,8 @@ int launch_relax_in_scratch(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, i
     d.psa = x.psa;
     d.psb = x.psb;
     d.omega = x.omega;
+    d.omegaf = float(x.omega);
+    d.omega1f = float(1.0 - x.omega);
     d.idel2 = double(x.idel * x.idel);
     d.isym = x.isym;
     d.kind = (x.kind == 1 && explicit_lr) ? 2 : x.kind;

@@ -280,7 +280,8 @@ std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf
   for (size_t k = 0; k < g.pts.size(); ++k) g.pts_rc[k] = ((g.pts[k] / g.n8) << 16) | (g.pts[k] % g.n8);
   // cluster plan for the on-chip FP32 sweep: contiguous tile ranges, ~30
   // rows per CTA, 2..16 CTAs; each CTA keeps its FP32 band with 4-row halos
-  // plus the band's residual and omega/lhs in shared memory
+  // plus the band's residual, omega/lhs, coefficient rows and point list in
+  // shared memory
   g.cl_size = 0;
   {
     const int rows = nmu - 4;
@@ -305,28 +306,78 @@ std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf
         maxrows = std::max(maxrows, g.tile_row1[t0[k + 1] - 1] - g.tile_row0[t0[k]]);
       }
       r0[C] = nmu;
-      const size_t smem = size_t(maxrows + 8) * g.n8 * sizeof(float) + 2 * size_t(maxrows) * g.n8 * sizeof(float);
+      // per (CTA, colour) nlev+1 segments: level-0 points whose stencil
+      // stays inside the band, level-0 points within 4 rows of an edge
+      // shared with another CTA (they read and feed halos), then levels
+      // 1..nlev-1.  Each segment is stored as chunks of up to 4 of its points
+      // on one row at stride 5 (same-colour points of a row are 5 columns
+      // apart), packed (band row << 19) | (col << 2) | (count - 1).
+      const int S = g.nlev + 1;
+      std::vector<int> chunks, coff(size_t(C) * 5 * S + 1, 0);
+      int maxchunks = 0;
+      for (int k = 0; k < C; ++k) {
+        const int first = int(chunks.size());
+        auto edge = [&](int row) { return (k > 0 && row < r0[k] + 4) || (k < C - 1 && row >= r0[k + 1] - 4); };
+        for (int c = 0; c < 5; ++c)
+          for (int seg = 0; seg < S; ++seg) {
+            coff[(size_t(k) * 5 + c) * S + seg] = int(chunks.size());
+            const int l = (seg < 2) ? 0 : seg - 1;
+            std::vector<std::pair<int, int>> pts;
+            for (int t = t0[k]; t < t0[k + 1]; ++t) {
+              const int o = (t * 5 + c) * g.nlev + l;
+              for (int q = g.off[o]; q < g.off[o + 1]; ++q) {
+                const int row = g.pts_rc[q] >> 16, col = g.pts_rc[q] & 0xffff;
+                if (seg < 2 && edge(row) != (seg == 1)) continue;
+                pts.push_back({row, col});
+              }
+            }
+            std::sort(pts.begin(), pts.end());
+            // chunks bucketed by the shared-memory bank of their first point;
+            // dealing the buckets round-robin gives every warp's 32 chunks
+            // distinct banks where the buckets allow (the stencil reads of a
+            // chunk sit at fixed offsets from its first point)
+            std::vector<std::vector<int>> bank(32);
+            for (size_t i = 0; i < pts.size();) {
+              size_t n = 1;
+              while (n < 4 && i + n < pts.size() && pts[i + n].first == pts[i].first &&
+                     pts[i + n].second == pts[i + n - 1].second + 5)
+                ++n;
+              const int lr = pts[i].first - r0[k];
+              bank[((lr + 4) * g.n8 + pts[i].second) % 32].push_back(
+                  int((unsigned(lr) << 19) | (unsigned(pts[i].second) << 2) | unsigned(n - 1)));
+              i += n;
+            }
+            for (size_t depth = 0, left = 1; left;) {
+              left = 0;
+              for (auto &bk : bank)
+                if (depth < bk.size()) {
+                  chunks.push_back(bk[depth]);
+                  left = 1;
+                }
+              ++depth;
+            }
+          }
+        maxchunks = std::max(maxchunks, int(chunks.size()) - first);
+      }
+      coff[size_t(C) * 5 * S] = int(chunks.size());
+      // shared memory: (residual, omega/lhs) pairs, correction band with
+      // 4-row halos, b(mu) of the band's rows, d(nu) by column, the segment
+      // offsets, then the CTA's chunk list
+      const size_t smem = 2 * size_t(maxrows) * g.n8 * sizeof(float) + size_t(maxrows + 8) * g.n8 * sizeof(float) +
+                          size_t(maxrows + g.n8) * sizeof(float) + size_t(5 * S + 1) * sizeof(int) +
+                          size_t(maxchunks) * sizeof(int);
       // a band must be at least 4 rows (halo pushes go to the next CTA only)
       for (int k = 0; k < C; ++k)
         if (r0[k + 1] - r0[k] < 4) ok = false;
-      if (ok && smem <= 200 * 1024) {
+      if (ok && maxrows < 4096 && g.n8 < (1 << 17) && smem <= 200 * 1024) {
         g.cl_size = C;
         g.cl_maxrows = maxrows;
+        g.cl_maxchunks = maxchunks;
         g.cl_smem = smem;
         g.cl_tile0 = t0;
         g.cl_row0 = r0;
-        g.cl_off.assign(size_t(C) * 5 * g.nlev + 1, 0);
-        g.cl_pts.clear();
-        for (int k = 0; k < C; ++k)
-          for (int c = 0; c < 5; ++c)
-            for (int l = 0; l < g.nlev; ++l) {
-              g.cl_off[(size_t(k) * 5 + c) * g.nlev + l] = int(g.cl_pts.size());
-              for (int t = t0[k]; t < t0[k + 1]; ++t) {
-                const int o = (t * 5 + c) * g.nlev + l;
-                for (int q = g.off[o]; q < g.off[o + 1]; ++q) g.cl_pts.push_back(g.pts_rc[q]);
-              }
-            }
-        g.cl_off[size_t(C) * 5 * g.nlev] = int(g.cl_pts.size());
+        g.cl_pts = chunks;
+        g.cl_off = coff;
       }
     }
   }
@@ -411,5 +462,19 @@ extern "C" int x2g_host_cluster_plan(int nnu, int nmu, int *csize, int *maxrows,
   if (maxrows) *maxrows = g.cl_maxrows;
   if (smem) *smem = long(g.cl_smem);
   if (row0 && g.cl_size > 0) std::copy(g.cl_row0.begin(), g.cl_row0.end(), row0);
+  return X2G_OK;
+}
+
+// Chunk lists of the on-chip sweep: nchunks packed chunks and noff segment
+// offsets (CTA-major, 5 colours x (nlevels + 1) segments per CTA, plus the
+// end).  Call with null arrays for the counts.
+extern "C" int x2g_host_cluster_chunks(int nnu, int nmu, int *nchunks, int *noff, int *chunks, int *off) {
+  x2g::HostGrid g;
+  std::string msg = x2g::build_host_grid(g, nnu, nmu, 2.0, 40.0, 1.0, 1.0, 4);
+  if (!msg.empty()) return X2G_ERR_SCHEDULE;
+  if (nchunks) *nchunks = int(g.cl_pts.size());
+  if (noff) *noff = int(g.cl_off.size());
+  if (chunks) std::copy(g.cl_pts.begin(), g.cl_pts.end(), chunks);
+  if (off) std::copy(g.cl_off.begin(), g.cl_off.end(), off);
   return X2G_OK;
 }
