@@ -122,6 +122,11 @@ int x2g_host_cluster_chunks(int nnu, int nmu, int *nchunks, int *noff, int *chun
 /* Mixed form sweep path: 1 (default) on-chip cluster kernel where the grid
  * fits, 0 the grid-barrier FP32 kernel. */
 int x2g_set_mixed_on_chip(x2g_ctx *ctx, int on);
+/* Self-check of the mixed form's integer-pipe FP64<->FP32 conversions
+ * against the hardware conversions on n values (edge cases, then hashed bit
+ * patterns from seed); mismatches outside the documented flush-to-zero
+ * range of float subnormals.  No reference counterpart. */
+int x2g_convert_selftest(x2g_ctx *ctx, long n, unsigned long long seed, unsigned long long *mismatches);
 /* Schedule statistics: tiles (row bands), colour levels, points per sweep. */
 int x2g_grid_info(x2g_grid *grid, int *nnu, int *nmu, int *ntiles, int *nlevels, int *npoints);
 

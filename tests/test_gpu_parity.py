@@ -204,3 +204,11 @@ def test_scf_he_mixed_converges_to_fp64():
         s.close()
     assert abs(e[xg.MIXED] - e[xg.FP64]) < 1e-9
     ctx.close()
+
+
+def test_integer_pipe_conversions_match_hardware(ctx):
+    """The mixed form narrows its FP64 residual and widens its FP32 correction
+    with integer operations; they equal the hardware conversions bit for bit
+    (NaN to NaN) on edge cases and 16M hashed bit patterns, outside the float
+    subnormal range that they flush to zero."""
+    assert ctx.convert_selftest(1 << 24, seed=12345) == 0

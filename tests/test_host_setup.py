@@ -94,17 +94,24 @@ def test_large_grid_has_no_cluster_plan():
 @pytest.mark.parametrize("nnu,nmu", [(31, 31), (91, 121), (151, 241), (331, 481)])
 def test_cluster_chunks_cover_schedule(nnu, nmu):
     """The on-chip sweep's chunks hold every scheduled point exactly once, in
-    its CTA's band and in the segment of its colour and level; a chunk is up
-    to 4 points of one row at stride 5; edge segments hold exactly the rows
-    within 4 of a band edge shared with another CTA."""
+    its CTA's band and in the segment of its colour and kind: level-0 points
+    off the shared band edges, level-0 points within 4 rows of one, level-0
+    seam points (a same-colour stencil neighbour has a higher level), then
+    one segment per higher level.  A chunk is up to 4 points of one row at
+    stride 5."""
     C, maxrows, smem, row0 = xg.host_cluster_plan(nnu, nmu)
     ch, off = xg.host_cluster_chunks(nnu, nmu)
-    order, pts, tile, col, lev = xg.host_schedule(nnu, nmu)
+    order, pts, tile, colour, lev = xg.host_schedule(nnu, nmu)
     nlev = int(lev.max()) + 1
-    S = nlev + 1
+    S = nlev + 2
     assert off.size == C * 5 * S + 1 and off[-1] == ch.size
     n8 = nnu + 8
-    want = {int(p): (int(c), int(l)) for p, c, l in zip(pts, col, lev)}
+    info = {int(p): (int(c), int(l)) for p, c, l in zip(pts, colour, lev)}
+    offsets = [d for k in range(1, 5) for d in (k, -k, k * n8, -k * n8)]
+    seam = set()
+    for p, (c, l) in info.items():
+        if l == 0 and any(info.get(p + d, (-1, 0))[0] == c and info[p + d][1] > 0 for d in offsets):
+            seam.add(p)
     seen = set()
     for k in range(C):
         for c in range(5):
@@ -117,11 +124,13 @@ def test_cluster_chunks_cover_schedule(nnu, nmu):
                     edge = (k > 0 and row < row0[k] + 4) or (k < C - 1 and row >= row0[k + 1] - 4)
                     for j in range(n):
                         p = row * n8 + cl + 5 * j
-                        assert p in want and p not in seen
+                        assert p in info and p not in seen
                         seen.add(p)
-                        assert want[p][0] == c
-                        if seg < 2:
-                            assert want[p][1] == 0 and edge == (seg == 1)
+                        assert info[p][0] == c
+                        if seg < 3:
+                            assert info[p][1] == 0 and (p in seam) == (seg == 2)
+                            if seg < 2:
+                                assert edge == (seg == 1)
                         else:
-                            assert want[p][1] == seg - 1
-    assert len(seen) == len(want)
+                            assert info[p][1] == seg - 2
+    assert len(seen) == len(info)

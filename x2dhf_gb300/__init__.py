@@ -73,6 +73,7 @@ EXPORTS = [
     "x2g_kernel_launches", "mcsor_pthread_", "mcsor_tpool_", "coulExch_pthread_", "coulExch_tpool_",
     "tpoolStop4mcsor_", "tpoolStop4pots_", "x2g_host_table", "x2g_host_schedule", "x2g_profile",
     "x2g_relax_noalloc", "x2g_host_cluster_plan", "x2g_set_mixed_on_chip", "x2g_host_cluster_chunks",
+    "x2g_convert_selftest",
 ]
 
 _lib = None
@@ -105,6 +106,7 @@ def lib():
     L.x2g_grid_info.argtypes = [P] + [C.POINTER(C.c_int)] * 5
     L.x2g_relax.argtypes = [P, P, C.POINTER(Job), I, I, I]
     L.x2g_relax_noalloc.argtypes = [P, P, C.POINTER(Job), I, I]
+    L.x2g_convert_selftest.argtypes = [P, C.c_long, C.c_ulonglong, C.POINTER(C.c_ulonglong)]
     L.x2g_putin.argtypes = [P, P, I, P, P]
     L.x2g_putout.argtypes = [P, P, P, P]
     L.x2g_mcsor_host.argtypes = [P, P, I, I, D, I, dp, dp, dp]
@@ -341,6 +343,12 @@ class Context:
 
     def set_mixed_on_chip(self, on):
         _check(self.L.x2g_set_mixed_on_chip(self.h, 1 if on else 0))
+
+    def convert_selftest(self, n, seed=1):
+        """Mismatches of the integer-pipe FP64<->FP32 conversions against the hardware ones."""
+        bad = C.c_ulonglong()
+        _check(self.L.x2g_convert_selftest(self.h, n, seed, C.byref(bad)))
+        return bad.value
 
     def profile(self, enable=-1, precision=FP64):
         """Sweep-kernel CUDA-event timing: (ms, point_updates, launches)."""

@@ -162,6 +162,11 @@ int x2g_profile(x2g_ctx *c, int enable, int precision, double *ms, double *point
 
 long x2g_kernel_launches(x2g_ctx *c) { return c ? c->launches : 0; }
 
+int x2g_convert_selftest(x2g_ctx *c, long n, unsigned long long seed, unsigned long long *mismatches) {
+  if (!c || !mismatches || n < 0) return set_status(X2G_ERR_ARG, "bad argument");
+  return convert_selftest(c, n, seed, mismatches);
+}
+
 int x2g_set_mixed_on_chip(x2g_ctx *c, int on) {
   if (!c) return set_status(X2G_ERR_ARG, "null context");
   c->no_cluster = on ? 0 : 1;
@@ -247,6 +252,19 @@ int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, doubl
   d.diag = h.diag;
   std::vector<float> b32(h.borb_mu.begin(), h.borb_mu.end()), p32(h.bpot_mu.begin(), h.bpot_mu.end()),
       d32(h.d_nu.begin(), h.d_nu.end());
+  std::vector<double> cmo(size_t(h.nmu) * 8), cmp(size_t(h.nmu) * 8), cnu(size_t(h.nni) * 8);
+  for (int mu = 0; mu < h.nmu; ++mu)
+    for (int q = 0; q < 4; ++q) {
+      cmo[mu * 8 + q] = h.dmu2[q] + h.borb_mu[mu] * h.dmu1[q];
+      cmo[mu * 8 + 4 + q] = h.dmu2[q] - h.borb_mu[mu] * h.dmu1[q];
+      cmp[mu * 8 + q] = h.dmu2[q] + h.bpot_mu[mu] * h.dmu1[q];
+      cmp[mu * 8 + 4 + q] = h.dmu2[q] - h.bpot_mu[mu] * h.dmu1[q];
+    }
+  for (int nu = 0; nu < h.nni; ++nu)
+    for (int q = 0; q < 4; ++q) {
+      cnu[nu * 8 + q] = h.dni2[q] + h.d_nu[nu] * h.dni1[q];
+      cnu[nu * 8 + 4 + q] = h.dni2[q] - h.d_nu[nu] * h.dni1[q];
+    }
   const void *tmp;
   int rc = X2G_OK;
 #define UP(vec, field)                                                                  \
@@ -284,6 +302,9 @@ int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, doubl
   d.cl_size = h.cl_size;
   d.cl_maxrows = h.cl_maxrows;
   d.cl_maxchunks = h.cl_maxchunks;
+  d.cl_wa = h.cl_wa;
+  d.cl_wb = h.cl_wb;
+  d.cl_ws = h.cl_ws;
   if (h.cl_size > 0) {
     UP(h.cl_tile0, cl_tile0);
     UP(h.cl_row0, cl_row0);
@@ -295,7 +316,28 @@ int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, doubl
   UP(b32, borb_mu32);
   UP(p32, bpot_mu32);
   UP(d32, d_nu32);
+  UP(cmo, cmu_orb);
+  UP(cmp, cmu_pot);
+  UP(cnu, cnu);
 #undef UP
+  {
+    double *exm = nullptr, *asy = nullptr;
+    cudaError_t e = cudaMalloc(&exm, size_t(40) * h.mxsize * sizeof(double));
+    if (e == cudaSuccess) gr->allocs.push_back(exm);
+    if (e == cudaSuccess) e = cudaMalloc(&asy, size_t(50) * 4 * h.nni * sizeof(double));
+    if (e == cudaSuccess) gr->allocs.push_back(asy);
+    if (e != cudaSuccess) {
+      rc = cuda_status(e, "moment tables");
+      x2g_grid_destroy(gr);
+      return rc;
+    }
+    d.exm = exm;
+    d.asy = asy;
+    if ((rc = build_moment_tables(ctx, d, exm, asy)) != X2G_OK) {
+      x2g_grid_destroy(gr);
+      return rc;
+    }
+  }
   *out = gr;
   return set_status(X2G_OK, "");
 }

@@ -41,14 +41,16 @@ struct HostGrid {
   std::vector<int> pts_rc;  // same points as (ext row << 16) | ext col
   // cluster plan of the on-chip FP32 sweep: cl_size CTAs per job, CTA k
   // owns tiles [cl_tile0[k], cl_tile0[k+1]) = ext rows [cl_row0[k], cl_row0[k+1])
-  int cl_size = 0, cl_maxrows = 0, cl_maxchunks = 0;
+  int cl_size = 0, cl_maxrows = 0, cl_maxchunks = 0, cl_wa = 1, cl_wb = 1, cl_ws = 1;
   size_t cl_smem = 0;
   std::vector<int> cl_tile0, cl_row0;
   // the CTAs' points regrouped [cta][colour][segment] as chunks of up to 4
   // points of one row at stride 5, packed (band row << 19) | (col << 2) |
-  // (count - 1); segments: level 0 off the band edges, level 0 within 4 rows
-  // of an edge shared with another CTA, then levels 1..nlev-1; cl_off has
-  // cl_size * 5 * (nlev + 1) + 1 chunk offsets
+  // (count - 1); segments: level-0 points off the band edges, level-0 points
+  // within 4 rows of an edge shared with another CTA, level-0 seam points
+  // (same-colour neighbours of higher levels), then levels 1..nlev-1; cl_off
+  // has cl_size * 5 * (nlev + 2) + 1 chunk offsets; cl_wa/wb/ws warps per
+  // CTA work on the three kinds
   std::vector<int> cl_pts, cl_off;
 };
 
@@ -66,10 +68,22 @@ struct GridDev {
   const double *dmu9, *dni9;
   const double *vxi, *vxisq, *veta, *vetasq;
   const int *tile_row0, *tile_row1, *pts, *off, *pts_rc;
-  int cl_size, cl_maxrows, cl_maxchunks;
+  int cl_size, cl_maxrows, cl_maxchunks, cl_wa, cl_wb, cl_ws;
   const int *cl_tile0, *cl_row0, *cl_pts, *cl_off;
   // FP32 copies of the coefficient tables for the mixed form
   const float *borb_mu32, *bpot_mu32, *d_nu32;
+  // separable stencil weights of the mixed form's FP64 residual: for the
+  // neighbours at distance 4,3,2,1 before and after the point, cmu_*[mu * 8 +
+  // q] = dmu2 + b dmu1 (q < 4, before) and dmu2 - b dmu1 (q >= 4, after) with
+  // b = borb or bpot; cnu[nu * 8 + q] likewise with dni2, d(nu), dni1
+  const double *cmu_orb, *cmu_pot, *cnu;
+  // per-grid moment tables (built on the device at grid creation):
+  // exm[(idel * 8 + q) * mxsize + k] = wgt2 f4 P_{q+1}^idel(cos th) (r2 r)^(q+1)
+  // for idel 0..4, q < mpole; asy[slot * 4 nni + p] on the 4 boundary rows
+  // (p = row * nni + nu): slot 0 r2 xi, 1 1/(r2 r), 2+m-1 P_m(cos th)
+  // (r2 r)^-(m+1) for m = 1..8, 10 + idel * 8 + m-1 the exchange functions
+  // P_m^idel(cos th) (r2 r)^-(m+1)
+  const double *exm, *asy;
   // FP32 stencil weights, rounded on the host: GB300 issues double->float
   // conversions on its narrow FP64 pipe, so the FP32 kernels never convert
   float dmu1f[4], dmu2f[4], dni1f[4], dni2f[4], exevenf[5];

@@ -370,11 +370,10 @@ __global__ void __launch_bounds__(kThreads) k_mcsor_f32(GridDev g, const JobDev 
 // coefficient rows and its point list; after updating a point within 4 rows
 // of its band edge it also stores the value into the neighbouring CTA's halo
 // through distributed shared memory, and the colour phases are separated by
-// the cluster's hardware barrier.  Ends by writing e of the band's interior
-// points to the job's FP32 correction array (u += e and the FP64 axis
-// extrapolation run afterwards on the whole GPU).
+// the cluster's hardware barrier.  Ends with u += e (FP64) on the band's
+// interior points and the FP64 axis re-extrapolation of u.
 // ----------------------------------------------------------------------
-constexpr int kClusterThreads = 512;
+constexpr int kClusterMaxThreads = 768;  // 24 warps: interior + edge + seam roles
 
 __device__ __forceinline__ float ex5f(const float *ex, const float *p, int s) {
   return ex[0] * p[s] + ex[1] * p[2 * s] + ex[2] * p[3 * s] + ex[3] * p[4 * s] + ex[4] * p[5 * s];
@@ -408,7 +407,7 @@ __device__ void smem_boundary(const GridDev &g, float *E, int R0, int R1, int ra
 // rows, d(nu) by ext column, the CTA's segment offsets, then its chunk list
 size_t cluster_smem_bytes(const GridDev &g) {
   return 2 * size_t(g.cl_maxrows) * g.n8 * sizeof(float) + size_t(g.cl_maxrows + 8) * g.n8 * sizeof(float) +
-         size_t(g.cl_maxrows + g.n8) * sizeof(float) + size_t(5 * (g.nlev + 1) + 1) * sizeof(int) +
+         size_t(g.cl_maxrows + g.n8) * sizeof(float) + size_t(5 * (g.nlev + 2) + 1) * sizeof(int) +
          size_t(g.cl_maxchunks) * sizeof(int);
 }
 
@@ -416,6 +415,48 @@ size_t cluster_smem_bytes(const GridDev &g) {
 // distributed-shared writes, wait acquires every CTA's released writes
 __device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
 __device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
+// float -> double by bit manipulation on the integer pipes (GB300 issues
+// conversion instructions on its narrow FP64 pipe); exact for normal floats,
+// infinities and NaNs; float subnormals (|e| < 1.2e-38, far below any
+// correction that matters) become signed zero
+__device__ __forceinline__ double widen_f32(float f) {
+  const unsigned b = __float_as_uint(f), ex = (b >> 23) & 0xffu, m = b & 0x7fffffu;
+  const unsigned sign = b & 0x80000000u;
+  if (ex == 0) return __hiloint2double(int(sign), 0);
+  const unsigned dex = (ex == 0xffu) ? 0x7ffu : ex + 896u;
+  return __hiloint2double(int(sign | (dex << 20) | (m >> 3)), int(m << 29));
+}
+
+// FP64 axis extrapolation of one point from its 5 neighbours at stride st
+// (sormcsor.F90:94-129 order)
+__device__ __forceinline__ double extrap64(const GridDev &g, const double *u, int ij, int st) {
+  return A(A(A(A(M(g.exeven[0], u[ij + st]), M(g.exeven[1], u[ij + 2 * st])), M(g.exeven[2], u[ij + 3 * st])),
+             M(g.exeven[3], u[ij + 4 * st])),
+           M(g.exeven[4], u[ij + 5 * st]));
+}
+
+// (row, col) of the points k, k+T, k+2T, ... of a band's interior listed
+// row by row from (ra, 5) with ncols columns per row, advanced without
+// division
+struct BandWalk {
+  int row, col, step_r, step_c, col_end, ncols;
+  __device__ BandWalk(int k, int T, int ra, int nc) : ncols(nc) {
+    row = ra + k / nc;
+    col = 5 + k % nc;
+    step_r = T / nc;
+    step_c = T % nc;
+    col_end = 5 + nc;
+  }
+  __device__ __forceinline__ void next() {
+    row += step_r;
+    col += step_c;
+    if (col >= col_end) {
+      col -= ncols;
+      ++row;
+    }
+  }
+};
 
 struct ClusterBand {
   float *E;               // correction rows [R0-4, R1+4) of the band
@@ -492,13 +533,19 @@ __device__ __forceinline__ void cluster_chunk(const ClusterBand &B, unsigned q) 
   }
 }
 
-// update chunks [b0, b1) of the CTA's list (their points are independent)
+// update chunks [b0, b1) of the CTA's list (their points are independent),
+// thread t of the n threads of a warp role taking chunks t, t+n, ...
 template <bool halo>
-__device__ __forceinline__ void cluster_chunks(const ClusterBand &B, int b0, int b1) {
-  for (int k = b0 + threadIdx.x; k < b1; k += blockDim.x) cluster_chunk<halo>(B, B.PL[k]);
+__device__ __forceinline__ void cluster_chunks(const ClusterBand &B, int b0, int b1, int t, int n) {
+  for (int k = b0 + t; k < b1; k += n) cluster_chunk<halo>(B, B.PL[k]);
 }
 
-__global__ void __launch_bounds__(kClusterThreads, 1) k_mixed_cluster(GridDev g, const JobDev *__restrict__ jobs,
+// barrier among the seam warps only (named barrier 1)
+__device__ __forceinline__ void seam_barrier(int nthreads) {
+  asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
+}
+
+__global__ void __launch_bounds__(kClusterMaxThreads, 1) k_mixed_cluster(GridDev g, const JobDev *__restrict__ jobs,
                                                                         int nsweeps) {
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
@@ -508,7 +555,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_mixed_cluster(GridDev g,
   const bool even = (J.isym == 1);
   const float *const bt = (J.kind >= 1) ? g.bpot_mu32 : g.borb_mu32;
   extern __shared__ float2 smem2[];
-  const int n8 = g.n8, nni = g.nni, nlev = g.nlev, S = nlev + 1;
+  const int n8 = g.n8, nni = g.nni, nlev = g.nlev, S = nlev + 2;
   const int R0 = g.cl_row0[rank], R1 = g.cl_row0[rank + 1];
   const int nloc = (g.cl_maxrows + 8) * n8;
   float2 *const RW = smem2;
@@ -525,10 +572,27 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_mixed_cluster(GridDev g,
   for (int k = threadIdx.x; k < n8; k += blockDim.x) DN[k] = (k >= 4 && k < nni + 4) ? g.d_nu32[k - 4] : 0.0f;
   for (int k = threadIdx.x; k < npl; k += blockDim.x) PL[k] = unsigned(g.cl_pts[pbase + k]);
   const int ra = (R0 < 5) ? 5 : R0, ncols = nni - 2, nband = (R1 - ra) * ncols;
-  for (int k = threadIdx.x; k < nband; k += blockDim.x) {
-    const int row = ra + k / ncols, col = 5 + k % ncols;
-    const int ik = (row - 4) * nni + (col - 4);
-    RW[(row - R0) * n8 + col] = make_float2(r32[ik], w32[ik]);
+  {
+    // four points per thread in flight: all loads before the stores
+    BandWalk w(threadIdx.x, blockDim.x, ra, ncols);
+    for (int k = threadIdx.x; k < nband; k += 4 * blockDim.x) {
+      float rv[4], wv[4];
+      int ls[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        ls[j] = -1;
+        if (k + j * int(blockDim.x) < nband) {
+          const int ik = (w.row - 4) * nni + (w.col - 4);
+          ls[j] = (w.row - R0) * n8 + w.col;
+          rv[j] = r32[ik];
+          wv[j] = w32[ik];
+        }
+        w.next();
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (ls[j] >= 0) RW[ls[j]] = make_float2(rv[j], wv[j]);
+    }
   }
   ClusterBand B;
   B.E = E;
@@ -550,6 +614,12 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_mixed_cluster(GridDev g,
   // neighbours' halo rows, addressed by this CTA's band offsets
   B.up = (rank > 0) ? cl.map_shared_rank(E, rank - 1) + (R0 - g.cl_row0[rank - 1]) * n8 : nullptr;
   B.dn = (rank < C - 1) ? cl.map_shared_rank(E, rank + 1) + (R0 - R1) * n8 : nullptr;
+  // warp roles: interior, edge, seam
+  const int warp = threadIdx.x >> 5;
+  const int role = (warp < g.cl_wa) ? 0 : (warp < g.cl_wa + g.cl_wb) ? 1 : 2;
+  const int rbase = (role == 0) ? 0 : (role == 1) ? g.cl_wa : g.cl_wa + g.cl_wb;
+  const int rt = threadIdx.x - 32 * rbase;
+  const int rn = 32 * ((role == 0) ? g.cl_wa : (role == 1) ? g.cl_wb : g.cl_ws);
   __syncthreads();
   cluster_arrive();  // this band is zeroed: neighbours may push into its halos
   for (int s = 0; s < nsweeps; ++s) {
@@ -559,27 +629,70 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_mixed_cluster(GridDev g,
         __syncthreads();
       }
       const int *o = SO + c * S;
-      // level-0 points off the shared edges need only this CTA's values
-      cluster_chunks<false>(B, o[0], o[1]);
-      // halos hold the neighbours' previous colour, and the neighbours no
-      // longer read the halo values this colour overwrites
-      cluster_wait();
-      cluster_chunks<true>(B, o[1], o[2]);
-      __syncthreads();
-      for (int l = 1; l < nlev; ++l) {
-        if (o[l + 1] == o[l + 2]) continue;
-        cluster_chunks<true>(B, o[l + 1], o[l + 2]);
-        __syncthreads();
+      // After the cluster wait the halos hold the neighbours' previous
+      // colour, and the neighbours no longer read the halo values this colour
+      // overwrites.  Interior points need only this CTA's values; seam points
+      // go level by level among the seam warps.
+      if (role == 0) {
+        cluster_chunks<false>(B, o[0], o[1], rt, rn);
+        cluster_wait();
+      } else if (role == 1) {
+        cluster_wait();
+        cluster_chunks<true>(B, o[1], o[2], rt, rn);
+      } else {
+        cluster_wait();
+        cluster_chunks<true>(B, o[2], o[3], rt, rn);
+        for (int l = 1; l < nlev; ++l) {
+          if (o[2 + l] == o[3 + l]) continue;
+          seam_barrier(rn);
+          cluster_chunks<true>(B, o[2 + l], o[3 + l], rt, rn);
+        }
       }
+      __syncthreads();
       cluster_arrive();
     }
   }
   cluster_wait();  // no CTA leaves while a neighbour may still write its halo
-  // the band's interior corrections out to the job's FP32 array
-  float *const e32 = J.e32;
-  for (int k = threadIdx.x; k < nband; k += blockDim.x) {
-    const int row = ra + k / ncols, col = 5 + k % ncols;
-    e32[row * n8 + col] = E[(row - R0 + 4) * n8 + col];
+  // u += e on the band's interior points, then the FP64 axis of u for the
+  // band's rows (the mu=1 row and corners by the first CTA, whose band holds
+  // rows 4..9)
+  double *const u = J.u;
+  {
+    BandWalk w(threadIdx.x, blockDim.x, ra, ncols);
+    for (int k = threadIdx.x; k < nband; k += 4 * blockDim.x) {
+      double uv[4];
+      int ij[4], le[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        ij[j] = -1;
+        if (k + j * int(blockDim.x) < nband) {
+          ij[j] = w.row * n8 + w.col;
+          le[j] = (w.row - R0 + 4) * n8 + w.col;
+          uv[j] = u[ij[j]];
+        }
+        w.next();
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (ij[j] >= 0) u[ij[j]] = uv[j] + widen_f32(E[le[j]]);
+    }
+  }
+  __syncthreads();
+  const int nrow7 = (rank == 0) ? nni - 2 : 0, nside = 2 * (R1 - ra);
+  for (int k = threadIdx.x; k < nrow7 + nside; k += blockDim.x) {
+    if (k < nrow7) {
+      const int ij = 4 * n8 + 5 + k;
+      u[ij] = even ? extrap64(g, u, ij, n8) : 0.0;
+    } else {
+      const int q = k - nrow7, r = ra + q / 2, side = q % 2;
+      const int ij = r * n8 + (side == 0 ? 4 : nni + 3);
+      u[ij] = even ? extrap64(g, u, ij, side == 0 ? 1 : -1) : 0.0;
+    }
+  }
+  __syncthreads();
+  if (rank == 0 && threadIdx.x < 2) {
+    const int ij = 4 * n8 + (threadIdx.x == 0 ? 4 : nni + 3);
+    u[ij] = even ? extrap64(g, u, ij, threadIdx.x == 0 ? 1 : -1) : 0.0;
   }
 }
 
@@ -615,42 +728,58 @@ __global__ void k_ghost_jobs(GridDev g, const JobDev *__restrict__ jobs) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) ghost_point(g, J.u, k, J.isym);
 }
 
+// double -> float with round to nearest even, on the integer pipes (GB300
+// issues conversion instructions on its narrow FP64 pipe); values beyond the
+// float range become infinities, values below its normal range signed zero
+__device__ __forceinline__ float narrow_f64(double x) {
+  const unsigned hi = unsigned(__double2hiint(x)), lo = unsigned(__double2loint(x));
+  const unsigned sign = hi & 0x80000000u;
+  const int dex = int((hi >> 20) & 0x7ffu);
+  if (dex == 0x7ff) return __uint_as_float(sign | 0x7f800000u | ((hi & 0xfffffu) ? 0x400000u : 0u));
+  const int fex = dex - 896;
+  if (fex >= 255) return __uint_as_float(sign | 0x7f800000u);
+  if (fex <= 0) return __uint_as_float(sign);
+  // 23 mantissa bits: 20 from hi, 3 from lo; the remaining 29 bits round
+  unsigned bits = (unsigned(fex) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const unsigned rest = lo & 0x1fffffffu;
+  if (rest > 0x10000000u || (rest == 0x10000000u && (bits & 1u))) ++bits;  // may carry into the exponent
+  return __uint_as_float(sign | bits);
+}
+
+// Mixed form residual r = rhs - A u in FP64 over the interior, stored as
+// FP32 with omega / lhs; the stencil uses the grid's separable weights (one
+// FMA per neighbour).
 __global__ void k_residual(GridDev g, const JobDev *__restrict__ jobs, int zero_e) {
   const JobDev &J = jobs[blockIdx.y];
   const int nint = (g.nni - 2) * (g.nmu - 5);
-  const int n1 = g.n8, n2 = 2 * g.n8, n3 = 3 * g.n8, n4 = 4 * g.n8;
+  const int n8 = g.n8;
   if (zero_e)
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.next; k += gridDim.x * blockDim.x) J.e32[k] = 0.0f;
+  const double *cmu = (J.kind == 0) ? g.cmu_orb : g.cmu_pot;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nint; k += gridDim.x * blockDim.x) {
     const int mu = 1 + k / (g.nni - 2), nu = 1 + k % (g.nni - 2);
-    const int ik = mu * g.nni + nu, ij = (mu + 4) * g.n8 + nu + 4;
+    const int ik = mu * g.nni + nu, ij = (mu + 4) * n8 + nu + 4;
     const double *u = J.u;
-    double rhs, lhs, b;
+    double rhs, lhs;
     if (J.kind == 1) {
       rhs = (J.psa[ij] * J.psb[ij]) * g.g[ik];
-      lhs = (J.idel2 == 0.0) ? g.f3_mu[mu] : g.f3_mu[mu] + J.idel2 * g.e[ik];
-      b = g.bpot_mu[mu];
+      lhs = (J.idel2 == 0.0) ? g.f3_mu[mu] : fma(J.idel2, g.e[ik], g.f3_mu[mu]);
     } else {
       rhs = J.rhs[ik];
       lhs = J.lhs[ik];
-      b = (J.kind == 2) ? g.bpot_mu[mu] : g.borb_mu[mu];
     }
-    const double d = g.d_nu[nu];
-    double dm2 = 0, dm1 = 0, dn2 = 0, dn1 = 0;
-    const int offs[4] = {n4, n3, n2, n1};
+    const double *cm = cmu + mu * 8, *cn = g.cnu + nu * 8;
+    double cc = lhs * u[ij];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const double a = u[ij - offs[q]], c = u[ij + offs[q]];
-      dm2 = fma(g.dmu2[q], a + c, dm2);
-      dm1 = fma(g.dmu1[q], a - c, dm1);
-      const double l = u[ij - (4 - q)], r = u[ij + (4 - q)];
-      dn2 = fma(g.dni2[q], l + r, dn2);
-      dn1 = fma(g.dni1[q], l - r, dn1);
+      const int dm = (4 - q) * n8, dn = 4 - q;
+      cc = fma(cm[q], u[ij - dm], cc);
+      cc = fma(cm[4 + q], u[ij + dm], cc);
+      cc = fma(cn[q], u[ij - dn], cc);
+      cc = fma(cn[4 + q], u[ij + dn], cc);
     }
-    const double cc = fma(d, dn1, fma(b, dm1, dm2) + dn2);
-    const double res = rhs - cc - lhs * u[ij];
-    J.r32[ik] = float(res);
-    J.w32[ik] = J.omegaf / float(lhs);
+    J.r32[ik] = narrow_f64(rhs - cc);
+    J.w32[ik] = J.omegaf / narrow_f64(lhs);
   }
 }
 
@@ -888,44 +1017,77 @@ __device__ void assoc_legendre(int mt, int mpole, double costh, double *dome, bo
   for (int k = mpole + 1; k <= 8; ++k) dome[k] = 0.0;
 }
 
+// Moment tables of a grid: exchange moment weights over the plain grid and
+// the boundary functions of potAsympt on mu = nmu-4..nmu-1 (0-based),
+// evaluated once per grid with the formulas of coulAsympt/vcoul,
+// exchAsympt/vexch and exchMom (scfUtils.F90:615-1270).
+__global__ void k_moment_tables(GridDev g, double *exm, double *asy) {
+  const int stride = gridDim.x * blockDim.x;
+  double dome[10];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += stride) {
+    const int mu = k / g.nni, nu = k - mu * g.nni;
+    const double rr = sqrt(g.vxisq[mu] + g.vetasq[nu] - 1.0);
+    const double xrr = g.r2 * rr;
+    const double costh = (fabs(rr) > kPrecis) ? g.veta[nu] * g.vxi[mu] / rr : 0.0;
+    const double wk = g.wgt2[k] * g.f4[k];
+    for (int idel = 0; idel <= 4; ++idel) {
+      assoc_legendre(idel, g.mpole, costh, dome, false);
+      double xw = xrr;
+      for (int q = 0; q < g.mpole; ++q) {
+        if (q > 0) xw = xw * xrr;
+        exm[(size_t(idel) * 8 + q) * g.mxsize + k] = wk * (dome[q + 1] * xw);
+      }
+    }
+  }
+  const int P = 4 * g.nni;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += stride) {
+    const int jj = p / g.nni, i = p - jj * g.nni, j = g.nmu - 4 + jj;
+    const double rr = sqrt(g.vxisq[j] + g.vetasq[i] - 1.0);
+    asy[p] = g.r2 * g.vxi[j];
+    const double rr1 = 1.0 / (rr * g.r2);
+    asy[P + p] = rr1;
+    const double costh = g.veta[i] * g.vxi[j] / rr;
+    dome[1] = costh;
+    dome[2] = (3.0 * costh * costh - 1.0) * 0.5;
+    for (int m = 2; m <= g.mpole - 1; m++)
+      dome[m + 1] = (double(2 * m + 1) * costh * dome[m] - double(m) * dome[m - 1]) / double(m + 1);
+    double rp = rr1;
+    for (int m = 1; m <= 8; m++) {
+      rp = rp * rr1;
+      asy[size_t(2 + m - 1) * P + p] = (m <= g.mpole) ? dome[m] * rp : 0.0;
+    }
+    const double costx = (fabs(rr) > kPrecis) ? costh : 0.0;
+    const double rs = rr * g.r2;
+    for (int idel = 0; idel <= 4; ++idel) {
+      assoc_legendre(idel, g.mpole, costx, dome, true);  // vexch's m=3 branch
+      double xrn = rs;
+      for (int m = 1; m <= 8; m++) {
+        xrn = xrn * rs;
+        asy[size_t(10 + idel * 8 + m - 1) * P + p] = (m <= g.mpole) ? dome[m] / xrn : 0.0;
+      }
+    }
+  }
+}
+
 // potAsympt: Coulomb (coulAsympt/vcoul) and exchange (exchAsympt/vexch)
-// boundary values on mu = nmu-4..nmu-1 (0-based).
+// boundary values on mu = nmu-4..nmu-1 (0-based) from the grid's tables.
 __global__ void k_asympt(GridDev g, AsymptArgs a) {
   const AsymptItem &it = a.it[blockIdx.y];
-  const int n = 4 * g.nni;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    const int jj = k / g.nni, i = k - jj * g.nni;
-    const int j = g.nmu - 4 + jj;
-    const int ij = (j + 4) * g.n8 + i + 4;
-    double rr = sqrt(g.vxisq[j] + g.vetasq[i] - 1.0);
+  const int P = 4 * g.nni;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < P; p += gridDim.x * blockDim.x) {
+    const int jj = p / g.nni, i = p - jj * g.nni;
+    const int ij = (g.nmu + jj) * g.n8 + i + 4;
+    double pe = 0.0;
     if (it.type == 0) {
-      const double rr1 = 1.0 / (rr * g.r2);
-      const double costh = g.veta[i] * g.vxi[j] / rr;
-      double dome[10];
-      dome[1] = costh;
-      dome[2] = (3.0 * costh * costh - 1.0) * 0.5;
-      for (int m = 2; m <= g.mpole - 1; m++)
-        dome[m + 1] = (double(2 * m + 1) * costh * dome[m] - double(m) * dome[m - 1]) / double(m + 1);
-      double pe = 0.0;
-      for (int m = 1; m <= g.mpole; m++)
-        pe = pe + a.cmulti[it.idx * 8 + (m - 1)] * dome[m] * pow(rr1, double(m + 1));
-      it.pot[ij] = g.r2 * g.vxi[j] * (rr1 + pe);
-    } else {
-      double pe = 0.0;
-      if (it.idel <= 4) {
-        const double costh = (fabs(rr) > kPrecis) ? g.veta[i] * g.vxi[j] / rr : 0.0;
-        rr = rr * g.r2;
-        double dome[10];
-        assoc_legendre(it.idel, g.mpole, costh, dome, true);
-        double xrn = rr * rr;
-        pe = dome[1] * a.excm[it.idx * 8 + 0] / xrn;
-        for (int m = 2; m <= g.mpole; m++) {
-          xrn = xrn * rr;
-          pe = pe + dome[m] * a.excm[it.idx * 8 + (m - 1)] / xrn;
-        }
-      }
-      it.pot[ij] = g.r2 * g.vxi[j] * pe;
+      const double *cm = a.cmulti + it.idx * 8;
+      for (int m = 1; m <= g.mpole; m++) pe = fma(cm[m - 1], g.asy[size_t(1 + m) * P + p], pe);
+      pe = g.asy[P + p] + pe;
+    } else if (it.idel <= 4) {
+      const double *xm = a.excm + it.idx * 8;
+      const double *X = g.asy + size_t(10 + it.idel * 8) * P + p;
+      for (int m = 1; m <= g.mpole; m++) pe = fma(X[size_t(m - 1) * P], xm[m - 1], pe);
     }
+    it.pot[ij] = g.asy[p] * pe;
   }
 }
 
@@ -1076,25 +1238,58 @@ __global__ void k_coulmom(GridDev g, const double *psi, int homo, double *partia
   block_sum_store<8>(v, partials);
 }
 
-// exchMom (scfUtils.F90:615-844): normalised P_k^q r^k evaluated on the fly
+// exchMom (scfUtils.F90:615-844) with the grid's weighted P_k^q r^k tables
 __global__ void k_exchmom(GridDev g, const double *psa, const double *psb, int idel, double *partials) {
   double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
-    const int mu = k / g.nni, nu = k - mu * g.nni;
-    const int ij = (mu + 4) * g.n8 + nu + 4;
-    const double rr = sqrt(g.vxisq[mu] + g.vetasq[nu] - 1.0);
-    const double xrr = g.r2 * rr;
-    const double costh = (fabs(rr) > kPrecis) ? g.veta[nu] * g.vxi[mu] / rr : 0.0;
-    double dome[10];
-    assoc_legendre(idel, g.mpole, costh, dome, false);
-    const double wk1 = M(M(psa[ij], psb[ij]), g.f4[k]);
-    double xw = xrr;
-    for (int q = 0; q < g.mpole; ++q) {
-      if (q > 0) xw = xw * xrr;
-      v[q] += g.wgt2[k] * M(dome[q + 1] * xw, wk1);
+  if (idel <= 4) {
+    const double *T = g.exm + size_t(idel) * 8 * g.mxsize;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+      const int mu = k / g.nni, nu = k - mu * g.nni;
+      const int ij = (mu + 4) * g.n8 + nu + 4;
+      const double wk1 = psa[ij] * psb[ij];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (q < g.mpole) v[q] = fma(T[size_t(q) * g.mxsize + k], wk1, v[q]);
     }
   }
   block_sum_store<8>(v, partials);
+}
+
+// Checks narrow_f64 / widen_f32 against the hardware conversions on n
+// values: edge cases, then bit patterns from a counter hash.  Counts
+// mismatches outside the documented flush ranges (float subnormals); NaNs
+// must map to NaNs.
+__global__ void k_convert_selftest(long n, unsigned long long seed, unsigned long long *bad) {
+  unsigned long long nb = 0;
+  for (long i = blockIdx.x * long(blockDim.x) + threadIdx.x; i < n; i += long(gridDim.x) * blockDim.x) {
+    unsigned long long h = (unsigned long long)i * 0x9E3779B97F4A7C15ull + seed;
+    h ^= h >> 31;
+    h *= 0xBF58476D1CE4E5B9ull;
+    h ^= h >> 29;
+    double x = __longlong_as_double((long long)h);
+    if (i < 16) {
+      const double edge[16] = {0.0, -0.0, 1.0, -1.0, 3.4028234663852886e38, 3.4028235677973366e38, 1e39, -1e39,
+                               1.1754943508222875e-38, 1.1754942e-38, 1e-300, 0.1, 1.0 + 0x1p-24, 1.0 + 0x1p-23 + 0x1p-24,
+                               __longlong_as_double(0x7ff0000000000000ll), __longlong_as_double(0x7ff8000000000001ll)};
+      x = edge[i];
+    }
+    // narrowing
+    const float a = narrow_f64(x), b = __double2float_rn(x);
+    const bool sub = fabs(x) < 1.1754943508222875e-38 && x != 0.0;
+    if (!sub) {
+      if (isnan(b)) nb += isnan(a) ? 0 : 1;
+      else nb += (__float_as_uint(a) == __float_as_uint(b)) ? 0 : 1;
+    }
+    // widening of a float pattern
+    const float f = __uint_as_float(unsigned(h >> 32));
+    const double wa = widen_f32(f), wb = double(f);
+    const bool fsub = (__float_as_uint(f) & 0x7f800000u) == 0 && (__float_as_uint(f) & 0x7fffffu) != 0;
+    if (!fsub) {
+      if (isnan(wb)) nb += isnan(wa) ? 0 : 1;
+      else nb += (__double_as_longlong(wa) == __double_as_longlong(wb)) ? 0 : 1;
+    }
+  }
+  if (nb) atomicAdd(bad, nb);
 }
 
 inline int grid_blocks(int n) {
@@ -1180,7 +1375,7 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
     // the cluster must be schedulable on this device (shared memory per CTA,
     // non-portable sizes above 8): ask the occupancy calculator once
     const size_t smem = cluster_smem_bytes(g);
-    const long key = long(smem) * 64 + g.cl_size;
+    const long key = (long(smem) * 64 + g.cl_size) * 32 + (g.cl_wa + g.cl_wb + g.cl_ws);
     if (ctx->cluster_checked_key != key) {
       ctx->cluster_checked_key = key;
       ctx->cluster_ok = 0;
@@ -1194,7 +1389,7 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
         ctx->cluster_nonportable = (g.cl_size > 8);
         cudaLaunchConfig_t q = {};
         q.gridDim = dim3(unsigned(g.cl_size));
-        q.blockDim = dim3(kClusterThreads);
+        q.blockDim = dim3(unsigned(32 * (g.cl_wa + g.cl_wb + g.cl_ws)));
         q.dynamicSmemBytes = smem;
         cudaLaunchAttribute qa[1];
         qa[0].id = cudaLaunchAttributeClusterDimension;
@@ -1234,7 +1429,7 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(unsigned(njobs * g.cl_size));
-    cfg.blockDim = dim3(kClusterThreads);
+    cfg.blockDim = dim3(unsigned(32 * (g.cl_wa + g.cl_wb + g.cl_ws)));
     cfg.dynamicSmemBytes = smem;
     cfg.stream = ctx->stream;
     cudaLaunchAttribute attr[1];
@@ -1265,11 +1460,7 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
       cudaEventRecord(pe.b, ctx->stream);
       ctx->pending.push_back(pe);
     }
-    // u += e and the FP64 axis of u, on the whole GPU
-    dim3 gu(grid_blocks((g.nni - 2) * (g.nmu - 5)), njobs);
-    k_update<<<gu, kThreads, 0, ctx->stream>>>(g, djobs);
-    k_extrap_jobs<<<njobs, kThreads, 0, ctx->stream>>>(g, djobs);
-    ctx->launches += 3;
+    ctx->launches += 1;
     return X2G_OK;
   }
   static int max_f64 = -1, max_f32 = -1;
@@ -1427,6 +1618,28 @@ void launch_ortho_apply(x2g_ctx *ctx, const GridDev &g, double *psi, const doubl
   for (int q = 0; q < n && q < kMaxTerms; ++q) L.p[q] = others[q];
   k_ortho_apply<<<grid_blocks(g.mxsize), kThreads, 0, ctx->stream>>>(g, psi, L, n, ovl_dev);
   ctx->launches++;
+}
+
+int convert_selftest(x2g_ctx *ctx, long n, unsigned long long seed, unsigned long long *mismatches) {
+  unsigned long long *d = nullptr;
+  cudaError_t e = cudaMallocAsync(&d, sizeof(unsigned long long), ctx->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, sizeof(unsigned long long), ctx->stream);
+  if (e == cudaSuccess) {
+    k_convert_selftest<<<4 * ctx->num_sms, kThreads, 0, ctx->stream>>>(n, seed, d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(mismatches, d, sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream);
+  if (d) cudaFreeAsync(d, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  return (e == cudaSuccess) ? X2G_OK : cuda_status(e, "conversion self-test");
+}
+
+int build_moment_tables(x2g_ctx *ctx, const GridDev &g, double *exm, double *asy) {
+  k_moment_tables<<<grid_blocks(g.mxsize), kThreads, 0, ctx->stream>>>(g, exm, asy);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  return (e == cudaSuccess) ? X2G_OK : cuda_status(e, "moment tables");
 }
 
 void launch_asympt(x2g_ctx *ctx, const GridDev &g, const AsymptArgs &a) {

@@ -70,6 +70,10 @@ void launch_scale(x2g_ctx *ctx, const GridDev &g, double *psi, const double *nor
 void launch_ortho_apply(x2g_ctx *ctx, const GridDev &g, double *psi, const double *const *others, int n,
                         const double *ovl_dev);
 void launch_asympt(x2g_ctx *ctx, const GridDev &g, const AsymptArgs &a);
+// narrow_f64 / widen_f32 against the hardware conversions on n values
+int convert_selftest(x2g_ctx *ctx, long n, unsigned long long seed, unsigned long long *mismatches);
+// fills g's exm (40 x mxsize) and asy (50 x 4 nni) tables; synchronous
+int build_moment_tables(x2g_ctx *ctx, const GridDev &g, double *exm, double *asy);
 void launch_zero(x2g_ctx *ctx, double *p, size_t n);
 
 // ---- reductions (deterministic two-pass; results in device memory) ----

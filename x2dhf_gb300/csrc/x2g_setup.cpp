@@ -306,28 +306,39 @@ std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf
         maxrows = std::max(maxrows, g.tile_row1[t0[k + 1] - 1] - g.tile_row0[t0[k]]);
       }
       r0[C] = nmu;
-      // per (CTA, colour) nlev+1 segments: level-0 points whose stencil
-      // stays inside the band, level-0 points within 4 rows of an edge
-      // shared with another CTA (they read and feed halos), then levels
-      // 1..nlev-1.  Each segment is stored as chunks of up to 4 of its points
-      // on one row at stride 5 (same-colour points of a row are 5 columns
-      // apart), packed (band row << 19) | (col << 2) | (count - 1).
-      const int S = g.nlev + 1;
+      // Per (CTA, colour) nlev+2 segments, each processed by its own warps:
+      //   A  level-0 points off the band edges (no halo read or write),
+      //   B  level-0 points within 4 rows of an edge shared with another CTA,
+      //   S0 level-0 points with a same-colour stencil neighbour of a higher
+      //      level (seam points), S1.. the levels 1..nlev-1.
+      // A and B points have no same-colour neighbour at all, so A, B and S0
+      // run concurrently and only the seam warps step through the levels.
+      // Each segment is stored as chunks of up to 4 of its points on one row
+      // at stride 5 (same-colour points of a row are 5 columns apart),
+      // packed (band row << 19) | (col << 2) | (count - 1).
+      const int S = g.nlev + 2;
+      std::vector<char> seam0(g.next, 0);
+      for (auto &d : deps)
+        if (lev[d.first] == 0) seam0[g.order[d.first]] = 1;
       std::vector<int> chunks, coff(size_t(C) * 5 * S + 1, 0);
-      int maxchunks = 0;
+      int maxchunks = 0, maxa = 0, maxb = 0, maxs = 0;
       for (int k = 0; k < C; ++k) {
         const int first = int(chunks.size());
         auto edge = [&](int row) { return (k > 0 && row < r0[k] + 4) || (k < C - 1 && row >= r0[k + 1] - 4); };
         for (int c = 0; c < 5; ++c)
           for (int seg = 0; seg < S; ++seg) {
-            coff[(size_t(k) * 5 + c) * S + seg] = int(chunks.size());
-            const int l = (seg < 2) ? 0 : seg - 1;
+            const int seg0 = int(chunks.size());
+            coff[(size_t(k) * 5 + c) * S + seg] = seg0;
+            const int l = (seg < 2) ? 0 : seg - 2;
             std::vector<std::pair<int, int>> pts;
             for (int t = t0[k]; t < t0[k + 1]; ++t) {
               const int o = (t * 5 + c) * g.nlev + l;
               for (int q = g.off[o]; q < g.off[o + 1]; ++q) {
                 const int row = g.pts_rc[q] >> 16, col = g.pts_rc[q] & 0xffff;
-                if (seg < 2 && edge(row) != (seg == 1)) continue;
+                const bool s0 = seam0[row * g.n8 + col] != 0;
+                if (seg == 0 && (s0 || edge(row))) continue;
+                if (seg == 1 && (s0 || !edge(row))) continue;
+                if (seg == 2 && !s0) continue;
                 pts.push_back({row, col});
               }
             }
@@ -356,6 +367,10 @@ std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf
                 }
               ++depth;
             }
+            const int n = int(chunks.size()) - seg0;
+            if (seg == 0) maxa = std::max(maxa, n);
+            else if (seg == 1) maxb = std::max(maxb, n);
+            else maxs = std::max(maxs, n);
           }
         maxchunks = std::max(maxchunks, int(chunks.size()) - first);
       }
@@ -373,6 +388,16 @@ std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf
         g.cl_size = C;
         g.cl_maxrows = maxrows;
         g.cl_maxchunks = maxchunks;
+        // warps per role: enough for one pass over the largest segment, at
+        // most 24 warps in all (the roles loop when a segment is larger)
+        g.cl_wa = std::max(1, (maxa + 31) / 32);
+        g.cl_wb = std::max(1, (maxb + 31) / 32);
+        g.cl_ws = std::max(1, (maxs + 31) / 32);
+        while (g.cl_wa + g.cl_wb + g.cl_ws > 24) {
+          if (g.cl_wa >= g.cl_wb && g.cl_wa >= g.cl_ws) --g.cl_wa;
+          else if (g.cl_wb >= g.cl_ws) --g.cl_wb;
+          else --g.cl_ws;
+        }
         g.cl_smem = smem;
         g.cl_tile0 = t0;
         g.cl_row0 = r0;
