@@ -324,7 +324,7 @@ int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, doubl
     double *exm = nullptr, *asy = nullptr;
     cudaError_t e = cudaMalloc(&exm, size_t(40) * h.mxsize * sizeof(double));
     if (e == cudaSuccess) gr->allocs.push_back(exm);
-    if (e == cudaSuccess) e = cudaMalloc(&asy, size_t(50) * 4 * h.nni * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&asy, size_t(51) * 4 * h.nni * sizeof(double));
     if (e == cudaSuccess) gr->allocs.push_back(asy);
     if (e != cudaSuccess) {
       rc = cuda_status(e, "moment tables");

@@ -82,7 +82,7 @@ struct GridDev {
   // for idel 0..4, q < mpole; asy[slot * 4 nni + p] on the 4 boundary rows
   // (p = row * nni + nu): slot 0 r2 xi, 1 1/(r2 r), 2+m-1 P_m(cos th)
   // (r2 r)^-(m+1) for m = 1..8, 10 + idel * 8 + m-1 the exchange functions
-  // P_m^idel(cos th) (r2 r)^-(m+1)
+  // P_m^idel(cos th) (r2 r)^-(m+1), 50 orbAsymptGet's raiq(mu-1) - raiq(mu)
   const double *exm, *asy;
   // FP32 stencil weights, rounded on the host: GB300 issues double->float
   // conversions on its narrow FP64 pipe, so the FP32 kernels never convert
@@ -102,6 +102,14 @@ struct JobDev {
   double idel2;
   float omegaf, omega1f;  // omega and 1 - omega rounded to FP32 on the host
   int isym, kind;
+};
+
+// Jobs of one relaxation launch, passed by value as a kernel parameter
+// (__grid_constant__): no host-to-device copy per call.  Larger batches are
+// split into launches of kParamJobs.
+constexpr int kParamJobs = 32;
+struct JobTable {
+  JobDev j[kParamJobs];
 };
 
 // Grid barrier state in device memory.

@@ -264,14 +264,14 @@ __device__ void tile_rhs(const GridDev &g, const JobDev &J, int t) {
 // Persistent cooperative MCSOR kernel: all jobs x tiles, 5 colour phases
 // per micro-sweep, grid barrier between phases.
 // ----------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_mcsor_f64(GridDev g, const JobDev *__restrict__ jobs, int njobs,
+__global__ void __launch_bounds__(kThreads) k_mcsor_f64(GridDev g, const __grid_constant__ JobTable jobs, int njobs,
                                                         int nsweeps, BarrierDev bar, unsigned nblocks) {
   const int nitems = njobs * g.ntiles;
   for (int s = 0; s < nsweeps; ++s) {
     for (int c = 0; c < 5; ++c) {
       for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
         const int jb = item / g.ntiles, t = item - jb * g.ntiles;
-        const JobDev &J = jobs[jb];
+        const JobDev &J = jobs.j[jb];
         double *u = J.u;
         if (c == 0) {
           if (s == 0) {
@@ -310,12 +310,12 @@ __global__ void __launch_bounds__(kThreads) k_mcsor_f64(GridDev g, const JobDev 
   }
   for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
     const int jb = item / g.ntiles, t = item - jb * g.ntiles;
-    tile_boundary<double>(g, jobs[jb].u, t, jobs[jb].isym);
+    tile_boundary<double>(g, jobs.j[jb].u, t, jobs.j[jb].isym);
     __syncthreads();
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_mcsor_f32(GridDev g, const JobDev *__restrict__ jobs, int njobs,
+__global__ void __launch_bounds__(kThreads) k_mcsor_f32(GridDev g, const __grid_constant__ JobTable jobs, int njobs,
                                                         int nsweeps, BarrierDev bar, unsigned nblocks) {
   const int nitems = njobs * g.ntiles;
   CoefF cf;
@@ -329,7 +329,7 @@ __global__ void __launch_bounds__(kThreads) k_mcsor_f32(GridDev g, const JobDev 
     for (int c = 0; c < 5; ++c) {
       for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
         const int jb = item / g.ntiles, t = item - jb * g.ntiles;
-        const JobDev &J = jobs[jb];
+        const JobDev &J = jobs.j[jb];
         float *e = J.e32;
         if (c == 0 && s > 0) {
           tile_boundary<float>(g, e, t, J.isym);
@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(kThreads) k_mcsor_f32(GridDev g, const JobDev 
   }
   for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
     const int jb = item / g.ntiles, t = item - jb * g.ntiles;
-    tile_boundary<float>(g, jobs[jb].e32, t, jobs[jb].isym);
+    tile_boundary<float>(g, jobs.j[jb].e32, t, jobs.j[jb].isym);
     __syncthreads();
   }
 }
@@ -545,12 +545,12 @@ __device__ __forceinline__ void seam_barrier(int nthreads) {
   asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
 }
 
-__global__ void __launch_bounds__(kClusterMaxThreads, 1) k_mixed_cluster(GridDev g, const JobDev *__restrict__ jobs,
+__global__ void __launch_bounds__(kClusterMaxThreads, 1) k_mixed_cluster(GridDev g, const __grid_constant__ JobTable jobs,
                                                                         int nsweeps) {
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
   const int C = int(cl.num_blocks()), rank = int(cl.block_rank());
-  const JobDev &J = jobs[blockIdx.x / C];
+  const JobDev &J = jobs.j[blockIdx.x / C];
   const float *const r32 = J.r32, *const w32 = J.w32;
   const bool even = (J.isym == 1);
   const float *const bt = (J.kind >= 1) ? g.bpot_mu32 : g.borb_mu32;
@@ -722,12 +722,6 @@ __device__ __forceinline__ void ghost_point(const GridDev &g, double *u, int k, 
   }
 }
 
-__global__ void k_ghost_jobs(GridDev g, const JobDev *__restrict__ jobs) {
-  const JobDev &J = jobs[blockIdx.y];
-  const int n = g.nmu * 8 + 4 * g.nni;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) ghost_point(g, J.u, k, J.isym);
-}
-
 // double -> float with round to nearest even, on the integer pipes (GB300
 // issues conversion instructions on its narrow FP64 pipe); values beyond the
 // float range become infinities, values below its normal range signed zero
@@ -746,11 +740,33 @@ __device__ __forceinline__ float narrow_f64(double x) {
   return __uint_as_float(sign | bits);
 }
 
+// u at ext (row, col) with the putin ghost cells (inout.F90:47-80) read as
+// the mirrored interior value, negated for odd functions (a sign-bit flip);
+// the corner ghosts, never filled by putin, are not reachable by the cross
+// stencil
+__device__ __forceinline__ double ghost_read(const GridDev &g, const double *u, int row, int col, int isym) {
+  bool m = false;
+  if (col < 4) {
+    col = 8 - col;
+    m = true;
+  } else if (col > g.nni + 3) {
+    col = 2 * g.nni + 6 - col;
+    m = true;
+  }
+  if (row < 4) {
+    row = 8 - row;
+    m = true;
+  }
+  const double v = u[row * g.n8 + col];
+  return (m && isym != 1) ? __longlong_as_double(__double_as_longlong(v) ^ (1ll << 63)) : v;
+}
+
 // Mixed form residual r = rhs - A u in FP64 over the interior, stored as
 // FP32 with omega / lhs; the stencil uses the grid's separable weights (one
-// FMA per neighbour).
-__global__ void k_residual(GridDev g, const JobDev *__restrict__ jobs, int zero_e) {
-  const JobDev &J = jobs[blockIdx.y];
+// FMA per neighbour) and reads the ghost cells as mirrored interior values,
+// so u needs no ghost refresh first.
+__global__ void k_residual(GridDev g, const __grid_constant__ JobTable jobs, int zero_e) {
+  const JobDev &J = jobs.j[blockIdx.y];
   const int nint = (g.nni - 2) * (g.nmu - 5);
   const int n8 = g.n8;
   if (zero_e)
@@ -770,21 +786,35 @@ __global__ void k_residual(GridDev g, const JobDev *__restrict__ jobs, int zero_
     }
     const double *cm = cmu + mu * 8, *cn = g.cnu + nu * 8;
     double cc = lhs * u[ij];
+    if (mu >= 4 && nu >= 4 && nu <= g.nni - 5) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int dm = (4 - q) * n8, dn = 4 - q;
-      cc = fma(cm[q], u[ij - dm], cc);
-      cc = fma(cm[4 + q], u[ij + dm], cc);
-      cc = fma(cn[q], u[ij - dn], cc);
-      cc = fma(cn[4 + q], u[ij + dn], cc);
+      for (int q = 0; q < 4; ++q) {
+        const int dm = (4 - q) * n8, dn = 4 - q;
+        cc = fma(cm[q], u[ij - dm], cc);
+        cc = fma(cm[4 + q], u[ij + dm], cc);
+        cc = fma(cn[q], u[ij - dn], cc);
+        cc = fma(cn[4 + q], u[ij + dn], cc);
+      }
+    } else {
+      // the stencil reaches the putin ghosts: read them as mirrored interior
+      // values
+      const int row = mu + 4, col = nu + 4;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int d = 4 - q;
+        cc = fma(cm[q], ghost_read(g, u, row - d, col, J.isym), cc);
+        cc = fma(cm[4 + q], u[ij + d * n8], cc);
+        cc = fma(cn[q], ghost_read(g, u, row, col - d, J.isym), cc);
+        cc = fma(cn[4 + q], ghost_read(g, u, row, col + d, J.isym), cc);
+      }
     }
     J.r32[ik] = narrow_f64(rhs - cc);
     J.w32[ik] = J.omegaf / narrow_f64(lhs);
   }
 }
 
-__global__ void k_update(GridDev g, const JobDev *__restrict__ jobs) {
-  const JobDev &J = jobs[blockIdx.y];
+__global__ void k_update(GridDev g, const __grid_constant__ JobTable jobs) {
+  const JobDev &J = jobs.j[blockIdx.y];
   const int nint = (g.nni - 2) * (g.nmu - 5);
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nint; k += gridDim.x * blockDim.x) {
     const int mu = 1 + k / (g.nni - 2), nu = 1 + k % (g.nni - 2);
@@ -794,8 +824,8 @@ __global__ void k_update(GridDev g, const JobDev *__restrict__ jobs) {
 }
 
 // Axis extrapolation of the FP64 function after the update (one block per job).
-__global__ void k_extrap_jobs(GridDev g, const JobDev *__restrict__ jobs) {
-  const JobDev &J = jobs[blockIdx.x];
+__global__ void k_extrap_jobs(GridDev g, const __grid_constant__ JobTable jobs) {
+  const JobDev &J = jobs.j[blockIdx.x];
   double *u = J.u;
   const int n8 = g.n8, nni = g.nni;
   const bool even = (J.isym == 1);
@@ -844,36 +874,42 @@ __global__ void k_putout(GridDev g, const double *ext, double *plain) {
   }
 }
 
-// fockHF (src/fock.F90:57-186), per grid point in the reference's order.
+// fockHF (src/fock.F90:57-186), per grid point: exact keeps the reference's
+// unfused order, otherwise (mixed form) products are fused into FMAs.
+template <bool exact>
+__device__ __forceinline__ double madd(double a, double b, double c) {  // a*b + c
+  if (exact) return A(M(a, b), c);
+  return fma(a, b, c);
+}
+
+template <bool exact>
 __global__ void k_fock(GridDev g, FockArgs a) {
   const double ee = *a.ee;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
     const int mu = k / g.nni, nu = k - mu * g.nni;
     const int ij = (mu + 4) * g.n8 + nu + 4;
     double fock1 = g.f0[k];
-    fock1 = A(M(ee, g.f1[k]), fock1);
-    if (a.m != 0) fock1 = A(M(double(a.m * a.m), g.e[k]), fock1);
+    fock1 = madd<exact>(ee, g.f1[k], fock1);
+    if (a.m != 0) fock1 = madd<exact>(double(a.m * a.m), g.e[k], fock1);
     double fock2 = 0.0;
     if (!a.nel1) {
       double wk1 = 0.0;
       for (int q = 0; q < a.nterms; ++q) {
         const FockTerm &T = a.t[q];
-        wk1 = A(M(T.coo, T.coul[ij]), wk1);
+        wk1 = madd<exact>(T.coo, T.coul[ij], wk1);
         if (T.mode == 0) {
           double wk2 = M(T.gec, T.ex[ij]);
-          if (T.ex2) wk2 = A(M(T.gec2, T.ex2[ij]), wk2);
-          wk2 = M(wk2, T.psi[ij]);
-          fock2 = A(fock2, wk2);
+          if (T.ex2) wk2 = madd<exact>(T.gec2, T.ex2[ij], wk2);
+          fock2 = madd<exact>(wk2, T.psi[ij], fock2);
         } else if (T.mode == 1) {
           const double wk2 = M(T.ex[ij], T.psi[ij]);
-          fock2 = A(M(T.gec, wk2), fock2);
+          fock2 = madd<exact>(T.gec, wk2, fock2);
         }
       }
       a.coulp[k] = wk1;
       a.exchp[k] = fock2;
-      wk1 = M(wk1, g.f2[k]);
       fock2 = M(fock2, g.f2[k]);
-      fock1 = A(fock1, wk1);
+      fock1 = madd<exact>(wk1, g.f2[k], fock1);
     }
     a.lhs[k] = A(fock1, g.diag);
     a.rhs[k] = fock2;
@@ -890,10 +926,11 @@ __global__ void k_asympt_get(GridDev g, const double *fa, double *edecay) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const int jj = k / g.nni, i = k - jj * g.nni;
     const int j = g.nmu - 4 + jj;  // 0-based mu
-    const double raiq1 = sqrt(g.vxisq[j - 1] + g.vetasq[i] - 1.0);
-    const double raiq = sqrt(g.vxisq[j] + g.vetasq[i] - 1.0);
+    (void)j;
+    // raiq1 - raiq from the grid's table; x**0.25 as sqrt(sqrt(x))
+    const double dr = g.asy[size_t(50) * n + k];
     const double fj = fa[(jj + 1) * g.nni + i], fjm = fa[jj * g.nni + i];
-    edecay[k] = pow(fabs(fj / fjm), 0.250) * exp(sqrt(fabs(fjm)) * (raiq1 - raiq));
+    edecay[k] = sqrt(sqrt(fabs(fj / fjm))) * exp(sqrt(fabs(fjm)) * dr);
   }
 }
 
@@ -931,6 +968,26 @@ __global__ void k_scale(GridDev g, double *psi, const double *xnorm) {
     const int mu = k / g.nni, nu = k - mu * g.nni;
     const int ij = (mu + 4) * g.n8 + nu + 4;
     psi[ij] = M(zarea, psi[ij]);
+  }
+}
+
+// norm scaling followed by setCiOrb (normOrtho.F90:50-52, scfUtils.F90:380-
+// 434) in one pass: the left half of each row is scaled and mirrored, the
+// middle column scaled (gerade) or zeroed (ungerade)
+__global__ void k_scale_setci(GridDev g, double *psi, const double *xnorm, int ihomo) {
+  const double zarea = D(1.0, sqrt(*xnorm));
+  const int n2 = g.nni / 2 + 1;
+  const int n = n2 * g.nmu;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int mu = k / n2, ni = k - mu * n2;
+    const int row = (mu + 4) * g.n8 + 4;
+    if (ni < n2 - 1) {
+      const double v = M(zarea, psi[row + ni]);
+      psi[row + ni] = v;
+      psi[row + (g.nni - 1 - ni)] = (ihomo == 1) ? v : -v;
+    } else {
+      psi[row + ni] = (ihomo == 1) ? M(zarea, psi[row + ni]) : 0.0;
+    }
   }
 }
 
@@ -1044,6 +1101,7 @@ __global__ void k_moment_tables(GridDev g, double *exm, double *asy) {
     const int jj = p / g.nni, i = p - jj * g.nni, j = g.nmu - 4 + jj;
     const double rr = sqrt(g.vxisq[j] + g.vetasq[i] - 1.0);
     asy[p] = g.r2 * g.vxi[j];
+    asy[size_t(50) * P + p] = sqrt(g.vxisq[j - 1] + g.vetasq[i] - 1.0) - rr;  // orbAsymptGet's raiq1 - raiq
     const double rr1 = 1.0 / (rr * g.r2);
     asy[P + p] = rr1;
     const double costh = g.veta[i] * g.vxi[j] / rr;
@@ -1096,8 +1154,8 @@ __global__ void k_zero(double *p, size_t n) {
 }
 
 // ----------------------------------------------------------------------
-// Deterministic reductions: fixed grid -> per-block partials -> one block
-// sums the partials in block order.
+// Deterministic reductions: fixed grid -> per-block partials -> the last
+// block to finish sums the partials in block order.
 // ----------------------------------------------------------------------
 constexpr int kRedBlocks = 160;
 constexpr int kMaxK = 16;
@@ -1120,13 +1178,25 @@ __device__ void block_sum_store(double (&v)[K], double *partials) {
   }
 }
 
-// final pass: out[q] = sum over blocks, then an optional epilogue
+// Every block stores its K partial sums; the block that finishes last (an
+// atomic ticket, reset by that block) sums the partials of all blocks in
+// block order -- the same order on every run -- and
+// writes out[0..nout).  Returns true in that block.  No block waits for
+// another.
 template <int K>
-__global__ void k_reduce_final(const double *partials, int nblocks, double *out, int nout) {
+__device__ bool block_sum_finish(double (&v)[K], double *partials, double *out, int nout, unsigned *ticket) {
+  __shared__ bool s_last;
   __shared__ double sh[kThreads / 32];
+  block_sum_store<K>(v, partials);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!s_last) return false;
+  __threadfence();
   for (int q = 0; q < nout; ++q) {
     double s = 0.0;
-    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partials[b * K + q];
+    for (int b = threadIdx.x; b < int(gridDim.x); b += blockDim.x) s += __ldcg(partials + size_t(b) * K + q);
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
     __syncthreads();
@@ -1137,19 +1207,22 @@ __global__ void k_reduce_final(const double *partials, int nblocks, double *out,
     }
     __syncthreads();
   }
+  if (threadIdx.x == 0) *ticket = 0u;
+  return true;
 }
 
-__global__ void k_norm(GridDev g, const double *psi, double *partials) {
+__global__ void k_norm(GridDev g, const double *psi, double *partials, double *out, unsigned *ticket) {
   double v[1] = {0.0};
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
     const int mu = k / g.nni, nu = k - mu * g.nni;
     const double p = psi[(mu + 4) * g.n8 + nu + 4];
     v[0] += g.wgt2[k] * M(M(p, p), g.f4[k]);
   }
-  block_sum_store<1>(v, partials);
+  block_sum_finish<1>(v, partials, out, 1, ticket);
 }
 
-__global__ void k_overlaps(GridDev g, const double *psi, PtrList o, int n, double *partials) {
+__global__ void k_overlaps(GridDev g, const double *psi, PtrList o, int n, double *partials, double *out,
+                           unsigned *ticket) {
   double v[kMaxK];
   for (int q = 0; q < kMaxK; ++q) v[q] = 0.0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
@@ -1158,13 +1231,16 @@ __global__ void k_overlaps(GridDev g, const double *psi, PtrList o, int n, doubl
     const double p = psi[ij], w = g.wgt2[k], f4 = g.f4[k];
     for (int q = 0; q < n; ++q) v[q] += w * M(M(p, o.p[q][ij]), f4);
   }
-  block_sum_store<kMaxK>(v, partials);
+  block_sum_finish<kMaxK>(v, partials, out, n, ticket);
 }
 
 // EaHF = oneelij(i,i) + (J + K): per point terms of integrals.F90:406-480
-// and lagrangeMultipliers.F90:67-72.  psi has its ghosts filled.
-__global__ void k_eahf(GridDev g, const double *psi, int m, const double *coulp, const double *exchp,
-                       double *partials) {
+// and lagrangeMultipliers.F90:67-72.  psi's ghost cells are read as the
+// mirrored interior values (identical to a putin ghost refresh); exact keeps
+// the reference's unfused order, otherwise products are fused (mixed form).
+template <bool exact>
+__global__ void k_eahf(GridDev g, const double *psi, int isym, int m, const double *coulp, const double *exchp,
+                       double *partials, double *sums, double *ee_out, double *parts, unsigned *ticket) {
   double v[5] = {0, 0, 0, 0, 0};
   const int n8 = g.n8;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
@@ -1172,25 +1248,41 @@ __global__ void k_eahf(GridDev g, const double *psi, int m, const double *coulp,
     const int ij = (mu + 4) * n8 + nu + 4;
     // diffnu: sum_k f(nu+k-4) dni(k,nu); diffmu: sum_k f(mu+k-4) dmu(k,mu) (dgemv order)
     double sn = 0.0, sm = 0.0;
+    const double *dn = g.dni9 + 9 * nu, *dm = g.dmu9 + 9 * mu;
+    if (mu >= 4 && nu >= 4 && nu <= g.nni - 5) {
 #pragma unroll
-    for (int q = 0; q < 9; ++q) sn = A(sn, M(psi[ij + q - 4], g.dni9[9 * nu + q]));
+      for (int q = 0; q < 9; ++q) sn = madd<exact>(psi[ij + q - 4], dn[q], sn);
 #pragma unroll
-    for (int q = 0; q < 9; ++q) sm = A(sm, M(psi[ij + (q - 4) * n8], g.dmu9[9 * mu + q]));
+      for (int q = 0; q < 9; ++q) sm = madd<exact>(psi[ij + (q - 4) * n8], dm[q], sm);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 9; ++q) sn = madd<exact>(ghost_read(g, psi, mu + 4, nu + q, isym), dn[q], sn);
+#pragma unroll
+      for (int q = 0; q < 9; ++q) sm = madd<exact>(ghost_read(g, psi, mu + q, nu + 4, isym), dm[q], sm);
+    }
     double kin = A(sn, sm);
     const double p = psi[ij];
-    if (m != 0) kin = A(M(M(double(m * m), g.e[k]), p), kin);
-    const double t = M(A(M(p, g.f0[k]), kin), p);
-    v[0] += g.wgt1[k] * t;                   // oneel
-    v[1] += g.wgt1[k] * M(kin, p);           // kinetic (+ m^2 e term)
-    v[2] += g.wgt1[k] * M(M(p, g.f0[k]), p);  // nuclear
-    v[3] += g.wgt2[k] * M(M(p, coulp[k]), p);
-    v[4] += g.wgt2[k] * M(p, exchp[k]);
+    if (m != 0) kin = madd<exact>(M(double(m * m), g.e[k]), p, kin);
+    const double pf0 = M(p, g.f0[k]);
+    const double w1 = g.wgt1[k], w2 = g.wgt2[k];
+    if (exact) {
+      const double t = M(A(pf0, kin), p);
+      v[0] += w1 * t;                   // oneel
+      v[1] += w1 * M(kin, p);           // kinetic (+ m^2 e term)
+      v[2] += w1 * M(pf0, p);           // nuclear
+      v[3] += w2 * M(M(p, coulp[k]), p);
+      v[4] += w2 * M(p, exchp[k]);
+    } else {
+      const double kp = kin * p, np = pf0 * p;
+      v[1] = fma(w1, kp, v[1]);
+      v[2] = fma(w1, np, v[2]);
+      v[3] = fma(w2, (p * coulp[k]) * p, v[3]);
+      v[4] = fma(w2, p * exchp[k], v[4]);
+    }
   }
-  block_sum_store<5>(v, partials);
-}
-
-__global__ void k_eahf_final(const double *sums, double *ee_out, double *parts) {
-  if (threadIdx.x == 0) {
+  if (!exact) v[0] = v[1] + v[2];  // oneel = kinetic + nuclear, summed per block
+  if (block_sum_finish<5>(v, partials, sums, 5, ticket) && threadIdx.x == 0) {
+    // EaHF and its parts (lagrangeMultipliers.F90:67-72)
     const double woneel = sums[0], wc = sums[3], wx = -sums[4];
     *ee_out = woneel + (wc + wx);
     if (parts) {
@@ -1207,7 +1299,7 @@ struct TripleList {
   TripleItem it[kMaxK];
 };
 
-__global__ void k_triples(GridDev g, TripleList L, int n, double *partials) {
+__global__ void k_triples(GridDev g, TripleList L, int n, double *partials, double *out, unsigned *ticket) {
   double v[kMaxK];
   for (int q = 0; q < kMaxK; ++q) v[q] = 0.0;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
@@ -1220,11 +1312,11 @@ __global__ void k_triples(GridDev g, TripleList L, int n, double *partials) {
       v[q] += w * t;
     }
   }
-  block_sum_store<kMaxK>(v, partials);
+  block_sum_finish<kMaxK>(v, partials, out, n, ticket);
 }
 
 // coulMom (scfUtils.F90:490-603)
-__global__ void k_coulmom(GridDev g, const double *psi, int homo, double *partials) {
+__global__ void k_coulmom(GridDev g, const double *psi, int homo, double *partials, double *out, unsigned *ticket) {
   double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
     const int mu = k / g.nni, nu = k - mu * g.nni;
@@ -1235,11 +1327,12 @@ __global__ void k_coulmom(GridDev g, const double *psi, int homo, double *partia
       v[q] += g.wgt2[k] * M(g.leg[size_t(q) * g.mxsize + k], wk1);
     }
   }
-  block_sum_store<8>(v, partials);
+  block_sum_finish<8>(v, partials, out, g.mpole, ticket);
 }
 
 // exchMom (scfUtils.F90:615-844) with the grid's weighted P_k^q r^k tables
-__global__ void k_exchmom(GridDev g, const double *psa, const double *psb, int idel, double *partials) {
+__global__ void k_exchmom(GridDev g, const double *psa, const double *psb, int idel, double *partials, double *out,
+                          unsigned *ticket) {
   double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   if (idel <= 4) {
     const double *T = g.exm + size_t(idel) * 8 * g.mxsize;
@@ -1252,7 +1345,7 @@ __global__ void k_exchmom(GridDev g, const double *psa, const double *psb, int i
         if (q < g.mpole) v[q] = fma(T[size_t(q) * g.mxsize + k], wk1, v[q]);
     }
   }
-  block_sum_store<8>(v, partials);
+  block_sum_finish<8>(v, partials, out, g.mpole, ticket);
 }
 
 // Checks narrow_f64 / widen_f32 against the hardware conversions on n
@@ -1315,104 +1408,93 @@ static double *reduction_partials(x2g_ctx *ctx, int K) {
   return static_cast<double *>(ctx->red);
 }
 
-int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, int nsweeps, int precision) {
-  if (njobs <= 0) return X2G_OK;
-  if (nsweeps <= 0) return set_status(X2G_ERR_ARG, "nsweeps must be positive");
-  const GridDev &g = grid->d;
-  const bool mixed = (precision == X2G_MIXED);
-  // device job table + per-job scratch
-  const size_t ext_bytes = size_t(g.next) * sizeof(double);
-  const size_t plain_bytes = size_t(g.mxsize) * sizeof(double);
-  const size_t per_job = mixed ? (size_t(g.next) * sizeof(float) + 2 * size_t(g.mxsize) * sizeof(float) + 256)
-                               : (plain_bytes + 256);
-  const size_t jobs_bytes = (sizeof(JobDev) * njobs + 255) / 256 * 256;
-  char *ws = static_cast<char *>(ctx_workspace(ctx, jobs_bytes + per_job * njobs + 256));
-  if (!ws) return set_status(X2G_ERR_ALLOC, "workspace allocation failed");
-  (void)ext_bytes;
-  std::vector<JobDev> h(njobs);
-  char *scratch = ws + jobs_bytes;
-  for (int i = 0; i < njobs; ++i) {
-    const x2g_job &x = jobs[i];
-    const bool explicit_lr = (x.lhs && x.rhs);
-    if (!x.u || (x.kind != 0 && x.kind != 1) || (x.kind == 0 && !explicit_lr) ||
-        (x.kind == 1 && !explicit_lr && (!x.psa || !x.psb)) || (x.isym != 1 && x.isym != -1))
-      return set_status(X2G_ERR_ARG, "bad relaxation job");
-    JobDev &d = h[i];
-    d.u = x.u;
-    d.lhs = x.lhs;
-    d.rhs = x.rhs;
-    d.psa = x.psa;
-    d.psb = x.psb;
-    d.omega = x.omega;
-    d.omegaf = float(x.omega);
-    d.omega1f = float(1.0 - x.omega);
-    d.idel2 = double(x.idel * x.idel);
-    d.isym = x.isym;
-    // kind 0 orbital (borb); 1 potential built from psa/psb; 2 potential
-    // given explicit lhs/rhs arrays (bpot)
-    d.kind = (x.kind == 1 && explicit_lr) ? 2 : x.kind;
-    char *p = scratch + per_job * i;
-    if (mixed) {
-      d.e32 = reinterpret_cast<float *>(p);
-      d.r32 = reinterpret_cast<float *>(p + (size_t(g.next) * sizeof(float) + 127) / 128 * 128);
-      d.w32 = d.r32 + g.mxsize;
-      d.rhs_buf = nullptr;
-    } else {
-      d.rhs_buf = reinterpret_cast<double *>(p);
-      d.e32 = nullptr;
-      d.r32 = d.w32 = nullptr;
-    }
+// Job-table entry of one x2g_job (kind 0 orbital with borb; 1 potential
+// built from psa/psb; 2 potential given explicit lhs/rhs arrays, bpot).
+static bool make_job(const x2g_job &x, JobDev &d) {
+  const bool explicit_lr = (x.lhs && x.rhs);
+  if (!x.u || (x.kind != 0 && x.kind != 1) || (x.kind == 0 && !explicit_lr) ||
+      (x.kind == 1 && !explicit_lr && (!x.psa || !x.psb)) || (x.isym != 1 && x.isym != -1))
+    return false;
+  d = JobDev{};
+  d.u = x.u;
+  d.lhs = x.lhs;
+  d.rhs = x.rhs;
+  d.psa = x.psa;
+  d.psb = x.psb;
+  d.omega = x.omega;
+  d.omegaf = float(x.omega);
+  d.omega1f = float(1.0 - x.omega);
+  d.idel2 = double(x.idel * x.idel);
+  d.isym = x.isym;
+  d.kind = (x.kind == 1 && explicit_lr) ? 2 : x.kind;
+  return true;
+}
+
+static int take_event(x2g_ctx *ctx, cudaEvent_t *ev) {
+  if (!ctx->event_pool.empty()) {
+    *ev = ctx->event_pool.back();
+    ctx->event_pool.pop_back();
+    return X2G_OK;
   }
-  JobDev *djobs = reinterpret_cast<JobDev *>(ws);
-  cudaError_t err = cudaMemcpyAsync(djobs, h.data(), sizeof(JobDev) * njobs, cudaMemcpyHostToDevice, ctx->stream);
-  if (err != cudaSuccess) return cuda_status(err, "job table upload");
-  BarrierDev bar{ctx->bar, ctx->bar + 1, reinterpret_cast<int *>(ctx->bar + 2)};
-  err = cudaMemsetAsync(ctx->bar, 0, 4 * sizeof(unsigned), ctx->stream);
-  if (err != cudaSuccess) return cuda_status(err, "barrier reset");
-  const int nitems = njobs * g.ntiles;
-  bool on_chip = mixed && g.cl_size >= 2 && !ctx->no_cluster;
-  if (on_chip) {
-    // the cluster must be schedulable on this device (shared memory per CTA,
-    // non-portable sizes above 8): ask the occupancy calculator once
-    const size_t smem = cluster_smem_bytes(g);
-    const long key = (long(smem) * 64 + g.cl_size) * 32 + (g.cl_wa + g.cl_wb + g.cl_ws);
-    if (ctx->cluster_checked_key != key) {
-      ctx->cluster_checked_key = key;
-      ctx->cluster_ok = 0;
-      bool attr_ok = cudaFuncSetAttribute((const void *)k_mixed_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          int(smem)) == cudaSuccess;
-      if (attr_ok && g.cl_size > 8)
-        attr_ok = cudaFuncSetAttribute((const void *)k_mixed_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed,
-                                       1) == cudaSuccess;
-      if (attr_ok) {
-        ctx->cluster_smem_set = smem;
-        ctx->cluster_nonportable = (g.cl_size > 8);
-        cudaLaunchConfig_t q = {};
-        q.gridDim = dim3(unsigned(g.cl_size));
-        q.blockDim = dim3(unsigned(32 * (g.cl_wa + g.cl_wb + g.cl_ws)));
-        q.dynamicSmemBytes = smem;
-        cudaLaunchAttribute qa[1];
-        qa[0].id = cudaLaunchAttributeClusterDimension;
-        qa[0].val.clusterDim.x = unsigned(g.cl_size);
-        qa[0].val.clusterDim.y = 1;
-        qa[0].val.clusterDim.z = 1;
-        q.attrs = qa;
-        q.numAttrs = 1;
-        int nclusters = 0;
-        if (cudaOccupancyMaxActiveClusters(&nclusters, (const void *)k_mixed_cluster, &q) == cudaSuccess &&
-            nclusters > 0)
-          ctx->cluster_ok = 1;
-      }
-      (void)cudaGetLastError();
+  cudaError_t err = cudaEventCreate(ev);
+  return (err == cudaSuccess) ? X2G_OK : cuda_status(err, "profiling event");
+}
+
+// whether the on-chip cluster sweep can run this grid here (asked once per
+// shape: shared memory per CTA, cluster size, block size)
+static bool cluster_usable(x2g_ctx *ctx, const GridDev &g) {
+  if (g.cl_size < 2 || ctx->no_cluster) return false;
+  const size_t smem = cluster_smem_bytes(g);
+  const long key = (long(smem) * 64 + g.cl_size) * 32 + (g.cl_wa + g.cl_wb + g.cl_ws);
+  if (ctx->cluster_checked_key != key) {
+    ctx->cluster_checked_key = key;
+    ctx->cluster_ok = 0;
+    bool attr_ok = cudaFuncSetAttribute((const void *)k_mixed_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        int(smem)) == cudaSuccess;
+    if (attr_ok && g.cl_size > 8)
+      attr_ok = cudaFuncSetAttribute((const void *)k_mixed_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                                     1) == cudaSuccess;
+    if (attr_ok) {
+      ctx->cluster_smem_set = smem;
+      ctx->cluster_nonportable = (g.cl_size > 8);
+      cudaLaunchConfig_t q = {};
+      q.gridDim = dim3(unsigned(g.cl_size));
+      q.blockDim = dim3(unsigned(32 * (g.cl_wa + g.cl_wb + g.cl_ws)));
+      q.dynamicSmemBytes = smem;
+      cudaLaunchAttribute qa[1];
+      qa[0].id = cudaLaunchAttributeClusterDimension;
+      qa[0].val.clusterDim.x = unsigned(g.cl_size);
+      qa[0].val.clusterDim.y = 1;
+      qa[0].val.clusterDim.z = 1;
+      q.attrs = qa;
+      q.numAttrs = 1;
+      int nclusters = 0;
+      if (cudaOccupancyMaxActiveClusters(&nclusters, (const void *)k_mixed_cluster, &q) == cudaSuccess &&
+          nclusters > 0)
+        ctx->cluster_ok = 1;
     }
-    on_chip = ctx->cluster_ok != 0;
+    (void)cudaGetLastError();
   }
+  return ctx->cluster_ok != 0;
+}
+
+// One launch batch (at most kParamJobs jobs) of launch_relax.
+static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, int nsweeps, bool mixed,
+                       bool on_chip) {
+  cudaError_t err;
+  x2g_ctx::Pending pe{};
+  const double points = double(njobs) * double(g.nni - 2) * double(g.nmu - 5) * double(nsweeps);
   if (mixed) {
-    dim3 gg(grid_blocks(g.nmu * 8 + 4 * g.nni), njobs);
-    k_ghost_jobs<<<gg, kThreads, 0, ctx->stream>>>(g, djobs);
     dim3 gr(grid_blocks((g.nni - 2) * (g.nmu - 5)), njobs);
-    k_residual<<<gr, kThreads, 0, ctx->stream>>>(g, djobs, on_chip ? 0 : 1);
-    ctx->launches += 2;
+    k_residual<<<gr, kThreads, 0, ctx->stream>>>(g, jt, on_chip ? 0 : 1);
+    ctx->launches += 1;
+  }
+  if (ctx->profiling) {
+    int rc;
+    if ((rc = take_event(ctx, &pe.a)) || (rc = take_event(ctx, &pe.b))) return rc;
+    pe.precision = mixed ? 1 : 0;
+    pe.points = points;
+    cudaEventRecord(pe.a, ctx->stream);
   }
   if (on_chip) {
     const size_t smem = cluster_smem_bytes(g);
@@ -1439,78 +1521,89 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    x2g_ctx::Pending pe{};
-    if (ctx->profiling) {
-      for (cudaEvent_t *ev : {&pe.a, &pe.b}) {
-        if (!ctx->event_pool.empty()) {
-          *ev = ctx->event_pool.back();
-          ctx->event_pool.pop_back();
-        } else if ((err = cudaEventCreate(ev)) != cudaSuccess) {
-          return cuda_status(err, "profiling event");
-        }
-      }
-      pe.precision = 1;
-      pe.points = double(njobs) * double(g.nni - 2) * double(g.nmu - 5) * double(nsweeps);
-      cudaEventRecord(pe.a, ctx->stream);
-    }
     GridDev gd = g;
-    err = cudaLaunchKernelEx(&cfg, k_mixed_cluster, gd, (const JobDev *)djobs, nsweeps);
+    err = cudaLaunchKernelEx(&cfg, k_mixed_cluster, gd, jt, nsweeps);
     if (err != cudaSuccess) return cuda_status(err, "cluster MCSOR launch");
+    ctx->launches += 1;
     if (ctx->profiling) {
       cudaEventRecord(pe.b, ctx->stream);
       ctx->pending.push_back(pe);
     }
+  } else {
+    // persistent cooperative kernel with grid barriers
+    err = cudaMemsetAsync(ctx->bar, 0, 4 * sizeof(unsigned), ctx->stream);
+    if (err != cudaSuccess) return cuda_status(err, "barrier reset");
+    BarrierDev bar{ctx->bar, ctx->bar + 1, reinterpret_cast<int *>(ctx->bar + 2)};
+    static int max_f64 = -1, max_f32 = -1;
+    int *pmax = mixed ? &max_f32 : &max_f64;
+    if (*pmax < 0) {
+      int per_sm = 0;
+      err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_sm, mixed ? (const void *)k_mcsor_f32 : (const void *)k_mcsor_f64, kThreads, 0);
+      if (err != cudaSuccess) return cuda_status(err, "occupancy query");
+      *pmax = per_sm * ctx->num_sms;
+    }
+    const int nitems = njobs * g.ntiles;
+    unsigned nblocks = unsigned(nitems < *pmax ? nitems : *pmax);
+    if (nblocks < 1) nblocks = 1;
+    int nj = njobs, ns = nsweeps;
+    GridDev gd = g;
+    void *args[] = {&gd, &jt, &nj, &ns, &bar, &nblocks};
+    err = cudaLaunchCooperativeKernel(mixed ? (const void *)k_mcsor_f32 : (const void *)k_mcsor_f64, dim3(nblocks),
+                                      dim3(kThreads), args, 0, ctx->stream);
+    if (err != cudaSuccess) return cuda_status(err, "cooperative MCSOR launch");
     ctx->launches += 1;
-    return X2G_OK;
+    if (ctx->profiling) {
+      cudaEventRecord(pe.b, ctx->stream);
+      ctx->pending.push_back(pe);
+    }
+    if (mixed) {
+      dim3 gu(grid_blocks((g.nni - 2) * (g.nmu - 5)), njobs);
+      k_update<<<gu, kThreads, 0, ctx->stream>>>(g, jt);
+      k_extrap_jobs<<<njobs, kThreads, 0, ctx->stream>>>(g, jt);
+      ctx->launches += 2;
+    }
   }
-  static int max_f64 = -1, max_f32 = -1;
-  int *pmax = mixed ? &max_f32 : &max_f64;
-  if (*pmax < 0) {
-    int per_sm = 0;
-    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, mixed ? (const void *)k_mcsor_f32 : (const void *)k_mcsor_f64, kThreads, 0);
-    if (err != cudaSuccess) return cuda_status(err, "occupancy query");
-    *pmax = per_sm * ctx->num_sms;
-  }
-  unsigned nblocks = unsigned(nitems < *pmax ? nitems : *pmax);
-  if (nblocks < 1) nblocks = 1;
-  int nj = njobs, ns = nsweeps;
-  GridDev gd = g;
-  void *args[] = {&gd, &djobs, &nj, &ns, &bar, &nblocks};
-  x2g_ctx::Pending pe{};
-  if (ctx->profiling) {
-    for (cudaEvent_t *ev : {&pe.a, &pe.b}) {
-      if (!ctx->event_pool.empty()) {
-        *ev = ctx->event_pool.back();
-        ctx->event_pool.pop_back();
-      } else if ((err = cudaEventCreate(ev)) != cudaSuccess) {
-        return cuda_status(err, "profiling event");
+  return X2G_OK;
+}
+
+int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, int nsweeps, int precision) {
+  if (njobs <= 0) return X2G_OK;
+  if (nsweeps <= 0) return set_status(X2G_ERR_ARG, "nsweeps must be positive");
+  const GridDev &g = grid->d;
+  const bool mixed = (precision == X2G_MIXED);
+  const bool on_chip = mixed && cluster_usable(ctx, g);
+  // per-job scratch: FP64 rhs of potentials, or the mixed form's FP32
+  // correction, residual and omega/lhs
+  const size_t per_job = mixed ? (size_t(g.next) * sizeof(float) + 2 * size_t(g.mxsize) * sizeof(float) + 256)
+                               : (size_t(g.mxsize) * sizeof(double) + 256);
+  char *scratch = static_cast<char *>(ctx_workspace(ctx, per_job * njobs + 256));
+  if (!scratch) return set_status(X2G_ERR_ALLOC, "workspace allocation failed");
+  for (int b0 = 0; b0 < njobs; b0 += kParamJobs) {
+    const int nb = (njobs - b0 < kParamJobs) ? njobs - b0 : kParamJobs;
+    JobTable jt{};
+    for (int i = 0; i < nb; ++i) {
+      JobDev &d = jt.j[i];
+      if (!make_job(jobs[b0 + i], d)) return set_status(X2G_ERR_ARG, "bad relaxation job");
+      char *p = scratch + per_job * size_t(b0 + i);
+      if (mixed) {
+        d.e32 = reinterpret_cast<float *>(p);
+        d.r32 = reinterpret_cast<float *>(p + (size_t(g.next) * sizeof(float) + 127) / 128 * 128);
+        d.w32 = d.r32 + g.mxsize;
+      } else {
+        d.rhs_buf = reinterpret_cast<double *>(p);
       }
     }
-    pe.precision = mixed ? 1 : 0;
-    pe.points = double(njobs) * double(g.nni - 2) * double(g.nmu - 5) * double(nsweeps);
-    cudaEventRecord(pe.a, ctx->stream);
-  }
-  err = cudaLaunchCooperativeKernel(mixed ? (const void *)k_mcsor_f32 : (const void *)k_mcsor_f64, dim3(nblocks),
-                                    dim3(kThreads), args, 0, ctx->stream);
-  if (err != cudaSuccess) return cuda_status(err, "cooperative MCSOR launch");
-  if (ctx->profiling) {
-    cudaEventRecord(pe.b, ctx->stream);
-    ctx->pending.push_back(pe);
-  }
-  ctx->launches += 1;
-  if (mixed) {
-    dim3 gu(grid_blocks((g.nni - 2) * (g.nmu - 5)), njobs);
-    k_update<<<gu, kThreads, 0, ctx->stream>>>(g, djobs);
-    k_extrap_jobs<<<njobs, kThreads, 0, ctx->stream>>>(g, djobs);
-    ctx->launches += 2;
+    int rc = relax_batch(ctx, g, jt, nb, nsweeps, mixed, on_chip);
+    if (rc) return rc;
   }
   // barrier error word: checked by the caller at its next synchronisation
   return X2G_OK;
 }
 
-// Scratch layout of launch_relax_in_scratch: 4 barrier words, the job
-// table, then one plain right-hand-side buffer per job (256-byte aligned).
+// Scratch layout of launch_relax_in_scratch: 4 barrier words, a reserved
+// region the size of a job table, then one plain right-hand-side buffer per
+// job (256-byte aligned).
 size_t relax_scratch_bytes(const GridDev &g, int njobs) {
   const size_t head = 256;
   const size_t table = (sizeof(JobDev) * size_t(njobs) + 255) / 256 * 256;
@@ -1526,48 +1619,31 @@ int launch_relax_in_scratch(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, i
   if (need > scratch_bytes) return set_status(X2G_ERR_ARG, "batch does not fit the scratch");
   char *base = static_cast<char *>(scratch);
   unsigned *barw = reinterpret_cast<unsigned *>(base);
-  JobDev *djobs = reinterpret_cast<JobDev *>(base + 256);
   char *rhs0 = base + 256 + (sizeof(JobDev) * size_t(njobs) + 255) / 256 * 256;
   const size_t plain = (size_t(g.mxsize) * sizeof(double) + 255) / 256 * 256;
-  std::vector<JobDev> h(njobs);
-  for (int i = 0; i < njobs; ++i) {
-    const x2g_job &x = jobs[i];
-    const bool explicit_lr = (x.lhs && x.rhs);
-    if (!x.u || (x.kind != 0 && x.kind != 1) || (x.kind == 0 && !explicit_lr) ||
-        (x.kind == 1 && !explicit_lr && (!x.psa || !x.psb)) || (x.isym != 1 && x.isym != -1))
-      return set_status(X2G_ERR_ARG, "bad relaxation job");
-    JobDev &d = h[i];
-    d = JobDev{};
-    d.u = x.u;
-    d.lhs = x.lhs;
-    d.rhs = x.rhs;
-    d.psa = x.psa;
-    d.psb = x.psb;
-    d.omega = x.omega;
-    d.omegaf = float(x.omega);
-    d.omega1f = float(1.0 - x.omega);
-    d.idel2 = double(x.idel * x.idel);
-    d.isym = x.isym;
-    d.kind = (x.kind == 1 && explicit_lr) ? 2 : x.kind;
-    d.rhs_buf = reinterpret_cast<double *>(rhs0 + plain * size_t(i));
-  }
-  cudaError_t err = cudaMemsetAsync(barw, 0, 4 * sizeof(unsigned), ctx->stream);
-  if (err != cudaSuccess) return cuda_status(err, "scratch barrier reset");
-  err = cudaMemcpyAsync(djobs, h.data(), sizeof(JobDev) * njobs, cudaMemcpyHostToDevice, ctx->stream);
-  if (err != cudaSuccess) return cuda_status(err, "scratch job table upload");
-  BarrierDev bar{barw, barw + 1, reinterpret_cast<int *>(barw + 2)};
   int per_sm = 0;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k_mcsor_f64, kThreads, 0);
+  cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k_mcsor_f64, kThreads, 0);
   if (err != cudaSuccess) return cuda_status(err, "occupancy query");
-  const int nitems = njobs * g.ntiles, cap = per_sm * ctx->num_sms;
-  unsigned nblocks = unsigned(nitems < cap ? nitems : cap);
-  if (nblocks < 1) nblocks = 1;
-  int nj = njobs, ns = nsweeps;
-  GridDev gd = g;
-  void *args[] = {&gd, &djobs, &nj, &ns, &bar, &nblocks};
-  err = cudaLaunchCooperativeKernel((const void *)k_mcsor_f64, dim3(nblocks), dim3(kThreads), args, 0, ctx->stream);
-  if (err != cudaSuccess) return cuda_status(err, "cooperative MCSOR launch");
-  ctx->launches += 1;
+  for (int b0 = 0; b0 < njobs; b0 += kParamJobs) {
+    const int nb = (njobs - b0 < kParamJobs) ? njobs - b0 : kParamJobs;
+    JobTable jt{};
+    for (int i = 0; i < nb; ++i) {
+      if (!make_job(jobs[b0 + i], jt.j[i])) return set_status(X2G_ERR_ARG, "bad relaxation job");
+      jt.j[i].rhs_buf = reinterpret_cast<double *>(rhs0 + plain * size_t(b0 + i));
+    }
+    err = cudaMemsetAsync(barw, 0, 4 * sizeof(unsigned), ctx->stream);
+    if (err != cudaSuccess) return cuda_status(err, "scratch barrier reset");
+    BarrierDev bar{barw, barw + 1, reinterpret_cast<int *>(barw + 2)};
+    const int nitems = nb * g.ntiles, cap = per_sm * ctx->num_sms;
+    unsigned nblocks = unsigned(nitems < cap ? nitems : cap);
+    if (nblocks < 1) nblocks = 1;
+    int nj = nb, ns = nsweeps;
+    GridDev gd = g;
+    void *args[] = {&gd, &jt, &nj, &ns, &bar, &nblocks};
+    err = cudaLaunchCooperativeKernel((const void *)k_mcsor_f64, dim3(nblocks), dim3(kThreads), args, 0, ctx->stream);
+    if (err != cudaSuccess) return cuda_status(err, "cooperative MCSOR launch");
+    ctx->launches += 1;
+  }
   return X2G_OK;
 }
 
@@ -1588,7 +1664,10 @@ void launch_putout(x2g_ctx *ctx, const GridDev &g, const double *ext, double *pl
 }
 
 void launch_fock(x2g_ctx *ctx, const GridDev &g, const FockArgs &a) {
-  k_fock<<<grid_blocks(g.mxsize), kThreads, 0, ctx->stream>>>(g, a);
+  if (a.exact)
+    k_fock<true><<<grid_blocks(g.mxsize), kThreads, 0, ctx->stream>>>(g, a);
+  else
+    k_fock<false><<<grid_blocks(g.mxsize), kThreads, 0, ctx->stream>>>(g, a);
   ctx->launches++;
 }
 
@@ -1609,6 +1688,11 @@ void launch_setci(x2g_ctx *ctx, const GridDev &g, double *psi, int ihomo) {
 
 void launch_scale(x2g_ctx *ctx, const GridDev &g, double *psi, const double *norm_dev) {
   k_scale<<<grid_blocks(g.mxsize), kThreads, 0, ctx->stream>>>(g, psi, norm_dev);
+  ctx->launches++;
+}
+
+void launch_scale_setci(x2g_ctx *ctx, const GridDev &g, double *psi, const double *norm_dev, int ihomo) {
+  k_scale_setci<<<grid_blocks((g.nni / 2 + 1) * g.nmu), kThreads, 0, ctx->stream>>>(g, psi, norm_dev, ihomo);
   ctx->launches++;
 }
 
@@ -1656,9 +1740,8 @@ void launch_zero(x2g_ctx *ctx, double *p, size_t n) {
 
 void launch_norm(x2g_ctx *ctx, const GridDev &g, const double *psi, double *out) {
   double *part = reduction_partials(ctx, 1);
-  k_norm<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psi, part);
-  k_reduce_final<1><<<1, kThreads, 0, ctx->stream>>>(part, kRedBlocks, out, 1);
-  ctx->launches += 2;
+  k_norm<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psi, part, out, ctx->bar + 3);
+  ctx->launches += 1;
 }
 
 void launch_overlaps(x2g_ctx *ctx, const GridDev &g, const double *psi, const double *const *others, int n,
@@ -1668,20 +1751,22 @@ void launch_overlaps(x2g_ctx *ctx, const GridDev &g, const double *psi, const do
     const int m = (n - b < kMaxK) ? n - b : kMaxK;
     PtrList L{};
     for (int q = 0; q < m; ++q) L.p[q] = others[b + q];
-    k_overlaps<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psi, L, m, part);
-    k_reduce_final<kMaxK><<<1, kThreads, 0, ctx->stream>>>(part, kRedBlocks, out + b, m);
-    ctx->launches += 2;
+    k_overlaps<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psi, L, m, part, out + b, ctx->bar + 3);
+    ctx->launches += 1;
   }
 }
 
-void launch_eahf(x2g_ctx *ctx, const GridDev &g, const double *psi, int m, const double *coulp,
-                 const double *exchp, double *ee_out, double *parts) {
+void launch_eahf(x2g_ctx *ctx, const GridDev &g, const double *psi, int isym, int m, const double *coulp,
+                 const double *exchp, double *ee_out, double *parts, bool exact) {
   double *part = reduction_partials(ctx, 5);
   double *sums = part + size_t(kRedBlocks) * 5;
-  k_eahf<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psi, m, coulp, exchp, part);
-  k_reduce_final<5><<<1, kThreads, 0, ctx->stream>>>(part, kRedBlocks, sums, 5);
-  k_eahf_final<<<1, 32, 0, ctx->stream>>>(sums, ee_out, parts);
-  ctx->launches += 3;
+  if (exact)
+    k_eahf<true><<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psi, isym, m, coulp, exchp, part, sums, ee_out, parts,
+                                                           ctx->bar + 3);
+  else
+    k_eahf<false><<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psi, isym, m, coulp, exchp, part, sums, ee_out,
+                                                            parts, ctx->bar + 3);
+  ctx->launches += 1;
 }
 
 void launch_triples(x2g_ctx *ctx, const GridDev &g, const TripleItem *items, int n, double *out) {
@@ -1690,24 +1775,21 @@ void launch_triples(x2g_ctx *ctx, const GridDev &g, const TripleItem *items, int
     const int m = (n - b < kMaxK) ? n - b : kMaxK;
     TripleList L{};
     for (int q = 0; q < m; ++q) L.it[q] = items[b + q];
-    k_triples<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, L, m, part);
-    k_reduce_final<kMaxK><<<1, kThreads, 0, ctx->stream>>>(part, kRedBlocks, out + b, m);
-    ctx->launches += 2;
+    k_triples<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, L, m, part, out + b, ctx->bar + 3);
+    ctx->launches += 1;
   }
 }
 
 void launch_coulmom(x2g_ctx *ctx, const GridDev &g, const double *psi, int homo, double *out) {
   double *part = reduction_partials(ctx, 8);
-  k_coulmom<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psi, homo, part);
-  k_reduce_final<8><<<1, kThreads, 0, ctx->stream>>>(part, kRedBlocks, out, g.mpole);
-  ctx->launches += 2;
+  k_coulmom<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psi, homo, part, out, ctx->bar + 3);
+  ctx->launches += 1;
 }
 
 void launch_exchmom(x2g_ctx *ctx, const GridDev &g, const double *psa, const double *psb, int idel, double *out) {
   double *part = reduction_partials(ctx, 8);
-  k_exchmom<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psa, psb, idel, part);
-  k_reduce_final<8><<<1, kThreads, 0, ctx->stream>>>(part, kRedBlocks, out, g.mpole);
-  ctx->launches += 2;
+  k_exchmom<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psa, psb, idel, part, out, ctx->bar + 3);
+  ctx->launches += 1;
 }
 
 }  // namespace x2g

@@ -23,7 +23,7 @@ struct FockArgs {
   int nterms;
   int m;        // |lambda| of iorb
   int nel1;     // one-electron case: fockHF returns before the two-electron part
-  int pad;
+  int exact;    // 1: the reference's unfused FP64 order; 0 (mixed form): FMAs
   const double *ee;  // device: diagonal Lagrange multiplier of iorb
   double *lhs, *rhs; // plain outputs: fock1 + diag, fock2
   double *coulp, *exchp;  // plain: coulombptr, exchangeptr of iorb
@@ -67,12 +67,14 @@ void launch_asympt_get(x2g_ctx *ctx, const GridDev &g, const double *fa, double 
 void launch_asympt_set(x2g_ctx *ctx, const GridDev &g, double *psi, const double *edecay);
 void launch_setci(x2g_ctx *ctx, const GridDev &g, double *psi, int ihomo);
 void launch_scale(x2g_ctx *ctx, const GridDev &g, double *psi, const double *norm_dev);
+// psi /= sqrt(norm) then setCiOrb's symmetrisation, in one pass
+void launch_scale_setci(x2g_ctx *ctx, const GridDev &g, double *psi, const double *norm_dev, int ihomo);
 void launch_ortho_apply(x2g_ctx *ctx, const GridDev &g, double *psi, const double *const *others, int n,
                         const double *ovl_dev);
 void launch_asympt(x2g_ctx *ctx, const GridDev &g, const AsymptArgs &a);
 // narrow_f64 / widen_f32 against the hardware conversions on n values
 int convert_selftest(x2g_ctx *ctx, long n, unsigned long long seed, unsigned long long *mismatches);
-// fills g's exm (40 x mxsize) and asy (50 x 4 nni) tables; synchronous
+// fills g's exm (40 x mxsize) and asy (51 x 4 nni) tables; synchronous
 int build_moment_tables(x2g_ctx *ctx, const GridDev &g, double *exm, double *asy);
 void launch_zero(x2g_ctx *ctx, double *p, size_t n);
 
@@ -84,8 +86,10 @@ void launch_overlaps(x2g_ctx *ctx, const GridDev &g, const double *psi, const do
                      double *out);
 // EaHF: out = woneel + (wcoul + wexch); psi must have ghosts filled.
 // Also writes parts[0..4] = kinetic, nuclear, oneel, coul, exch.
-void launch_eahf(x2g_ctx *ctx, const GridDev &g, const double *psi, int m, const double *coulp,
-                 const double *exchp, double *ee_out, double *parts);
+// psi's ghost cells are read as mirrored interior values (no ghost refresh
+// needed); exact: the reference's unfused FP64 order, else FMAs (mixed form)
+void launch_eahf(x2g_ctx *ctx, const GridDev &g, const double *psi, int isym, int m, const double *coulp,
+                 const double *exchp, double *ee_out, double *parts, bool exact = true);
 // generic weighted triple products: out[k] = sum w * a_k * b_k * c_k (c may be null), w = wgt2
 struct TripleItem {
   const double *a, *b, *c;  // a,b ext arrays; c ext or null

@@ -281,6 +281,7 @@ int fock(x2g_scf *s, int iorb) {
   FockArgs a{};
   a.m = s->m[iorb];
   a.nel1 = (s->nel == 1);
+  a.exact = (s->cs.precision == X2G_FP64);
   a.ee = s->sc + x2g_scf::O_EE + iorb;
   a.lhs = s->lhs;
   a.rhs = s->rhs;
@@ -381,9 +382,8 @@ void ortho(x2g_scf *s, int iorb) {
 }
 
 void eahf(x2g_scf *s, int iorb, double *ee_out, double *parts) {
-  const GridDev &g = s->grid->d;
-  launch_ghost_fill(s->ctx, g, s->orb[iorb], s->isymOrb[iorb]);
-  launch_eahf(s->ctx, g, s->orb[iorb], s->m[iorb], s->coulp[iorb], s->exchp[iorb], ee_out, parts);
+  launch_eahf(s->ctx, s->grid->d, s->orb[iorb], s->isymOrb[iorb], s->m[iorb], s->coulp[iorb], s->exchp[iorb], ee_out,
+              parts, s->cs.precision == X2G_FP64);
 }
 
 void mpole_moments(x2g_scf *s) {
@@ -570,8 +570,15 @@ int scf_iteration(x2g_scf *s, int *rc) {
     if ((*rc = relax_potentials(s, iorb))) return 1;
     if (!s->lfixorb)
       if ((*rc = relax_orbital(s, iorb))) return 1;
-    if (s->ifixorb[iorb] == 0) norm(s, iorb);
-    if (s->cs.homonuclear) launch_setci(s->ctx, s->grid->d, s->orb[iorb], s->ihomo[iorb]);
+    if (s->ifixorb[iorb] == 0 && s->cs.homonuclear) {
+      // norm scaling and setCiOrb in one pass
+      double *out = s->sc + x2g_scf::O_NORM + iorb;
+      launch_norm(s->ctx, s->grid->d, s->orb[iorb], out);
+      launch_scale_setci(s->ctx, s->grid->d, s->orb[iorb], out, s->ihomo[iorb]);
+    } else {
+      if (s->ifixorb[iorb] == 0) norm(s, iorb);
+      if (s->cs.homonuclear) launch_setci(s->ctx, s->grid->d, s->orb[iorb], s->ihomo[iorb]);
+    }
     if (norb > 1 && s->ifixorb[iorb] == 0) ortho(s, iorb);
     if (s->ifixorb[iorb] != 0) fock(s, iorb);
     eahf(s, iorb, s->sc + x2g_scf::O_EE + iorb, nullptr);
