@@ -7,9 +7,12 @@
 # The sources are staged from the x2dhf tree into oracle/_ref/src (git-ignored)
 # so that the same build can run where the tree is not mounted.  The
 # reference passes an int* as void** to pthread_join (mcsor_pthread.c,
-# coulExch_pthread.c); it is built without the stack protector, as the
-# distribution compilers of its authors do by default, so that this write
-# does not abort the multi-threaded runs.
+# coulExch_pthread.c): the sources are compiled with pthread_join renamed to
+# the shim's x2r_pthread_join, which discards the exit value instead of
+# storing a pointer into 4 bytes of their stack.  The potential driver
+# (coulExch_pthread_ / relax_single_pot_pthread_, which writes past a stack
+# array at relax_single_pot_pthread.c:47) is linked but not called: the
+# shim's x2r_coulexch drives sorpt_ one thread per potential.
 set -e
 HERE="$(cd "$(dirname "$0")" && pwd)"
 REF="${X2DHF_REF:-/root/reference}"
@@ -23,7 +26,8 @@ for f in $FILES; do
   if [ ! -f "$OUT/src/$f" ]; then echo "build_ref: reference source $f not available" >&2; exit 0; fi
 done
 CC="${CC:-gcc}"
-$CC -O2 -fPIC -shared -ffp-contract=off -fno-stack-protector -pthread -w -I "$OUT/src" -o "$OUT/libx2dhf_refc.so" \
+$CC -O2 -fPIC -shared -ffp-contract=off -fno-stack-protector -pthread -w -Dpthread_join=x2r_pthread_join \
+    -I "$OUT/src" -o "$OUT/libx2dhf_refc.so" \
     "$OUT/src/sorpt.c" "$OUT/src/mcsor_pthread.c" "$OUT/src/mcsor_single_colour_pthread.c" \
     "$OUT/src/coulExch_pthread.c" "$OUT/src/relax_single_pot_pthread.c" "$HERE/ref_shim.c" -lm
 echo "built $OUT/libx2dhf_refc.so"

@@ -3,18 +3,34 @@
  *
  * x2dhf's src/c/*.c read their parameters from Fortran COMMON blocks and
  * call back into Fortran (putinc_/putoutc_).  Without a Fortran compiler
- * this file provides both, so the reference's own sorpt_,
- * mcsor_pthread_ / mcsor_single_colour_pthread_ and coulExch_pthread_ run
- * unmodified as a checker and as the timed CPU reference:
+ * this file provides both, so the reference's own sorpt_ and
+ * mcsor_pthread_ / mcsor_single_colour_pthread_ run unmodified as a checker
+ * and as the timed CPU reference:
  *   - COMMON block instances with the layouts of src/c/sorpt.h:58-249,
  *   - putinc_/putoutc_ restated from src/inout.F90:195-290,
  *   - x2r_* setters that fill the blocks from plain arrays (the values the
  *     Fortran program writes in initCBAllocArrays.F90 initMesh:2053-2370,
- *     initAddr:1339-1466, initSuppl:1636-2051, relaxPots.F90:137-142).
+ *     initAddr:1339-1466, initSuppl:1636-2051, relaxPots.F90:137-142),
+ *   - x2r_coulexch: the thread-per-potential driver of coulExch_pthread.c /
+ *     relax_single_pot_pthread.c restated around the reference's sorpt_.
+ *     The reference's own driver writes one element past a stack array
+ *     (relax_single_pot_pthread.c:47), which is not safe to run on aarch64.
  */
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 #include "sorpt.h"
+
+/* The reference sources are compiled with -Dpthread_join=x2r_pthread_join:
+ * they pass an int* as the void** exit value (mcsor_pthread.c:87,
+ * coulExch_pthread.c:120), so the real call would store a pointer into 4
+ * bytes of their stack.  The exit value is never used; it is discarded. */
+#undef pthread_join
+extern int pthread_join(pthread_t, void **);
+int x2r_pthread_join(pthread_t t, void **ret) {
+  (void)ret;
+  return pthread_join(t, NULL);
+}
 
 struct commonBlock_1_t c_interface_1_;
 struct commonBlock_2_t c_interface_2_;
@@ -210,7 +226,78 @@ void x2r_set_batch(int iorb, int npots, const int *ins1, const int *ins2, const 
   }
   c_interface_8_.nexchpotsc[iorb - 1] = npots;
 }
+/* One potential k of orbital iorb's batch: relax_single_pot_pthread.c:15-110
+ * (rhs = psi_in1 psi_in2 g, lhs = f3 + idel^2 e, maxsor1 x putinc_, sorpt_,
+ * putoutc_) with its own, correctly sized sor_t. */
+struct x2r_pot { int k, iorb; };
+static void *x2r_relax_pot(void *arg) {
+  const struct x2r_pot *a = (const struct x2r_pot *)arg;
+  const int k = a->k, iorb = a->iorb;
+  int nnu = c_interface_17_.nnu1c - 8, mxnmu = c_interface_17_.mxnmuc;
+  const int mxsize = c_interface_17_.mxsizec, maxsor1 = c_interface_17_.maxsor1c;
+  const int in1 = c_interface_1_.ins1[k][iorb - 1], in2 = c_interface_2_.ins2[k][iorb - 1];
+  const int ib1 = c_interface_7_.i1bc[in1 - 1], ib2 = c_interface_7_.i1bc[in2 - 1];
+  const int ibexc = c_interface_3_.ibexcpc[k][iorb - 1], idel = c_interface_4_.deltam4potc[k][iorb - 1];
+  int isym = c_interface_6_.isymsc[k][iorb - 1];
+  const double deltam2 = (double)idel * idel;
+  double *psi = c_orbptr_.cw_orb, *excp = c_exchptr_.cw_exch;
+  double *suppl = c_supplptr_.cw_suppl;
+  const double *ef = &suppl[c_i4b_.i4barr[3] - 1], *f3 = &suppl[c_i4b_.i4barr[7] - 1];
+  const double *gf = &suppl[c_i4b_.i4barr[9] - 1];
+  struct sor_t p;
+  memset(&p, 0, sizeof p);
+  p.threadsNum = 1;
+  p.threadNum = 0;
+  p.indxex = &c_sorptr_.cw_sor[c_iadex_.iadextc - 1];
+  p.indx = &c_sorptr_.cw_sor[c_iadex_.iadnorc - 1];
+  p.indx6a = &c_sorptr_.cw_sor[c_iadex_.iadex1c - 1];
+  p.indx6b = &c_sorptr_.cw_sor[c_iadex_.iadex2c - 1];
+  p.indx7 = &c_sorptr_.cw_sor[c_iadex_.iadex3c - 1];
+  p.b = &suppl[c_i4b_.i4barr[1] - 1];
+  p.d = &suppl[c_i4b_.i4barr[2] - 1];
+  p.isym = isym;
+  double *lhs = (double *)malloc(mxsize * sizeof(double));
+  double *rhs = (double *)malloc(mxsize * sizeof(double));
+  double *wk2 = (double *)malloc((size_t)(nnu + 8) * (mxnmu + 8) * sizeof(double));
+  for (int i = 0; i < mxsize; i++) rhs[i] = psi[ib1 + i - 1] * psi[ib2 + i - 1] * gf[i];
+  if (deltam2 == 0.0)
+    for (int i = 0; i < mxsize; i++) lhs[i] = f3[i];
+  else
+    for (int i = 0; i < mxsize; i++) lhs[i] = f3[i] + ef[i] * deltam2;
+  p.g = rhs;
+  p.e = lhs;
+  for (int it = 1; it <= maxsor1; it++) {
+    putinc_(&nnu, &mxnmu, &isym, &excp[ibexc - 1], wk2);
+    p.uext = wk2;
+    sorpt_((void *)&p);
+    putoutc_(&nnu, &mxnmu, &excp[ibexc - 1], wk2);
+  }
+  free(lhs);
+  free(rhs);
+  free(wk2);
+  return NULL;
+}
+
+/* coulExch_pthread.c:19-125: every potential of orbital iorb's batch, one
+ * thread each (a single potential runs on the calling thread). */
 void x2r_coulexch(int iorb) {
   c_interface_46_.iorbc = iorb;
-  coulExch_pthread_();
+  c_interface_17_.isstartc = 1;
+  c_interface_17_.isstopc = g_ngrid1;
+  const int n = c_interface_8_.nexchpotsc[iorb - 1];
+  if (n <= 0) return;
+  struct x2r_pot *args = (struct x2r_pot *)malloc(sizeof(struct x2r_pot) * n);
+  pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * n);
+  for (int k = 0; k < n; k++) {
+    args[k].k = k;
+    args[k].iorb = iorb;
+  }
+  if (n == 1) {
+    x2r_relax_pot(&args[0]);
+  } else {
+    for (int k = 0; k < n; k++) pthread_create(&th[k], NULL, x2r_relax_pot, &args[k]);
+    for (int k = 0; k < n; k++) pthread_join(th[k], NULL);
+  }
+  free(args);
+  free(th);
 }
