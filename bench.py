@@ -76,7 +76,35 @@ stop
 """
 
 
-WORKLOADS = {"n2": n2_deck, "h2": h2_deck}
+def kf_deck():
+    """KF (Z=19,9, R=4.1035 bohr; 3 pi + 8 sigma, 11 Coulomb + 61 exchange
+    potentials per SCF iteration) from the reference's kf-elprop/set-01 input,
+    on grid 793x1201 -> 781x1201, R_inf=60: the heteronuclear large-grid case."""
+    with open(os.path.join(ROOT, "tests", "golden", "kf_set01.input")) as f:
+        deck = f.read()
+    out = []
+    for ln in deck.splitlines():
+        key = ln.strip().lower()
+        if key.startswith("grid"):
+            ln = "grid 793 1201 60.0"
+        elif key.startswith(("mmoments", "conv", "stop", "!")):
+            continue
+        out.append(ln)
+    out += ["mcsor", "mcsor-ce", "stop"]
+    return "\n".join(out) + "\n"
+
+
+WORKLOADS = {"n2": n2_deck, "h2": h2_deck, "kf": kf_deck}
+# workloads timed over a fixed number of SCF iterations per step (a full
+# solve of the large grid takes thousands of iterations)
+FIXED_ITERS = {"kf": 20}
+WORKLOAD_TEXT = {
+    "n2": "N2 closed-shell HF SCF, Z=7,7 R=2.068, 6 orbitals, 22 Poisson solves/iteration, grid 337x481 -> 331x481, "
+          "R_inf=40",
+    "h2": "H2 HF SCF, Z=1,1 R=1.4, grid 169x241 -> 151x241, R_inf=40",
+    "kf": "KF HF SCF, Z=19,9 R=4.1035, 11 orbitals (3 pi, 8 sigma), 72 Poisson solves/iteration, grid 793x1201 -> "
+          "781x1201, R_inf=60; first 20 SCF iterations from the hydrogenic start per step",
+}
 
 
 def slater_sources(grid_h, nnu, nmu, r, batch, seed0=1234):
@@ -206,7 +234,7 @@ def run_gpu(args):
             if e2e:
                 case = xg.parse_deck(deck, precision=prec)
                 scf = xg.SCF(ctx, case)
-            res = scf.run()
+            res = scf.run(FIXED_ITERS.get(args.workload, 1 << 30))
             if e2e:
                 for i in range(1, case.norb + 1):
                     scf.orbital(i)
@@ -258,19 +286,24 @@ def run_gpu(args):
     # per-launch figures of the dominant kernel of the headline (mixed) run
     sweep_gbs_mx = ptsmx * BYTES_PER_PT[1] / (msmx / 1e3) / 1e9 if msmx > 0 else None
     sweep_gbs_64 = pts64 * BYTES_PER_PT[0] / (ms64 / 1e3) / 1e9 if ms64 > 0 else None
-    value = world * args.steps / totmx
-    fp64_value = world * args.steps / tot64
-    e2e_value = world * len(late2e) / tote2e
+    per_step = FIXED_ITERS.get(args.workload, 1)  # solves, or iterations for a fixed-iteration workload
+    unit = "SCF iterations/s" if args.workload in FIXED_ITERS else UNIT
+    metric = (f"SCF iterations/s over the first {per_step} iterations: mixed vs FP64 MCSOR, 1 GB300"
+              if args.workload in FIXED_ITERS else METRIC)
+    value = world * args.steps * per_step / totmx
+    fp64_value = world * args.steps * per_step / tot64
+    e2e_value = world * len(late2e) * per_step / tote2e
+    on_chip = xg.host_cluster_plan(c.nnu, c.nmu)[0] > 0
     mx_sorted = sorted(latmx)
     p99 = mx_sorted[min(len(mx_sorted) - 1, int(round(0.99 * (len(mx_sorted) - 1))))]
     h2d = (c.norb * 2 + 16) * (c.nnu + 8) * (c.nmu + 8) * 8  # orbitals + potentials of the initial guess
     d2h = c.norb * c.nnu * c.nmu * 8
     pts_per_launch = ptsmx / nmx if nmx else None
-    traffic = CLUSTER_DRAM_BYTES_PER_PT * pts_per_launch if pts_per_launch else None
+    traffic = CLUSTER_DRAM_BYTES_PER_PT * pts_per_launch if (pts_per_launch and on_chip) else None
     out = {
-        "metric": METRIC,
+        "metric": metric,
         "value": value,
-        "unit": UNIT,
+        "unit": unit,
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
@@ -279,12 +312,9 @@ def run_gpu(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32 sweeps + f64 defect correction (value); f64 (fp64 leg)",
-        "data": "synthetic: hydrogenic LCAO start of the reference's N2 input, no dataset",
+        "data": "synthetic: hydrogenic LCAO start of the reference's own input deck, no dataset",
         "config": {
-            "workload": f"{args.workload}: " + ("N2 closed-shell HF SCF, Z=7,7 R=2.068, 6 orbitals, 22 Poisson "
-                                                "solves/iteration, grid 337x481 -> 331x481, R_inf=40"
-                                                if args.workload == "n2" else
-                                                "H2 HF SCF, Z=1,1 R=1.4, grid 169x241 -> 151x241, R_inf=40"),
+            "workload": f"{args.workload}: " + WORKLOAD_TEXT[args.workload],
             "grid": [c.nnu, c.nmu],
             "points_per_sweep": mx_pts,
             "convergence": "orbital-energy change < 1e-12 for 4 consecutive SCF iterations",
@@ -292,18 +322,20 @@ def run_gpu(args):
             "parallelism": "replicas only (independent SCF solves per GPU)",
         },
         "latency_s": {"p50": statistics.median(latmx), "p99": p99, "fp64_p50": statistics.median(lat64)},
-        "fp64": {"value": fp64_value, "unit": UNIT, "iterations": it64,
+        "fp64": {"value": fp64_value, "unit": unit, "iterations": it64,
                  "total_energy": res64.total_energy if res64 else None, "sweeps": res64.sweeps if res64 else None},
         "mixed": {"iterations": itmx, "total_energy": resmx.total_energy if resmx else None,
                   "sweeps": resmx.sweeps if resmx else None,
                   "dE_vs_fp64": abs(resmx.total_energy - res64.total_energy) if (resmx and res64) else None,
                   "speedup_vs_fp64": value / fp64_value},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e_value, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches_mx,
         "roofline": {
             "bound": "hbm",
-            "kernel": "k_mixed_cluster (mixed-form FP32 correction sweeps, one 16-CTA cluster per relaxation job, "
-                      "band resident in shared memory)",
+            "kernel": ("k_mixed_cluster (mixed-form FP32 correction sweeps, one 16-CTA cluster per relaxation job, "
+                       "band resident in shared memory)" if on_chip else
+                       "k_mcsor_f32 (mixed-form FP32 correction sweeps, persistent grid-barrier kernel: the grid's "
+                       "bands do not fit one cluster's shared memory)"),
             "achieved": sweep_gbs_mx, "peak": hbm, "unit": "GB/s",
             "frac": (sweep_gbs_mx / hbm) if sweep_gbs_mx else None, "traffic": traffic,
             "peak_kind": peak_kind,
@@ -322,8 +354,10 @@ def run_gpu(args):
         "clocks": sampler.summary(),
     }
     if not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(deck, res64.iterations if res64 else REF_ITERATIONS[args.workload],
-                                           args.cpu_iters)
+        if args.workload in FIXED_ITERS:
+            out["cpu_baseline"] = cpu_baseline_iterations(deck, min(args.cpu_iters, 4))
+        else:
+            out["cpu_baseline"] = cpu_baseline(deck, REF_ITERATIONS[args.workload], args.cpu_iters)
     return out
 
 
@@ -383,6 +417,45 @@ def run_poisson(args):
                          "peak_kind": peak_kind, "kernel_ms": kms, "launches": nl, "traffic": None}}
 
 
+def run_serve(args):
+    """Serving loop (survey config 5): seeded Poisson arrivals of closed-shell
+    diatomic HF solves (H2, LiH, FH, CO, N2 decks of the reference, bond
+    length +-10 %, grids 151..241 x 241..361, R_inf=40), `--slots` concurrent
+    solves on one GPU, mixed form and FP64 form on the same request stream."""
+    import x2dhf_gb300 as xg
+    from x2dhf_gb300 import build, serve
+
+    build.build()
+    templates = {}
+    for n in ("h2", "lih", "fh", "co", "n2"):
+        with open(os.path.join(ROOT, "tests", "golden", n + "_set01.input")) as f:
+            templates[n] = f.read()
+    reqs = serve.make_requests(templates, args.requests, rate=args.rate, seed=42)
+    # warm-up: one request per template, not timed
+    warm = [q for i, q in enumerate(reqs) if q.template not in {r.template for r in reqs[:i]}]
+    out = {}
+    sampler = ClockSampler(0)
+    with sampler:
+        for name, prec in (("mixed", xg.MIXED), ("fp64", xg.FP64)):
+            srv = serve.Server(slots=args.slots, precision=prec)
+            srv.run(warm, realtime=False)
+            done, wall = srv.run(reqs)
+            out[name] = dict(serve.summary(done, wall), peak_footprint_bytes=srv.peak_bytes)
+            out[name + "_energies"] = [c.total_energy for c in done]
+    de = max(abs(a - b) for a, b in zip(out["mixed_energies"], out["fp64_energies"]))
+    mx, f64 = out["mixed"], out["fp64"]
+    return {"metric": "served SCF solves/s and p99 latency (Poisson arrivals), mixed vs FP64", "value":
+            mx["solves_per_s"], "unit": "SCF solves/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": 1e3 * mx["wall_s"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 sweeps + f64 defect correction", "data": "synthetic: seeded request stream",
+            "config": {"workload": f"serve: {args.requests} requests, rate {args.rate}/s, {args.slots} slots, "
+                                   "H2/LiH/FH/CO/N2, R +-10 %, grids 151..241 x 241..361, R_inf=40"},
+            "latency_s": {"p50": mx["latency_p50_s"], "p99": mx["latency_p99_s"],
+                          "fp64_p50": f64["latency_p50_s"], "fp64_p99": f64["latency_p99_s"]},
+            "mixed": {k: v for k, v in mx.items()}, "fp64": {k: v for k, v in f64.items()},
+            "max_dE_mixed_vs_fp64": de, "clocks": sampler.summary()}
+
+
 def C_double_pair(xg, nnu, nmu):
     import ctypes as C
     a, b = C.c_double(), C.c_double()
@@ -390,11 +463,13 @@ def C_double_pair(xg, nnu, nmu):
     return a.value, b.value
 
 
-# SCF iterations of a full solve by the reference algorithm (MCSOR for
-# orbitals and potentials, hydrogenic start): the GPU FP64 form runs the same
-# algorithm sweep for sweep (bit-exact sweeps), and its full solve took these
-# iteration counts on GB300.
-REF_ITERATIONS = {"n2": 902, "h2": 311}
+# SCF iterations of a full solve by the reference algorithm: the
+# reference's own C relaxation kernels (MCSOR potentials through sorpt_ on
+# the colour lists, orbitals through mcsor_pthread_ on 8 threads) under the
+# oracle's SCF driver, run to its convergence exit on an x86 host.  The
+# multi-threaded reference MCSOR races at the colour seams, so another run
+# can stop a few iterations apart.
+REF_ITERATIONS = {"n2": 973, "h2": 313}
 
 
 def _ref_backend(deck, nthreads):
@@ -434,12 +509,42 @@ def cpu_baseline(deck, iterations_per_solve, sample_iters):
                       f"{iterations_per_solve} iterations/solve"}
 
 
+def cpu_baseline_iterations(deck, sample_iters):
+    """SCF iterations/s of the reference's C relaxation kernels under the
+    oracle's SCF driver, on a bounded sample of iterations of the same case."""
+    nthreads = min(16, os.cpu_count() or 1)
+    setup, per_iter, kind = cpu_sample(deck, sample_iters, nthreads)
+    return {"value": 1.0 / per_iter, "unit": "SCF iterations/s", "cores": nthreads, "kind": kind,
+            "sample": f"setup + prepSCF + 1 iteration ({setup:.2f} s), then {sample_iters} SCF iterations "
+                      f"({per_iter:.3f} s/iteration) on {nthreads} threads"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return None
     deck = WORKLOADS[args.workload]()
     nthreads = min(16, os.cpu_count() or 1)
+    if args.workload in FIXED_ITERS:
+        n = FIXED_ITERS[args.workload]
+        rates, kind = [], "port"
+        for step in range(args.warmup + args.steps):
+            setup, per_iter, kind = cpu_sample(deck, min(args.cpu_iters, 4), nthreads)
+            if step >= args.warmup:
+                rates.append(1.0 / per_iter)
+        v = statistics.median(rates)
+        unit = "SCF iterations/s"
+        return {
+            "metric": f"SCF iterations/s over the first {n} iterations: mixed vs FP64 MCSOR, 1 GB300", "value": v,
+            "unit": unit, "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: hydrogenic LCAO start of the reference's input", "impl": "reference",
+            "config": {"workload": f"{args.workload}: " + WORKLOAD_TEXT[args.workload]},
+            "cpu_baseline": {"value": v, "unit": unit, "cores": nthreads, "kind": kind,
+                             "sample": f"per step: setup + prepSCF + 1 iteration, then {min(args.cpu_iters, 4)} "
+                                       f"timed SCF iterations on {nthreads} threads"},
+            "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
     iters = REF_ITERATIONS[args.workload]
     lat, kind = [], "port"
     for step in range(args.warmup + args.steps):
@@ -467,7 +572,10 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="n2", choices=sorted(WORKLOADS) + ["poisson"])
+    ap.add_argument("--workload", default="n2", choices=sorted(WORKLOADS) + ["poisson", "serve"])
+    ap.add_argument("--requests", type=int, default=48, help="serve workload: requests in the stream")
+    ap.add_argument("--rate", type=float, default=4.0, help="serve workload: mean arrivals per second")
+    ap.add_argument("--slots", type=int, default=4, help="serve workload: concurrent solves")
     ap.add_argument("--cpu-iters", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--legs", default="all", choices=["all", "mixed", "fp64"],
@@ -479,6 +587,9 @@ def main():
         args.warmup = 3
     if args.workload == "poisson":
         out = run_poisson(args)
+    elif args.workload == "serve":
+        out = run_serve(args) if args.impl != "reference" else {
+            "impl": "reference", "unavailable": "the reference has no serving loop (config 5 is GPU-side only)"}
     else:
         out = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if out is not None:

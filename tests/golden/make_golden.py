@@ -23,6 +23,13 @@ CASES = {
     "h_set04": "h/set-04",     # H 1pi, 131x?, one electron
     "n2_set01": "n2-elprop/set-01",  # N2 421x781 R_inf=200, 6 orbitals, 22 potentials
 }
+# decks whose reference output is not in the distribution: the input only
+INPUT_ONLY = {
+    "kf_set01": "kf-elprop/set-01",  # KF, 3 pi + 8 sigma, 11 Coulomb + 61 exchange potentials
+    "lih_set01": "lih/set-01",       # LiH, 2 sigma (4 electrons)
+    "fh_set01": "fh-elprop/set-01",  # FH, 1 pi + 3 sigma (10 electrons)
+    "co_set01": "co-elprop/set-01",  # CO, 1 pi + 5 sigma (14 electrons)
+}
 
 LINE = re.compile(r"^\s*(\d+)\s+(\d+)\s+(sigma|pi|delta|phi)\s*([gu]?)\s+"
                   r"(-?\d\.\d+E[+-]\d+)\s+(-?\d\.\d+E[+-]\d+)\s+(-?\d\.\d+E[+-]\d+)")
@@ -65,6 +72,12 @@ def main():
             json.dump({"source": f"test-sets/{rel}/reference.lst", "records": recs,
                        "total_energy": etot, "sweeps": sweeps}, f, indent=0)
         print(f"{name}: {len(recs)} records, E={etot}, sweeps={sweeps}")
+    for name, rel in INPUT_ONLY.items():
+        with open(os.path.join(root, "test-sets", rel, "input.data")) as f:
+            deck = f.read()
+        with open(os.path.join(out, name + ".input"), "w") as f:
+            f.write(deck)
+        print(f"{name}: input deck only")
 
 
 if __name__ == "__main__":

@@ -182,6 +182,25 @@ def test_scf_ne_trajectory_matches_oracle():
     _scf_records_match("ne_set01", 25)
 
 
+def _kf_small(deck):
+    """KF (Z=19,9, R=4.1035, 3 pi + 8 sigma) on a 91x121 grid, R_inf=60."""
+    out = []
+    for ln in deck.splitlines():
+        key = ln.strip().lower()
+        if key.startswith("grid"):
+            ln = "grid 91 121 60.0"
+        if key.startswith(("mmoments", "conv", "!")):
+            continue
+        out.append(ln)
+    return "\n".join(out) + "\n"
+
+
+def test_scf_kf_trajectory_matches_oracle():
+    """11 orbitals incl. pi-pi exchange pairs (two potentials each),
+    heteronuclear: 72 potentials per SCF iteration."""
+    _scf_records_match("kf_set01", 6, _kf_small)
+
+
 def test_scf_he_converged_energy_vs_golden():
     """He MCSOR converged to 1e-12: the reference's own final energy."""
     deck = _all_mcsor(with_hydrogen0(golden_deck("he_set02")))
