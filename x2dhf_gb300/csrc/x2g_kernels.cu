@@ -1440,6 +1440,27 @@ static int take_event(x2g_ctx *ctx, cudaEvent_t *ev) {
   return (err == cudaSuccess) ? X2G_OK : cuda_status(err, "profiling event");
 }
 
+// The cluster kernel's function attributes are shared by every context and
+// thread of the process: the dynamic shared memory cap is set once to the
+// device's opt-in maximum (never lowered, so concurrent contexts with
+// different grids cannot undercut each other) and clusters above 8 CTAs are
+// allowed.  Idempotent.
+static bool cluster_attributes(x2g_ctx *ctx) {
+  if (ctx->cluster_smem_set > 0 && ctx->cluster_nonportable) return true;
+  int optin = 0;
+  if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device) != cudaSuccess ||
+      cudaFuncSetAttribute((const void *)k_mixed_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute((const void *)k_mixed_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+          cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  ctx->cluster_smem_set = size_t(optin);
+  ctx->cluster_nonportable = 1;
+  return true;
+}
+
 // whether the on-chip cluster sweep can run this grid here (asked once per
 // shape: shared memory per CTA, cluster size, block size)
 static bool cluster_usable(x2g_ctx *ctx, const GridDev &g) {
@@ -1449,14 +1470,8 @@ static bool cluster_usable(x2g_ctx *ctx, const GridDev &g) {
   if (ctx->cluster_checked_key != key) {
     ctx->cluster_checked_key = key;
     ctx->cluster_ok = 0;
-    bool attr_ok = cudaFuncSetAttribute((const void *)k_mixed_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        int(smem)) == cudaSuccess;
-    if (attr_ok && g.cl_size > 8)
-      attr_ok = cudaFuncSetAttribute((const void *)k_mixed_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed,
-                                     1) == cudaSuccess;
+    const bool attr_ok = cluster_attributes(ctx) && smem <= ctx->cluster_smem_set;
     if (attr_ok) {
-      ctx->cluster_smem_set = smem;
-      ctx->cluster_nonportable = (g.cl_size > 8);
       cudaLaunchConfig_t q = {};
       q.gridDim = dim3(unsigned(g.cl_size));
       q.blockDim = dim3(unsigned(32 * (g.cl_wa + g.cl_wb + g.cl_ws)));
@@ -1498,17 +1513,8 @@ static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, 
   }
   if (on_chip) {
     const size_t smem = cluster_smem_bytes(g);
-    if (smem > ctx->cluster_smem_set) {
-      err = cudaFuncSetAttribute((const void *)k_mixed_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 int(smem));
-      if (err != cudaSuccess) return cuda_status(err, "cluster kernel shared memory");
-      ctx->cluster_smem_set = smem;
-    }
-    if (g.cl_size > 8 && !ctx->cluster_nonportable) {
-      err = cudaFuncSetAttribute((const void *)k_mixed_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-      if (err != cudaSuccess) return cuda_status(err, "non-portable cluster size");
-      ctx->cluster_nonportable = 1;
-    }
+    if (!cluster_attributes(ctx) || smem > ctx->cluster_smem_set)
+      return set_status(X2G_ERR_CUDA, "cluster kernel attributes could not be set");
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(unsigned(njobs * g.cl_size));
     cfg.blockDim = dim3(unsigned(32 * (g.cl_wa + g.cl_wb + g.cl_ws)));
