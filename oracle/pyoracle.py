@@ -57,6 +57,8 @@ def lib():
         L.x2o_pot_info.argtypes = [P, I, I] + [C.POINTER(C.c_int)] * 4
         L.x2o_get_pot.argtypes = [P, I, I, dp]
         L.x2o_set_pot.argtypes = [P, I, I, dp]
+        L.x2o_set_orbital_energy.argtypes = [P, I, C.c_double]
+        L.x2o_set_moments.argtypes = [P, dp, dp]
         L.x2o_putin.argtypes = [I, I, I, dp, dp]
         L.x2o_putout.argtypes = [I, I, dp, dp]
         L.x2o_sweep.argtypes = [P, I, I, I, D, dp, dp, dp, dp, dp, I, I, I]
@@ -179,6 +181,27 @@ class Case:
 
     def set_pot(self, iorb, k, v):
         self.L.x2o_set_pot(self.h, iorb, k, np.ascontiguousarray(v, np.float64))
+
+    def load_checkpoint(self, ck):
+        """orbpot old: orbitals, Coulomb and exchange potentials and the
+        diagonal Lagrange multipliers of a checkpoint (x2dhf_gb300.checkpoint)
+        into the case's storage (readFuncs, src/diskInterface.F90:247-779)."""
+        m = ck.m
+        for i in range(1, ck.norb + 1):
+            self.set_orbital(i, ck.orbitals[i - 1].reshape(-1))
+            self.L.x2o_set_orbital_energy(self.h, i, float(ck.ee[i - 1, i - 1]))
+        for iorb in range(1, ck.norb + 1):
+            for k in range(1, self.npots(iorb) + 1):
+                in1, in2, idel, _ = self.pot_info(iorb, k)
+                if in1 == in2 and idel == 0:
+                    v = ck.coulomb[in1 - 1]
+                else:
+                    a, b = min(in1, in2), max(in1, in2)
+                    second = a != b and m[a - 1] > 0 and m[b - 1] > 0 and idel == m[a - 1] + m[b - 1]
+                    v = ck.exchange[(a, b, 1 if second else 0)]
+                self.set_pot(iorb, k, v.reshape(-1))
+        self.L.x2o_set_moments(self.h, np.ascontiguousarray(ck.cmulti, np.float64),
+                               np.ascontiguousarray(ck.exc, np.float64).reshape(-1))
 
     def relax_pot(self, iorb, k, mode=1):
         self.L.x2o_relax_pot(self.h, iorb, k, mode)

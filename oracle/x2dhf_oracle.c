@@ -58,7 +58,7 @@ struct x2o_state {
   double recalcMMfactor, orbEnergyIncThld;
   int lhomonucl, lbreakCi;
   int maxsororb[2], maxsorpot[2];
-  int hydrogen_start;
+  int hydrogen_start, old_start;
 
   /* ---------------- grid ---------------- */
   int mxnmu, mxsize, nni8, mxsize8;
@@ -371,7 +371,18 @@ x2o_state *x2o_from_input(const char *text, char *err, int errlen) {
     } else if (!strcmp(label, "orbpot")) {
       /* src/inputInterface.F90:2257-2360 */
       const char *src = tok_str(&c);
-      if (strcmp(src, "hydrogen")) { snprintf(err, errlen, "only orbpot hydrogen is supported"); ok = 0; break; }
+      if (!strcmp(src, "old")) {
+        /* linitFuncsOld (:2311-2313): functions, Lagrange multipliers and
+         * moments come from a checkpoint (readFromDisk), no frozen start;
+         * the caller loads them with x2o_set_orbital/x2o_set_pot/
+         * x2o_set_orbital_energy after x2o_setup */
+        s->hydrogen_start = 0;
+        s->old_start = 1;
+        s->lfixorb4init = 0; s->lfixorb = 0;
+        for (int i = 1; i <= s->norb; i++) s->ifixorb[i] = 0;
+        continue;
+      }
+      if (strcmp(src, "hydrogen")) { snprintf(err, errlen, "only orbpot hydrogen and old are supported"); ok = 0; break; }
       int itmp;
       if (tok_int(&c, &itmp)) s->ienterm4init = itmp;
       if (s->ienterm4init > 0) {
@@ -1774,19 +1785,22 @@ static void prep_scf(x2o_state *s) {
   double *fk1 = dalloc(s->mxsize), *fk2 = dalloc(s->mxsize);
   for (int iorb = 1; iorb <= s->norb; iorb++) x2o_fock(s, iorb, fk1, fk2);
   free(fk1); free(fk2);
-  /* initAddData (hydrogenic start) */
-  for (int iorb = 1; iorb <= s->norb; iorb++) {
-    int jorb = s->norb + 1 - iorb;
-    x2o_norm(s, jorb);
-    x2o_ortho(s, jorb);
-  }
-  for (int iorb = 1; iorb <= s->norb; iorb++) s->itouch[iorb] = 1;
-  s->lmpoleInit = 1;
-  x2o_mpole_moments(s, 0);
-  for (int iorb = s->norb; iorb >= 1; iorb--) {
-    x2o_eahf(s, iorb);
-    s->eeOld[iorb] = s->ee[iorb][iorb];
-    eabhf(s, iorb);
+  /* initAddData (hydrogenic start, doSCF.F90:73-134); a checkpoint start
+   * keeps the stored norms, moments and Lagrange multipliers */
+  if (!s->old_start) {
+    for (int iorb = 1; iorb <= s->norb; iorb++) {
+      int jorb = s->norb + 1 - iorb;
+      x2o_norm(s, jorb);
+      x2o_ortho(s, jorb);
+    }
+    for (int iorb = 1; iorb <= s->norb; iorb++) s->itouch[iorb] = 1;
+    s->lmpoleInit = 1;
+    x2o_mpole_moments(s, 0);
+    for (int iorb = s->norb; iorb >= 1; iorb--) {
+      x2o_eahf(s, iorb);
+      s->eeOld[iorb] = s->ee[iorb][iorb];
+      eabhf(s, iorb);
+    }
   }
   x2o_etotal(s, NULL, NULL, NULL, NULL);
   if (s->verbose) {
@@ -2019,6 +2033,19 @@ void x2o_coeffs(const x2o_state *s, double *dmu1, double *dmu2, double *dni1, do
   memcpy(exeven, s->exeven, 40); *diag = s->diag;
 }
 void x2o_get_orbital(const x2o_state *s, int iorb, double *out) { memcpy(out, s->psi[iorb], sizeof(double) * s->mxsize); }
+/* multipole moments of an orbpot old start, as the checkpoint stores them
+ * (readFuncs, diskInterface.F90:350-390): cmulti(iorb + (k-1) norb) for
+ * MAXORB*MAXMPOLE entries, then excdi, excqu, ..., exc8 by pair index ipc,
+ * MAXORB*(MAXORB+1) entries each */
+void x2o_set_moments(x2o_state *s, const double *cmulti, const double *exc) {
+  for (int i = 1; i <= MAXMPOLE * MAXORB; i++) s->cmulti[i] = cmulti[i - 1];
+  for (int k = 0; k < MAXMPOLE; k++)
+    for (int i = 1; i <= MAXORB * (MAXORB + 1); i++) s->excm[k][i] = exc[k * MAXORB * (MAXORB + 1) + i - 1];
+}
+
+/* ee(iorb,iorb) of an orbpot old start (readFuncs, diskInterface.F90:335-337) */
+void x2o_set_orbital_energy(x2o_state *s, int iorb, double ee) { s->ee[iorb][iorb] = ee; }
+
 void x2o_set_orbital(x2o_state *s, int iorb, const double *in) { memcpy(s->psi[iorb], in, sizeof(double) * s->mxsize); }
 int x2o_npots(const x2o_state *s, int iorb) { return s->nexchpots[iorb]; }
 void x2o_pot_info(const x2o_state *s, int iorb, int k, int *in1, int *in2, int *idel, int *isym) {

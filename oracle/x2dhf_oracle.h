@@ -28,7 +28,7 @@ extern "C" {
 
 typedef struct x2o_state x2o_state;
 
-/* Parse a reference input file (cards: title method nuclei config grid orbpot
+/* Parse a reference input file (cards: title method nuclei config grid orbpot [hydrogen|old]
  * lcao scf conv mcsor mcsor-o mcsor-ce omega multipol altsweeps homo break
  * sor4orb sor4pot stop) -- restates src/inputInterface.F90:681-818 for the HF
  * subset.  Returns NULL and fills err on failure. */
@@ -73,6 +73,12 @@ void x2o_coeffs(const x2o_state *s, double *dmu1, double *dmu2, double *dni1, do
                 double *exeven, double *diag);
 void x2o_get_orbital(const x2o_state *s, int iorb, double *out);      /* plain mxsize */
 void x2o_set_orbital(x2o_state *s, int iorb, const double *in);
+/* diagonal Lagrange multiplier of iorb (an orbpot old start reads it from
+ * the checkpoint, src/diskInterface.F90:335-337) */
+void x2o_set_orbital_energy(x2o_state *s, int iorb, double ee);
+/* multipole moments stored in a checkpoint: cmulti (MAXORB*MAXMPOLE
+ * entries) and the exchange moments excdi..exc8 (8 x MAXORB*(MAXORB+1)) */
+void x2o_set_moments(x2o_state *s, const double *cmulti, const double *exc);
 /* potential slot k of orbital iorb's relaxation batch (1-based, k<=npots) */
 int x2o_npots(const x2o_state *s, int iorb);
 void x2o_pot_info(const x2o_state *s, int iorb, int k, int *in1, int *in2, int *idel, int *isym);

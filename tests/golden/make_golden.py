@@ -7,6 +7,8 @@ orbital label, orbital energy, energy difference, 1-norm), the final total
 energy and the (MC)SOR sweep count printed by the reference program.
 
 These files are the pins of the CPU oracle (tests/test_oracle_golden.py).
+The reference's own checkpoint files of be/set-01 (be-hf.*) are copied
+unchanged: they pin the checkpoint reader and the orbpot old start.
 Run:  python tests/golden/make_golden.py [/path/to/x2dhf]
 """
 import json
@@ -22,7 +24,10 @@ CASES = {
     "ne_set01": "ne/set-01",   # Ne 151x181, 4 orbitals incl. 1pi, SOR
     "h_set04": "h/set-04",     # H 1pi, 131x?, one electron
     "n2_set01": "n2-elprop/set-01",  # N2 421x781 R_inf=200, 6 orbitals, 22 potentials
+    "be_set01": "be/set-01",   # Be 151x181, SOR, started from the be-hf checkpoint (orbpot old)
 }
+# reference checkpoint files (orbpot old starts), copied as they are
+CHECKPOINTS = {"be_set01": ("be/set-01", "be-hf")}
 # decks whose reference output is not in the distribution: the input only
 INPUT_ONLY = {
     "kf_set01": "kf-elprop/set-01",  # KF, 3 pi + 8 sigma, 11 Coulomb + 61 exchange potentials
@@ -72,6 +77,14 @@ def main():
             json.dump({"source": f"test-sets/{rel}/reference.lst", "records": recs,
                        "total_energy": etot, "sweeps": sweeps}, f, indent=0)
         print(f"{name}: {len(recs)} records, E={etot}, sweeps={sweeps}")
+    for name, (rel, prefix) in CHECKPOINTS.items():
+        os.makedirs(os.path.join(out, name), exist_ok=True)
+        for ext in ("dat", "orb", "coul", "exch"):
+            with open(os.path.join(root, "test-sets", rel, f"{prefix}.{ext}"), "rb") as f:
+                blob = f.read()
+            with open(os.path.join(out, name, f"{prefix}.{ext}"), "wb") as f:
+                f.write(blob)
+        print(f"{name}: checkpoint {prefix}.{{dat,orb,coul,exch}}")
     for name, rel in INPUT_ONLY.items():
         with open(os.path.join(root, "test-sets", rel, "input.data")) as f:
             deck = f.read()
