@@ -219,6 +219,9 @@ typedef struct {
   int mpole;                    /* multipole terms (4) */
   int homonuclear;              /* g/u labels given: enforce C_i (setCi) */
   int precision;                /* X2G_FP64 or X2G_MIXED */
+  int start;                    /* 0: hydrogenic LCAO guess (orbpot hydrogen); 1: functions, moments and
+                                   Lagrange multipliers loaded by the caller before the first run
+                                   (orbpot old: x2g_scf_set_function, x2g_scf_set_start_values) */
 } x2g_case;
 
 typedef struct {
@@ -242,6 +245,24 @@ int x2g_scf_run(x2g_scf *scf, int max_iterations, x2g_result *result);
  * plain array of N_nu*N_mu values. */
 int x2g_scf_get_orbital(x2g_scf *scf, int iorb, double *host_plain);
 int x2g_scf_get_coulomb(x2g_scf *scf, int iorb, double *host_plain);
+/* Functions of the SCF as plain nnu*nmu host arrays (nu fastest): kind 0
+ * orbital i1, 1 Coulomb potential of i1, 2 exchange potential of the pair
+ * i1 <= i2 (which = 1: the second potential of two non-sigma orbitals,
+ * Delta m = m1 + m2); i2 = which = 0 for kinds 0 and 1.  Setting them before
+ * the first x2g_scf_run is the orbpot old start (readFuncs,
+ * src/diskInterface.F90:247-779). */
+int x2g_scf_set_function(x2g_scf *scf, int kind, int i1, int i2, int which, const double *host_plain);
+int x2g_scf_get_function(x2g_scf *scf, int kind, int i1, int i2, int which, double *host_plain);
+/* Values an orbpot old start takes from the checkpoint instead of
+ * recomputing them (prepSCF runs no initAddData, src/doSCF.F90:73-134), in
+ * the checkpoint's layout: diagonal Lagrange multipliers ee[norb], norms
+ * orbnorm[norb], Coulomb moments cmulti[iorb-1 + (k-1) norb] (X2G_MAXORB*8
+ * entries) and exchange moments exc[(k-1) X2G_MAXORB(X2G_MAXORB+1) +
+ * ipc-1] (8 arrays).  The getter returns the current values (for writing a
+ * checkpoint). */
+int x2g_scf_set_start_values(x2g_scf *scf, const double *ee, const double *orbnorm, const double *cmulti,
+                             const double *exc);
+int x2g_scf_get_start_values(x2g_scf *scf, double *ee, double *orbnorm, double *cmulti, double *exc);
 /* Per-iteration record i (0-based): iscf, iorb, ee, delta ee, 1-norm. */
 int x2g_scf_nrecords(x2g_scf *scf);
 int x2g_scf_record(x2g_scf *scf, int i, int *iscf, int *iorb, double *ee, double *dee, double *dnorm);

@@ -45,7 +45,7 @@ class Case(C.Structure):
         ("nscf2skip", C.c_int), ("nenlast", C.c_int), ("nnolast", C.c_int),
         ("maxsor_orb", C.c_int), ("maxsor_pot", C.c_int),
         ("omega_orb", C.c_double), ("omega_pot", C.c_double), ("recalc_mm", C.c_double),
-        ("mpole", C.c_int), ("homonuclear", C.c_int), ("precision", C.c_int),
+        ("mpole", C.c_int), ("homonuclear", C.c_int), ("precision", C.c_int), ("start", C.c_int),
     ]
 
 
@@ -70,6 +70,7 @@ EXPORTS = [
     "x2g_grid_table", "x2g_grid_info", "x2g_relax", "x2g_putin", "x2g_putout", "x2g_mcsor_host",
     "x2g_quadrature", "x2g_case_defaults", "x2g_scf_create", "x2g_scf_destroy", "x2g_scf_run",
     "x2g_scf_get_orbital", "x2g_scf_get_coulomb", "x2g_scf_nrecords", "x2g_scf_record",
+    "x2g_scf_set_function", "x2g_scf_get_function", "x2g_scf_set_start_values", "x2g_scf_get_start_values",
     "x2g_kernel_launches", "mcsor_pthread_", "mcsor_tpool_", "coulExch_pthread_", "coulExch_tpool_",
     "tpoolStop4mcsor_", "tpoolStop4pots_", "x2g_host_table", "x2g_host_schedule", "x2g_profile",
     "x2g_relax_noalloc", "x2g_host_cluster_plan", "x2g_set_mixed_on_chip", "x2g_host_cluster_chunks",
@@ -117,6 +118,10 @@ def lib():
     L.x2g_scf_run.argtypes = [P, I, C.POINTER(Result)]
     L.x2g_scf_get_orbital.argtypes = [P, I, dp]
     L.x2g_scf_get_coulomb.argtypes = [P, I, dp]
+    L.x2g_scf_set_function.argtypes = [P, I, I, I, I, dp]
+    L.x2g_scf_get_function.argtypes = [P, I, I, I, I, dp]
+    L.x2g_scf_set_start_values.argtypes = [P, dp, dp, dp, dp]
+    L.x2g_scf_get_start_values.argtypes = [P, dp, dp, dp, dp]
     L.x2g_scf_nrecords.argtypes = [P]
     L.x2g_scf_record.argtypes = [P, I, C.POINTER(C.c_int), C.POINTER(C.c_int), dp, dp, dp]
     L.x2g_host_table.argtypes = [I, I, D, D, D, D, I, dp]
@@ -216,8 +221,15 @@ def parse_deck(text, precision=FP64):
         elif lab == "grid":
             grid = ln[1:]
         elif lab == "orbpot":
+            if ln[1] == "old":
+                # functions, moments and Lagrange multipliers from a
+                # checkpoint (SCF.load_checkpoint), no frozen phase
+                c.start = 1
+                c.ienterm4init = 0
+                hydrogen = True
+                continue
             if ln[1] != "hydrogen":
-                raise ValueError("only orbpot hydrogen is supported")
+                raise ValueError("only orbpot hydrogen and orbpot old are supported")
             hydrogen = True
             v = nums(ln[2:])
             if v:
@@ -441,6 +453,49 @@ class SCF:
         out = np.zeros(self.case.nnu * self.case.nmu)
         _check(self.L.x2g_scf_get_orbital(self.h, iorb, _dp(out)))
         return out
+
+    def function(self, kind, i1, i2=0, which=0):
+        """Plain nnu*nmu copy: kind 0 orbital, 1 Coulomb, 2 exchange (i1 <= i2)."""
+        out = np.zeros(self.case.nnu * self.case.nmu)
+        _check(self.L.x2g_scf_get_function(self.h, kind, i1, i2, which, _dp(out)))
+        return out
+
+    def load_checkpoint(self, ck):
+        """orbpot old start from a checkpoint (x2dhf_gb300.checkpoint):
+        orbitals, Coulomb and exchange potentials, Lagrange multipliers,
+        norms and multipole moments, before the first run."""
+        from .checkpoint import MAXMPOLE, MAXORB
+
+        if (ck.nnu, ck.nmu, ck.norb) != (self.case.nnu, self.case.nmu, self.case.norb):
+            raise ValueError("checkpoint grid or orbital count differs from the case")
+        for i in range(1, ck.norb + 1):
+            _check(self.L.x2g_scf_set_function(self.h, 0, i, 0, 0, _dp(np.ascontiguousarray(ck.orbitals[i - 1]))))
+            _check(self.L.x2g_scf_set_function(self.h, 1, i, 0, 0, _dp(np.ascontiguousarray(ck.coulomb[i - 1]))))
+        for (a, b, w), v in ck.exchange.items():
+            _check(self.L.x2g_scf_set_function(self.h, 2, a, b, w, _dp(np.ascontiguousarray(v))))
+        ee = np.ascontiguousarray(np.diag(ck.ee), np.float64)
+        nrm = np.ones(ck.norb) if ck.orbnorm is None else np.ascontiguousarray(ck.orbnorm[:ck.norb], np.float64)
+        cm = np.zeros(MAXORB * MAXMPOLE) if ck.cmulti is None else np.ascontiguousarray(ck.cmulti, np.float64)
+        ex = (np.zeros(8 * MAXORB * (MAXORB + 1)) if ck.exc is None
+              else np.ascontiguousarray(ck.exc, np.float64).reshape(-1))
+        _check(self.L.x2g_scf_set_start_values(self.h, _dp(ee), _dp(nrm), _dp(cm), _dp(ex)))
+
+    def checkpoint(self, title="x2dhf-gb300", nel=None):
+        """The current state as a checkpoint (write it with checkpoint.write)."""
+        from . import checkpoint as ckm
+
+        c = self.case
+        n, shape = c.norb, (c.nmu, c.nnu)
+        m = [int(c.m[i]) for i in range(n)]
+        ee, nrm = np.zeros(n), np.zeros(n)
+        cm, ex = np.zeros(ckm.MAXORB * ckm.MAXMPOLE), np.zeros(8 * ckm.MAXORB * (ckm.MAXORB + 1))
+        _check(self.L.x2g_scf_get_start_values(self.h, _dp(ee), _dp(nrm), _dp(cm), _dp(ex)))
+        orbs = [self.function(0, i).reshape(shape) for i in range(1, n + 1)]
+        couls = [self.function(1, i).reshape(shape) for i in range(1, n + 1)]
+        exch = {k: self.function(2, *k).reshape(shape) for k in ckm.exchange_order(m)}
+        nel = nel if nel is not None else int(round(sum(c.occ[i] for i in range(n))))
+        return ckm.Checkpoint(title, c.nnu, c.nmu, c.rinf, c.z1, c.z2, c.r, nel, m, orbs, couls, exch, np.diag(ee),
+                              nrm, cm, ex.reshape(8, -1))
 
     def coulomb(self, iorb):
         out = np.zeros(self.case.nnu * self.case.nmu)

@@ -537,8 +537,16 @@ void update_wst(x2g_scf *s, int iorb) {
 }
 
 int prep_scf(x2g_scf *s) {
-  // prepSCF (doSCF.F90:24-174), hydrogenic start
+  // prepSCF (doSCF.F90:24-174)
   for (int i = 1; i <= s->norb; i++) fock(s, i);
+  if (s->cs.start == 1) {
+    // orbpot old: no initAddData, the checkpoint's norms, moments and
+    // Lagrange multipliers stand (doSCF.F90:73-134)
+    int rc = read_scalars(s);
+    if (rc) return rc;
+    for (int i = 1; i <= s->norb; i++) s->eeOld[i] = s->ee[i];
+    return etotal(s);
+  }
   for (int i = 1; i <= s->norb; i++) {
     int j = s->norb + 1 - i;
     norm(s, j);
@@ -863,12 +871,17 @@ int x2g_scf_create(x2g_ctx *ctx, const x2g_case *c, x2g_scf **out) {
         s->mm_ipc.push_back(ipc + norb * (norb + 1) / 2);
       }
     }
-  if ((rc = initial_guess(s))) {
+  if (c->start != 0 && c->start != 1) {
+    x2g_scf_destroy(s);
+    return set_status(X2G_ERR_ARG, "start must be 0 (hydrogenic) or 1 (loaded by the caller)");
+  }
+  if (c->start == 0 && (rc = initial_guess(s))) {
     x2g_scf_destroy(s);
     return rc;
   }
-  // orbpot hydrogen [ienterm4init] (inputInterface.F90:2257-2305)
-  if (c->ienterm4init > 0) {
+  // orbpot hydrogen [ienterm4init] (inputInterface.F90:2257-2305); an
+  // orbpot old start has no frozen phase
+  if (c->start == 0 && c->ienterm4init > 0) {
     s->lfixorb4init = s->lfixorb = 1;
     for (int i = 1; i <= norb; i++) s->ifixorb[i] = 1;
   }
@@ -942,6 +955,92 @@ int x2g_scf_get_coulomb(x2g_scf *s, int iorb, double *host) {
   if (rc) return rc;
   for (int i = 0; i < g.nmu; i++)
     for (int j = 0; j < g.nni; j++) host[i * g.nni + j] = ext[(i + 4) * g.n8 + j + 4];
+  return X2G_OK;
+}
+
+// device array of (kind, i1, i2, which), or null when it names no function
+static double *function_ptr(x2g_scf *s, int kind, int i1, int i2, int which) {
+  if (i1 < 1 || i1 > s->norb) return nullptr;
+  if (kind == 0 && i2 == 0 && which == 0) return s->orb[i1];
+  if (kind == 1 && i2 == 0 && which == 0) return s->coul[i1];
+  if (kind != 2 || i2 < i1 || i2 > s->norb || (which != 0 && which != 1)) return nullptr;
+  if (i1 == i2 && s->m[i1] == 0) return nullptr;  // no sigma self-exchange
+  const int k = s->k2[i1][i2];
+  if (which == 0) return s->exch[2 * k];
+  return (i1 != i2 && s->ilc2[i1][i2] == 2) ? s->exch[2 * k + 1] : nullptr;
+}
+
+int x2g_scf_set_function(x2g_scf *s, int kind, int i1, int i2, int which, const double *host) {
+  if (!s || !host) return set_status(X2G_ERR_ARG, "null argument");
+  double *d = function_ptr(s, kind, i1, i2, which);
+  if (!d) return set_status(X2G_ERR_ARG, "no such function");
+  cudaSetDevice(s->ctx->device);
+  int rc = x2g_synchronize(s->ctx);
+  if (rc) return rc;
+  std::vector<double> plain(host, host + s->grid->h.mxsize);
+  return upload_ext(s, d, plain);
+}
+
+int x2g_scf_get_function(x2g_scf *s, int kind, int i1, int i2, int which, double *host) {
+  if (!s || !host) return set_status(X2G_ERR_ARG, "null argument");
+  double *d = function_ptr(s, kind, i1, i2, which);
+  if (!d) return set_status(X2G_ERR_ARG, "no such function");
+  cudaSetDevice(s->ctx->device);
+  const HostGrid &g = s->grid->h;
+  std::vector<double> ext(g.next);
+  cudaError_t e = cudaMemcpyAsync(ext.data(), d, ext.size() * sizeof(double), cudaMemcpyDeviceToHost, s->ctx->stream);
+  if (e != cudaSuccess) return cuda_status(e, "function readback");
+  int rc = x2g_synchronize(s->ctx);
+  if (rc) return rc;
+  for (int i = 0; i < g.nmu; i++)
+    for (int j = 0; j < g.nni; j++) host[i * g.nni + j] = ext[(i + 4) * g.n8 + j + 4];
+  return X2G_OK;
+}
+
+// checkpoint layout <-> device scalars: cmulti(iorb + (k-1) norb) <->
+// O_CM + 8 (iorb-1) + k-1; exc_k(ipc) <-> O_EX + 8 ipc + k-1
+static constexpr size_t kExcLen = size_t(X2G_MAXORB) * (X2G_MAXORB + 1);
+
+int x2g_scf_set_start_values(x2g_scf *s, const double *ee, const double *orbnorm, const double *cmulti,
+                             const double *exc) {
+  if (!s || !ee || !orbnorm || !cmulti || !exc) return set_status(X2G_ERR_ARG, "null argument");
+  if (s->started) return set_status(X2G_ERR_ARG, "start values must be set before the first run");
+  cudaSetDevice(s->ctx->device);
+  int rc = x2g_synchronize(s->ctx);
+  if (rc) return rc;
+  std::vector<double> h(s->sc_count);
+  cudaError_t e = cudaMemcpy(h.data(), s->sc, h.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_status(e, "start values");
+  const int norb = s->norb;
+  for (int i = 1; i <= norb; i++) {
+    h[x2g_scf::O_EE + i] = s->ee[i] = ee[i - 1];
+    h[x2g_scf::O_NORM + i] = s->orbNorm[i] = orbnorm[i - 1];
+    for (int k = 1; k <= 8; k++) h[x2g_scf::O_CM + 8 * (i - 1) + (k - 1)] = cmulti[(i - 1) + (k - 1) * norb];
+  }
+  for (int ipc = 1; ipc < s->nslots && size_t(ipc) <= kExcLen; ipc++)
+    for (int k = 1; k <= 8; k++) h[x2g_scf::O_EX + 8 * size_t(ipc) + (k - 1)] = exc[(k - 1) * kExcLen + ipc - 1];
+  e = cudaMemcpy(s->sc, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? X2G_OK : cuda_status(e, "start values");
+}
+
+int x2g_scf_get_start_values(x2g_scf *s, double *ee, double *orbnorm, double *cmulti, double *exc) {
+  if (!s || !ee || !orbnorm || !cmulti || !exc) return set_status(X2G_ERR_ARG, "null argument");
+  cudaSetDevice(s->ctx->device);
+  int rc = x2g_synchronize(s->ctx);
+  if (rc) return rc;
+  std::vector<double> h(s->sc_count);
+  cudaError_t e = cudaMemcpy(h.data(), s->sc, h.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_status(e, "start values");
+  const int norb = s->norb;
+  std::fill(cmulti, cmulti + size_t(X2G_MAXORB) * 8, 0.0);
+  std::fill(exc, exc + 8 * kExcLen, 0.0);
+  for (int i = 1; i <= norb; i++) {
+    ee[i - 1] = h[x2g_scf::O_EE + i];
+    orbnorm[i - 1] = h[x2g_scf::O_NORM + i];
+    for (int k = 1; k <= 8; k++) cmulti[(i - 1) + (k - 1) * norb] = h[x2g_scf::O_CM + 8 * (i - 1) + (k - 1)];
+  }
+  for (int ipc = 1; ipc < s->nslots && size_t(ipc) <= kExcLen; ipc++)
+    for (int k = 1; k <= 8; k++) exc[(k - 1) * kExcLen + ipc - 1] = h[x2g_scf::O_EX + 8 * size_t(ipc) + (k - 1)];
   return X2G_OK;
 }
 
