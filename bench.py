@@ -195,6 +195,19 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def max_over_ranks(values, world, device):
+    """Element-wise maximum of per-rank timings over all ranks (replicas run
+    the same work independently; no collective touches the data path)."""
+    if world <= 1:
+        return list(values)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor(values, device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
 def run_gpu(args):
     import torch
     import x2dhf_gb300 as xg
@@ -270,13 +283,8 @@ def run_gpu(args):
             msmx, ptsmx, nmx = ctx.profile(-1, xg.MIXED)
             ctx.profile(0, xg.FP64)
             late2e, rese2e, _ = timed_solves(xg.MIXED, max(1, args.steps // 2), 1, e2e=True)
-    # max over ranks
-    tot64, totmx, tote2e = sum(lat64), sum(latmx), sum(late2e)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([tot64, totmx, tote2e], device=f"cuda:{local}", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot64, totmx, tote2e = t.tolist()
+    # max over ranks: the slowest replica sets the pace
+    tot64, totmx, tote2e = max_over_ranks([sum(lat64), sum(latmx), sum(late2e)], world, f"cuda:{local}")
     if rank != 0:
         return None
     hbm, peak_kind = peaks()

@@ -1,0 +1,63 @@
+"""Multi-GPU path (replicas only) on the CPU: two gloo ranks reduce their
+timings with bench.max_over_ranks; the reference arm runs on rank 0 only."""
+import os
+import socket
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, world, port, out):
+    sys.path.insert(0, ROOT)
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    import torch.distributed as dist
+
+    import bench
+
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    mine = [1.0 + rank, 10.0 - rank, 0.5 * (rank + 1)]
+    out[rank] = bench.max_over_ranks(mine, world, "cpu")
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_max_over_ranks_gloo_two_ranks():
+    torch = pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    out = ctx.Manager().dict()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, out)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    assert out[0] == out[1] == [2.0, 10.0, 1.0]
+
+
+def test_single_rank_is_identity():
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert bench.max_over_ranks([3.0, 4.0], 1, "cpu") == [3.0, 4.0]
+
+
+def test_reference_arm_runs_on_rank_zero_only(monkeypatch):
+    sys.path.insert(0, ROOT)
+    import argparse
+
+    import bench
+
+    monkeypatch.setenv("RANK", "1")
+    args = argparse.Namespace(workload="n2", warmup=3, steps=1, cpu_iters=1)
+    assert bench.run_reference(args) is None
