@@ -233,3 +233,51 @@ def test_integer_pipe_conversions_match_hardware(ctx):
     (NaN to NaN) on edge cases and 16M hashed bit patterns, outside the float
     subnormal range that they flush to zero."""
     assert ctx.convert_selftest(1 << 24, seed=12345) == 0
+
+
+def _initial_functions_match(deck, rtol=1e-13):
+    """Every orbital, Coulomb and exchange potential of the hydrogenic /
+    Thomas-Fermi start (initOrbitalsPotentials.F90:714-934,
+    coulombExchangePotentials.f90:14-239), evaluated on the device, against
+    the oracle's start on the same grid; device exp/pow may differ from the
+    host's in the last bit, so the bound is relative to each function's
+    largest value."""
+    oc = Case(deck)
+    ctx = xg.Context(0)
+    s = xg.SCF(ctx, xg.parse_deck(deck))
+    m = [int(s.case.m[i]) for i in range(s.case.norb)]
+    checked = 0
+    for i in range(1, s.case.norb + 1):
+        ref, got = oc.orbital(i), s.function(0, i)
+        assert np.max(np.abs(got - ref)) <= rtol * np.max(np.abs(ref)), ("orbital", i)
+        checked += 1
+    for iorb in range(1, s.case.norb + 1):
+        for k in range(1, oc.npots(iorb) + 1):
+            in1, in2, idel, _ = oc.pot_info(iorb, k)
+            if in1 == in2 and idel == 0:
+                got = s.function(1, in1)
+            else:
+                a, b = min(in1, in2), max(in1, in2)
+                second = a != b and m[a - 1] > 0 and m[b - 1] > 0 and idel == m[a - 1] + m[b - 1]
+                got = s.function(2, a, b, 1 if second else 0)
+            ref = oc.pot(iorb, k)
+            assert np.max(np.abs(got - ref)) <= rtol * max(np.max(np.abs(ref)), 1e-300), (iorb, k, in1, in2, idel)
+            checked += 1
+    assert checked > s.case.norb
+    s.close()
+    ctx.close()
+
+
+def test_initial_guess_n2_matches_oracle():
+    """N2: sigma and pi orbitals on both centres, pi-pi exchange pairs."""
+    _initial_functions_match(golden_deck("n2_set01"))
+
+
+def test_initial_guess_kf_matches_oracle():
+    """KF: heteronuclear, 3 pi + 8 sigma, n up to 4 (Laguerre and Legendre
+    series of several terms)."""
+    _initial_functions_match(_kf_small(golden_deck("kf_set01")))
+
+
+def test_initial_guess_lih_matches_oracle():
+    _initial_functions_match(golden_deck("lih_set01"))

@@ -79,15 +79,34 @@ double *dalloc(x2g_scf *s, size_t n) {
 
 // ---------------------------------------------------------------------
 // hydrogenic start (initOrbitalsPotentials.F90:714-934) and initial
-// potentials (coulombExchangePotentials.f90:14-239), evaluated on the host
+// potentials (coulombExchangePotentials.f90:14-239), evaluated on the
+// device, one elementwise launch per function; the orbital-constant
+// prefactors are formed on the host
 // ---------------------------------------------------------------------
-double factorial(int n) {
+// unfused product and sum on both sides: the device compiler would
+// otherwise contract a*b+c into one rounding, unlike the host build
+__host__ __device__ inline double mul_rn(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+__host__ __device__ inline double add_rn(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dadd_rn(a, b);
+#else
+  return a + b;
+#endif
+}
+
+__host__ __device__ inline double factorial(int n) {
   double f = 1.0;
   for (int i = 1; i <= n; i++) f = double(i) * f;
   return f;
 }
 
-double hyp1f1(int np, int lp, double x) {  // utils.f90:265-282
+__host__ __device__ inline double hyp1f1(int np, int lp, double x) {  // utils.f90:265-282
   double h = 1.0;
   if (-np == 0) return h;
   double t = double(np) * x / double(lp);
@@ -99,7 +118,7 @@ double hyp1f1(int np, int lp, double x) {  // utils.f90:265-282
   return h;
 }
 
-double hyp2f1(int na, int nb, int nc, double x) {  // utils.f90:289-309
+__host__ __device__ inline double hyp2f1(int na, int nb, int nc, double x) {  // utils.f90:289-309
   double h = 1.0;
   if (na == 0) return h;
   double a = na, b = nb, c = nc;
@@ -114,42 +133,111 @@ double hyp2f1(int na, int nb, int nc, double x) {  // utils.f90:289-309
 
 // associated Legendre as evaluated by plegendg (utils.f90:315-335); its
 // prefactor is written (-one**m), i.e. always -1 in Fortran precedence
-double plegendre(int l, int m, double c) {
-  double ct = std::fabs(1.0 - c * c);
+__host__ __device__ inline double plegendre(int l, int m, double c) {
+  double ct = fabs(add_rn(1.0, -mul_rn(c, c)));
   if (m == 0) return hyp2f1(-l, l + 1, 1, (1.0 - c) / 2.0);
   if (ct < kPrecis) return 0.0;
-  double fn0 = -std::pow(1.0, double(m)) * factorial(l + m) / factorial(l - m) / factorial(m) / std::pow(2.0, double(m));
-  return hyp2f1(m - l, m + l + 1, m + 1, (1.0 - c) / 2.0) * (fn0 * std::pow(ct, double(m) / 2.0));
+  double fn0 = -pow(1.0, double(m)) * factorial(l + m) / factorial(l - m) / factorial(m) / pow(2.0, double(m));
+  return hyp2f1(m - l, m + l + 1, m + 1, (1.0 - c) / 2.0) * (fn0 * pow(ct, double(m) / 2.0));
 }
 
-double hydrogenic(const HostGrid &g, int n, int l, int m, double z, bool centre_b, int i, int j) {
-  const double r = g.r;
-  double fn = std::pow(2.0 * z / double(n), 3.0 / 2.0 + double(l)) *
-              std::sqrt(factorial(n + l) / (2.0 * double(n) * factorial(n - l - 1))) / factorial(2 * l + 1);
-  double shn = (m == 0 ? 1.0 : std::pow(-1.0, double(m))) / std::sqrt(4.0 * kPi) *
-               std::sqrt((2.0 * l + 1.0) * factorial(l - m) / factorial(l + m));
-  double z0 = (r / 2.0) * g.vxi[i] * g.veta[j];
+// one hydrogenic function |n l m> of charge z on centre A or B
+struct HydroTerm {
+  int n, l, use, centre_b;
+  double z, co, fn, shn;
+};
+struct GuessOrbital {
+  HydroTerm t[2];
+  int m;
+};
+
+HydroTerm hydro_term(int n, int l, int m, double z, double co, bool centre_b) {
+  HydroTerm t{};
+  t.n = n;
+  t.l = l;
+  t.z = z;
+  t.co = co;
+  t.centre_b = centre_b;
+  t.use = std::fabs(co) > kPrecis;
+  t.fn = std::pow(2.0 * z / double(n), 3.0 / 2.0 + double(l)) *
+         std::sqrt(factorial(n + l) / (2.0 * double(n) * factorial(n - l - 1))) / factorial(2 * l + 1);
+  t.shn = (m == 0 ? 1.0 : std::pow(-1.0, double(m))) / std::sqrt(4.0 * kPi) *
+          std::sqrt((2.0 * l + 1.0) * factorial(l - m) / factorial(l + m));
+  return t;
+}
+
+__device__ double hydro_value(const HydroTerm &t, int m, double r, double xi, double eta) {
+  const double z0 = (r / 2.0) * xi * eta;
   double rt, c;
-  if (!centre_b) {
-    rt = (r / 2.0) * (g.vxi[i] + g.veta[j]);
-    c = (rt < kPrecis) ? -1.0 : std::min(1.0, std::max(-1.0, (z0 + r / 2.0) / rt));
+  if (!t.centre_b) {
+    rt = (r / 2.0) * (xi + eta);
+    c = (rt < kPrecis) ? -1.0 : fmin(1.0, fmax(-1.0, (z0 + r / 2.0) / rt));
   } else {
-    rt = (r / 2.0) * (g.vxi[i] - g.veta[j]);
-    c = (rt < kPrecis) ? -1.0 : std::min(1.0, std::max(-1.0, -(z0 - r / 2.0) / rt));
+    rt = (r / 2.0) * (xi - eta);
+    c = (rt < kPrecis) ? -1.0 : fmin(1.0, fmax(-1.0, -(z0 - r / 2.0) / rt));
   }
-  int np = n - l - 1, lp = 2 * l + 2;
-  double x = z * rt / double(n);
-  double lag = std::pow(rt, double(l)) * std::exp(-x) * hyp1f1(-np, lp, x + x);
-  return fn * lag * shn * plegendre(l, m, c);
+  const int np = t.n - t.l - 1, lp = 2 * t.l + 2;
+  const double x = t.z * rt / double(t.n);
+  const double lag = __dmul_rn(__dmul_rn(pow(rt, double(t.l)), exp(-x)), hyp1f1(-np, lp, x + x));
+  return __dmul_rn(__dmul_rn(__dmul_rn(t.fn, lag), t.shn), plegendre(t.l, m, c));
 }
 
-double thomas_fermi(double r, double veta, double vxi) {  // pottf, coulombExchangePotentials.f90:222-239
-  if (std::fabs(vxi + veta) < kPrecis) return 0.0;
+// pottf, coulombExchangePotentials.f90:222-239
+__host__ __device__ inline double thomas_fermi(double r, double veta, double vxi) {
+  if (fabs(vxi + veta) < kPrecis) return 0.0;
   double rab = r * (vxi + veta) / 2.0;
-  double w = std::sqrt(rab / 0.885340);
-  double t = w * (0.6011200 * w + 1.8106100) + 1.0;
-  w = w * (w * (w * (w * (0.0479300 * w + 0.2146500) + 0.7711200) + 1.3951500) + 1.8106100) + 1.0;
-  return (1.0 - (t / w) * (t / w)) / rab;
+  double w = sqrt(rab / 0.885340);
+  double t = add_rn(mul_rn(w, add_rn(mul_rn(0.6011200, w), 1.8106100)), 1.0);
+  double p = add_rn(mul_rn(0.0479300, w), 0.2146500);
+  p = add_rn(mul_rn(w, p), 0.7711200);
+  p = add_rn(mul_rn(w, p), 1.3951500);
+  p = add_rn(mul_rn(w, p), 1.8106100);
+  w = add_rn(mul_rn(w, p), 1.0);
+  return add_rn(1.0, -mul_rn(t / w, t / w)) / rab;
+}
+
+// orbital: co1 |n1 l1 m>_A + co2 |n2 l2 m>_B on the interior of ext
+__global__ void k_guess_orbital(GridDev g, double r, GuessOrbital a, double *ext) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+    const int i = k / g.nni, j = k - i * g.nni;
+    double psi = 0.0;
+    for (int p = 0; p < 2; p++)
+      if (a.t[p].use) psi = __dadd_rn(__dmul_rn(a.t[p].co, hydro_value(a.t[p], a.m, r, g.vxi[i], g.veta[j])), psi);
+    ext[(i + 4) * g.n8 + j + 4] = psi;
+  }
+}
+
+// Coulomb potential: -(TF_A crt1 + TF_B crt2) f4 (initCoulomb)
+__global__ void k_guess_coulomb(GridDev g, double r, double crt1, double crt2, int both, double *ext) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+    const int i = k / g.nni, j = k - i * g.nni;
+    double v;
+    if (i == 0 && (j == 0 || j == g.nni - 1))
+      v = 0.0;
+    else if (both)
+      v = __dadd_rn(__dmul_rn(-1.0 * thomas_fermi(r, g.veta[j], g.vxi[i]), crt1),
+                    __dmul_rn(-1.0 * thomas_fermi(r, -g.veta[j], g.vxi[i]), crt2));
+    else
+      v = __dmul_rn(-1.0 * thomas_fermi(r, g.veta[j], g.vxi[i]), crt1);
+    ext[(i + 4) * g.n8 + j + 4] = __dmul_rn(v, g.f4[k]);
+  }
+}
+
+// exchange potential: (co1/r_A + co2/r_B) f4 off the axis rows/columns
+// (initExchange); ext2, when set, receives the same values
+__global__ void k_guess_exchange(GridDev g, double r, double co1, double co2, double *ext, double *ext2) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+    const int i = k / g.nni, j = k - i * g.nni;
+    double v = 0.0;
+    if (i >= 1 && j >= 1 && j < g.nni - 1) {
+      const double ra1 = (r / 2.0) * (g.vxi[i] + g.veta[j]), ra2 = (r / 2.0) * (g.vxi[i] - g.veta[j]);
+      v = (ra1 > 1.0e-8) ? co1 / ra1 : 0.0;
+      if (ra2 > 1.0e-8) v = __dadd_rn(v, co2 / ra2);
+    }
+    v = __dmul_rn(v, g.f4[k]);
+    ext[(i + 4) * g.n8 + j + 4] = v;
+    if (ext2) ext2[(i + 4) * g.n8 + j + 4] = v;
+  }
 }
 
 int upload_ext(x2g_scf *s, double *dst, const std::vector<double> &plain) {
@@ -162,64 +250,36 @@ int upload_ext(x2g_scf *s, double *dst, const std::vector<double> &plain) {
 }
 
 int initial_guess(x2g_scf *s) {
-  const HostGrid &g = s->grid->h;
+  const HostGrid &h = s->grid->h;
+  const GridDev &g = s->grid->d;
   const x2g_case &c = s->cs;
-  const int mx = g.mxsize;
-  std::vector<double> psi(mx), tmp(mx);
+  const int blocks = (h.mxsize + 255) / 256 < 1184 ? (h.mxsize + 255) / 256 : 1184;
+  cudaStream_t st = s->ctx->stream;
   for (int o = 1; o <= s->norb; o++) {
     const int k = o - 1;
-    std::fill(psi.begin(), psi.end(), 0.0);
-    for (int pass = 0; pass < 2; pass++) {
-      double co = pass ? c.co2[k] : c.co1[k];
-      if (!(std::fabs(co) > kPrecis)) continue;
-      int n = pass ? c.n2[k] : c.n1[k], l = pass ? c.l2[k] : c.l1[k];
-      double z = pass ? c.zb[k] : c.za[k];
-      for (int i = 0; i < g.nmu; i++)
-        for (int j = 0; j < g.nni; j++) tmp[i * g.nni + j] = hydrogenic(g, n, l, s->m[o], z, pass == 1, i, j);
-      for (int q = 0; q < mx; q++) psi[q] = co * tmp[q] + psi[q];
-    }
-    int rc = upload_ext(s, s->orb[o], psi);
-    if (rc) return rc;
+    GuessOrbital a{};
+    a.m = s->m[o];
+    a.t[0] = hydro_term(c.n1[k], c.l1[k], s->m[o], c.za[k], c.co1[k], false);
+    a.t[1] = hydro_term(c.n2[k], c.l2[k], s->m[o], c.zb[k], c.co2[k], true);
+    k_guess_orbital<<<blocks, 256, 0, st>>>(g, h.r, a, s->orb[o]);
   }
-  const int iz1 = int(std::lround(g.z1)), iz2 = int(std::lround(g.z2));
+  const int iz1 = int(std::lround(h.z1)), iz2 = int(std::lround(h.z2));
   for (int o = 1; o <= s->norb; o++) {
     const int k = o - 1;
-    double crt1 = std::fabs(c.co1[k]), crt2 = std::fabs(c.co2[k]);
-    for (int i = 0; i < g.nmu; i++)
-      for (int j = 0; j < g.nni; j++) {
-        double v;
-        if (i == 0 && (j == 0 || j == g.nni - 1))
-          v = 0.0;
-        else if (iz1 != 0 && iz2 != 0)
-          v = -1.0 * thomas_fermi(g.r, g.veta[j], g.vxi[i]) * crt1 + -1.0 * thomas_fermi(g.r, -g.veta[j], g.vxi[i]) * crt2;
-        else
-          v = -1.0 * thomas_fermi(g.r, g.veta[j], g.vxi[i]) * crt1;
-        psi[i * g.nni + j] = v * g.f4[i * g.nni + j];
-      }
-    int rc = upload_ext(s, s->coul[o], psi);
-    if (rc) return rc;
+    k_guess_coulomb<<<blocks, 256, 0, st>>>(g, h.r, std::fabs(c.co1[k]), std::fabs(c.co2[k]),
+                                            (iz1 != 0 && iz2 != 0) ? 1 : 0, s->coul[o]);
   }
   for (int i1 = 1; i1 <= s->norb; i1++)
     for (int i2 = i1; i2 <= s->norb; i2++) {
       if (i1 == i2 && s->m[i2] == 0) continue;
       const int kk = s->k2[i1][i2];
-      std::fill(psi.begin(), psi.end(), 0.0);
-      for (int i = 1; i < g.nmu; i++)
-        for (int j = 1; j < g.nni - 1; j++) {
-          double ra1 = (g.r / 2.0) * (g.vxi[i] + g.veta[j]), ra2 = (g.r / 2.0) * (g.vxi[i] - g.veta[j]);
-          double v = (ra1 > 1.0e-8) ? c.co1[i1 - 1] / ra1 : 0.0;
-          if (ra2 > 1.0e-8) v = v + c.co2[i1 - 1] / ra2;
-          psi[i * g.nni + j] = v;
-        }
-      for (int q = 0; q < mx; q++) psi[q] = psi[q] * g.f4[q];
-      int rc = upload_ext(s, s->exch[2 * kk], psi);
-      if (rc) return rc;
-      if (i1 != i2 && s->m[i1] != 0 && s->m[i2] != 0) {
-        rc = upload_ext(s, s->exch[2 * kk + 1], psi);
-        if (rc) return rc;
-      }
+      double *second = (i1 != i2 && s->m[i1] != 0 && s->m[i2] != 0) ? s->exch[2 * kk + 1] : nullptr;
+      k_guess_exchange<<<blocks, 256, 0, st>>>(g, h.r, c.co1[i1 - 1], c.co2[i1 - 1], s->exch[2 * kk], second);
     }
-  return X2G_OK;
+  s->ctx->launches += 2 * s->norb;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  return e == cudaSuccess ? X2G_OK : cuda_status(e, "initial guess");
 }
 
 // exchange weights of a closed-shell configuration (initExWeights:3303-3436)
