@@ -342,15 +342,21 @@ def run_gpu(args):
             "bound": "hbm",
             "kernel": ("k_mixed_cluster (mixed-form FP32 correction sweeps, one 16-CTA cluster per relaxation job, "
                        "band resident in shared memory)" if on_chip else
-                       "k_mcsor_f32 (mixed-form FP32 correction sweeps, persistent grid-barrier kernel: the grid's "
-                       "bands do not fit one cluster's shared memory)"),
+                       "k_mcsor_f32s (mixed-form FP32 correction sweeps, persistent grid-barrier kernel staging "
+                       "each work item's rows in shared memory: the grid's bands do not fit one cluster's shared "
+                       "memory)"),
             "achieved": sweep_gbs_mx, "peak": hbm, "unit": "GB/s",
             "frac": (sweep_gbs_mx / hbm) if sweep_gbs_mx else None, "traffic": traffic,
             "peak_kind": peak_kind,
             "bytes_per_point_update": BYTES_PER_PT[1],
-            "note": "achieved = 16 algorithmic B per point-update / launch time; the correction lives in shared "
-                    "memory during the sweeps, so DRAM traffic is far below it and the launch is bound by the "
-                    "colour-phase latency (cluster barrier + shared-memory pipe), not by HBM",
+            "note": ("achieved = 16 algorithmic B per point-update / launch time; the correction lives in shared "
+                     "memory during the sweeps, so DRAM traffic is far below it and the launch is bound by the "
+                     "colour-phase latency (cluster barrier + shared-memory pipe), not by HBM" if on_chip else
+                     "achieved = 16 algorithmic B per point-update / launch time; every colour phase copies each "
+                     "work item's rows with 4-row halos from L2 into shared memory and streams the item's "
+                     "(residual, omega/lhs) pairs once per sweep; a launch takes only as many jobs as keep their "
+                     "corrections and pairs within 3/4 of L2, so DRAM traffic stays below the algorithmic bytes and "
+                     "the launch is bound by phase latency (grid barrier, staging, level chain), not by HBM"),
             "sweep_ms_total": msmx, "sweep_launches": nmx, "point_updates": ptsmx,
             "point_updates_per_launch": pts_per_launch,
             "fp64_kernel": {"kernel": "k_mcsor_f64", "achieved_gbs": sweep_gbs_64,

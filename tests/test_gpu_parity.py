@@ -281,3 +281,26 @@ def test_initial_guess_kf_matches_oracle():
 
 def test_initial_guess_lih_matches_oracle():
     _initial_functions_match(golden_deck("lih_set01"))
+
+
+def test_mixed_staged_sweep_scf_matches_on_chip():
+    """KF on 241x301 in the mixed form, once with the cluster sweep and once
+    with the staged grid-barrier sweep (batches of 32 potentials run as runs
+    of several tiles per work item, single orbitals one tile per item): both
+    sweep the same schedule, so the SCF records agree to the FP32 rounding
+    of the corrections, far below the FP64 defect-corrected energies."""
+    deck = _all_mcsor(_kf_small(golden_deck("kf_set01")))
+    ctx = xg.Context(0)
+    recs = []
+    for on_chip in (True, False):
+        ctx.set_mixed_on_chip(on_chip)
+        s = xg.SCF(ctx, xg.parse_deck(deck, precision=xg.MIXED))
+        s.run(4)
+        recs.append(s.records())
+        s.close()
+    ctx.set_mixed_on_chip(True)
+    assert len(recs[0]) == len(recs[1]) > 0
+    for a, b in zip(*recs):
+        assert a[:2] == b[:2]
+        assert abs(a[2] - b[2]) <= 1e-9 * max(1.0, abs(a[2])), (a, b)
+    ctx.close()

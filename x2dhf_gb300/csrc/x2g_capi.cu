@@ -299,6 +299,9 @@ int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, doubl
   UP(h.pts, pts);
   UP(h.off, off);
   UP(h.pts_rc, pts_rc);
+  UP(h.st_pts, st_pts);
+  UP(h.st_off, st_off);
+  for (int k = 0; k < 5; ++k) d.st_rows[k] = h.st_rows[k];
   d.cl_size = h.cl_size;
   d.cl_maxrows = h.cl_maxrows;
   d.cl_maxchunks = h.cl_maxchunks;

@@ -52,6 +52,14 @@ struct HostGrid {
   // has cl_size * 5 * (nlev + 2) + 1 chunk offsets; cl_wa/wb/ws warps per
   // CTA work on the three kinds
   std::vector<int> cl_pts, cl_off;
+  // staged FP32 sweep of grids beyond one cluster: the same points regrouped
+  // [colour][level][tile] (st_pts, packed (ext row << 16) | ext col), so that the points of one
+  // colour and level in any run of consecutive tiles are one contiguous
+  // range; st_off[(c * nlev + l) * (ntiles + 1) + t] is the start of tile t.
+  // st_rows[G] = most rows of any run of G consecutive tiles (G = 1..4), plus
+  // the 4-row halos on both sides
+  std::vector<int> st_pts, st_off;
+  int st_rows[5] = {0, 0, 0, 0, 0};
 };
 
 std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf, double z1, double z2, int mpole);
@@ -70,6 +78,8 @@ struct GridDev {
   const int *tile_row0, *tile_row1, *pts, *off, *pts_rc;
   int cl_size, cl_maxrows, cl_maxchunks, cl_wa, cl_wb, cl_ws;
   const int *cl_tile0, *cl_row0, *cl_pts, *cl_off;
+  const int *st_pts, *st_off;
+  int st_rows[5];
   // FP32 copies of the coefficient tables for the mixed form
   const float *borb_mu32, *bpot_mu32, *d_nu32;
   // separable stencil weights of the mixed form's FP64 residual: for the
@@ -98,6 +108,7 @@ struct JobDev {
   double *rhs_buf;  // materialised rhs for potentials
   float *e32;       // mixed: FP32 extended correction
   float *r32, *w32; // mixed: FP32 residual and omega / diagonal
+  float2 *rw;       // mixed, staged sweep: (residual, omega / diagonal) in st_pts order
   double omega;
   double idel2;
   float omegaf, omega1f;  // omega and 1 - omega rounded to FP32 on the host
@@ -139,6 +150,10 @@ struct x2g_ctx {
   int cluster_nonportable = 0;  // cluster kernel allowed more than 8 CTAs
   long cluster_checked_key = -1;  // (shared bytes, cluster size) last checked
   int cluster_ok = 0;             // that cluster shape is schedulable here
+  int staged_attr = 0;            // shared memory cap granted to the staged sweep
+  long staged_key = -1;           // shared bytes of the last staged occupancy query
+  int staged_blocks = 0;          // co-resident staged blocks for that size
+  size_t l2_bytes = 0;            // device L2 size (0: not queried yet)
   // optional per-launch timing of the sweep kernels (CUDA events on stream)
   int profiling = 0;
   struct Pending {

@@ -18,6 +18,7 @@ namespace x2g {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kStagedThreads = 512;
 constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
 
 __device__ __forceinline__ double A(double a, double b) { return __dadd_rn(a, b); }
@@ -108,20 +109,21 @@ struct CoefF {
   float dmu1[4], dmu2[4], dni1[4], dni2[4];
 };
 
-// FP32 correction sweep point update (same operator, FMA allowed); w is
-// omega / lhs of the point, formed once per relaxation call.
-__device__ __forceinline__ void relax_f32(float *__restrict__ e, int ij, int n8, const CoefF &c, float b, float d,
-                                          float w, float r, float omega1) {
+// FP32 correction sweep point update (same operator, FMA allowed) on a band
+// of the correction staged in shared memory; w is omega / lhs of the point,
+// formed once per relaxation call.  Returns the new value.
+__device__ __forceinline__ float relax_f32(const float *__restrict__ e, int ij, int n8, const CoefF &c, float b,
+                                           float d, float w, float r, float omega1) {
   const int n1 = n8, n2 = 2 * n8, n3 = 3 * n8, n4 = 4 * n8;
-  const float m4 = ldcg(e + ij - n4), p4 = ldcg(e + ij + n4);
-  const float m3 = ldcg(e + ij - n3), p3 = ldcg(e + ij + n3);
-  const float m2 = ldcg(e + ij - n2), p2 = ldcg(e + ij + n2);
-  const float m1 = ldcg(e + ij - n1), p1 = ldcg(e + ij + n1);
-  const float l4 = ldcg(e + ij - 4), r4 = ldcg(e + ij + 4);
-  const float l3 = ldcg(e + ij - 3), r3 = ldcg(e + ij + 3);
-  const float l2 = ldcg(e + ij - 2), r2 = ldcg(e + ij + 2);
-  const float l1 = ldcg(e + ij - 1), r1 = ldcg(e + ij + 1);
-  const float ec = ldcg(e + ij);
+  const float m4 = e[ij - n4], p4 = e[ij + n4];
+  const float m3 = e[ij - n3], p3 = e[ij + n3];
+  const float m2 = e[ij - n2], p2 = e[ij + n2];
+  const float m1 = e[ij - n1], p1 = e[ij + n1];
+  const float l4 = e[ij - 4], r4 = e[ij + 4];
+  const float l3 = e[ij - 3], r3 = e[ij + 3];
+  const float l2 = e[ij - 2], r2 = e[ij + 2];
+  const float l1 = e[ij - 1], r1 = e[ij + 1];
+  const float ec = e[ij];
   float dm2 = c.dmu2[0] * (m4 + p4);
   dm2 = __fmaf_rn(c.dmu2[1], m3 + p3, dm2);
   dm2 = __fmaf_rn(c.dmu2[2], m2 + p2, dm2);
@@ -139,7 +141,7 @@ __device__ __forceinline__ void relax_f32(float *__restrict__ e, int ij, int n8,
   dn1 = __fmaf_rn(c.dni1[2], l2 - r2, dn1);
   dn1 = __fmaf_rn(c.dni1[3], l1 - r1, dn1);
   const float cc = __fmaf_rn(d, dn1, __fmaf_rn(b, dm1, dm2) + dn2);
-  e[ij] = __fmaf_rn(omega1, ec, w * (r - cc));
+  return __fmaf_rn(omega1, ec, w * (r - cc));
 }
 
 // ----------------------------------------------------------------------
@@ -315,9 +317,22 @@ __global__ void __launch_bounds__(kThreads) k_mcsor_f64(GridDev g, const __grid_
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_mcsor_f32(GridDev g, const __grid_constant__ JobTable jobs, int njobs,
-                                                        int nsweeps, BarrierDev bar, unsigned nblocks) {
-  const int nitems = njobs * g.ntiles;
+// Staged persistent FP32 sweep for grids whose bands do not fit one cluster's
+// shared memory.  A work item is a run of G consecutive tiles of one job; in
+// every colour phase its block copies the item's rows with their 4-row halos
+// from the correction (in L2) into shared memory in 16-byte pieces, updates
+// the phase's points level by level there, and writes each new value to
+// shared memory and to the correction.  Points and their (residual,
+// omega/lhs) pairs are read in st_pts order, one coalesced 8-byte load per
+// point and sweep.  Same-colour stencil neighbours never lie in different
+// tiles, so an item's halo rows hold no value that changes in the phase.
+__global__ void __launch_bounds__(kStagedThreads) k_mcsor_f32s(GridDev g, const __grid_constant__ JobTable jobs,
+                                                               int njobs, int nsweeps, int G, BarrierDev bar,
+                                                               unsigned nblocks) {
+  extern __shared__ __align__(16) float sband[];
+  const int nrun = (g.ntiles + G - 1) / G;
+  const int nitems = njobs * nrun;
+  const int n8 = g.n8;
   CoefF cf;
   for (int k = 0; k < 4; ++k) {
     cf.dmu1[k] = g.dmu1f[k];
@@ -328,24 +343,35 @@ __global__ void __launch_bounds__(kThreads) k_mcsor_f32(GridDev g, const __grid_
   for (int s = 0; s < nsweeps; ++s) {
     for (int c = 0; c < 5; ++c) {
       for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
-        const int jb = item / g.ntiles, t = item - jb * g.ntiles;
+        const int jb = item / nrun, t0 = (item - jb * nrun) * G;
+        const int t1 = (t0 + G < g.ntiles) ? t0 + G : g.ntiles;
         const JobDev &J = jobs.j[jb];
         float *e = J.e32;
         if (c == 0 && s > 0) {
-          tile_boundary<float>(g, e, t, J.isym);
+          for (int t = t0; t < t1; ++t) tile_boundary<float>(g, e, t, J.isym);
           __syncthreads();
         }
+        // rows [row0 - 4, row1 + 4) as whole 16-byte pieces: piece f holds
+        // ext indices 4f..4f+3, stored at sband[4 (f - f0)]
+        const int f0 = ((g.tile_row0[t0] - 4) * n8) >> 2, f1 = ((g.tile_row1[t1 - 1] + 4) * n8 + 3) >> 2;
+        const float4 *src = reinterpret_cast<const float4 *>(e);
+        float4 *dst = reinterpret_cast<float4 *>(sband);
+        for (int f = f0 + int(threadIdx.x); f < f1; f += blockDim.x) dst[f - f0] = __ldcg(src + f);
+        __syncthreads();
+        const float *sb = sband - 4 * f0;  // indexed by ext index
         const float omega1 = J.omega1f;
         const float *bt = (J.kind >= 1) ? g.bpot_mu32 : g.borb_mu32;
         for (int l = 0; l < g.nlev; ++l) {
-          const int o = (t * 5 + c) * g.nlev + l;
-          const int b0 = g.off[o], b1 = g.off[o + 1];
+          const int *so = g.st_off + (c * g.nlev + l) * (g.ntiles + 1);
+          const int b0 = so[t0], b1 = so[t1];
           if (b0 == b1) continue;
-          for (int k = b0 + threadIdx.x; k < b1; k += blockDim.x) {
-            const int ij = g.pts[k];
-            const int row = ij / g.n8, col = ij - row * g.n8;
-            const int mu = row - 4, nu = col - 4, ik = mu * g.nni + nu;
-            relax_f32(e, ij, g.n8, cf, bt[mu], g.d_nu32[nu], J.w32[ik], J.r32[ik], omega1);
+          for (int k = b0 + int(threadIdx.x); k < b1; k += blockDim.x) {
+            const int rc = g.st_pts[k];
+            const int row = rc >> 16, col = rc & 0xffff, ij = row * n8 + col;
+            const float2 rw = __ldg(J.rw + k);
+            const float v = relax_f32(sb, ij, n8, cf, bt[row - 4], g.d_nu32[col - 4], rw.y, rw.x, omega1);
+            sband[ij - 4 * f0] = v;
+            e[ij] = v;
           }
           __syncthreads();
         }
@@ -356,8 +382,9 @@ __global__ void __launch_bounds__(kThreads) k_mcsor_f32(GridDev g, const __grid_
     }
   }
   for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
-    const int jb = item / g.ntiles, t = item - jb * g.ntiles;
-    tile_boundary<float>(g, jobs.j[jb].e32, t, jobs.j[jb].isym);
+    const int jb = item / nrun, t0 = (item - jb * nrun) * G;
+    const int t1 = (t0 + G < g.ntiles) ? t0 + G : g.ntiles;
+    for (int t = t0; t < t1; ++t) tile_boundary<float>(g, jobs.j[jb].e32, t, jobs.j[jb].isym);
     __syncthreads();
   }
 }
@@ -764,7 +791,10 @@ __device__ __forceinline__ double ghost_read(const GridDev &g, const double *u, 
 // Mixed form residual r = rhs - A u in FP64 over the interior, stored as
 // FP32 with omega / lhs; the stencil uses the grid's separable weights (one
 // FMA per neighbour) and reads the ghost cells as mirrored interior values,
-// so u needs no ghost refresh first.
+// so u needs no ghost refresh first.  kPacked: the points are taken in
+// st_pts order and stored as (r, w) pairs in that order (staged sweep);
+// otherwise r32 / w32 are plain nni x nmu arrays (cluster sweep).
+template <bool kPacked>
 __global__ void k_residual(GridDev g, const __grid_constant__ JobTable jobs, int zero_e) {
   const JobDev &J = jobs.j[blockIdx.y];
   const int nint = (g.nni - 2) * (g.nmu - 5);
@@ -773,7 +803,15 @@ __global__ void k_residual(GridDev g, const __grid_constant__ JobTable jobs, int
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.next; k += gridDim.x * blockDim.x) J.e32[k] = 0.0f;
   const double *cmu = (J.kind == 0) ? g.cmu_orb : g.cmu_pot;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nint; k += gridDim.x * blockDim.x) {
-    const int mu = 1 + k / (g.nni - 2), nu = 1 + k % (g.nni - 2);
+    int mu, nu;
+    if (kPacked) {
+      const int rc = g.st_pts[k];
+      mu = (rc >> 16) - 4;
+      nu = (rc & 0xffff) - 4;
+    } else {
+      mu = 1 + k / (g.nni - 2);
+      nu = 1 + k % (g.nni - 2);
+    }
     const int ik = mu * g.nni + nu, ij = (mu + 4) * n8 + nu + 4;
     const double *u = J.u;
     double rhs, lhs;
@@ -808,8 +846,12 @@ __global__ void k_residual(GridDev g, const __grid_constant__ JobTable jobs, int
         cc = fma(cn[4 + q], ghost_read(g, u, row, col + d, J.isym), cc);
       }
     }
-    J.r32[ik] = narrow_f64(rhs - cc);
-    J.w32[ik] = J.omegaf / narrow_f64(lhs);
+    if (kPacked) {
+      J.rw[k] = make_float2(narrow_f64(rhs - cc), J.omegaf / narrow_f64(lhs));
+    } else {
+      J.r32[ik] = narrow_f64(rhs - cc);
+      J.w32[ik] = J.omegaf / narrow_f64(lhs);
+    }
   }
 }
 
@@ -1493,6 +1535,47 @@ static bool cluster_usable(x2g_ctx *ctx, const GridDev &g) {
   return ctx->cluster_ok != 0;
 }
 
+// Launch shape of the staged FP32 sweep for a batch of njobs: G tiles per
+// work item (larger runs re-read fewer halo rows, smaller ones give more
+// items to a batch of few jobs), the shared memory of the item's rows and
+// halos, and as many blocks as fit the device at once (cooperative launch).
+// The function's shared memory cap is raised once to the device's opt-in
+// maximum, as for the cluster kernel.
+static int staged_shape(x2g_ctx *ctx, const GridDev &g, int njobs, int *G, size_t *smem, int *nblocks) {
+  int want = (njobs * g.ntiles) / (2 * ctx->num_sms);
+  want = want < 1 ? 1 : (want > 4 ? 4 : want);
+  *G = want;
+  *smem = (size_t(g.st_rows[want]) * g.n8 + 8) * sizeof(float);
+  *smem = (*smem + 15) / 16 * 16;
+  if (!ctx->staged_attr) {
+    // the cap counts dynamic bytes only: the opt-in maximum less the
+    // kernel's static shared memory (the grid barrier's flag)
+    int optin = 0;
+    cudaFuncAttributes fa{};
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, (const void *)k_mcsor_f32s) != cudaSuccess ||
+        cudaFuncSetAttribute((const void *)k_mcsor_f32s, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             optin - int(fa.sharedSizeBytes)) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return set_status(X2G_ERR_CUDA, "staged sweep attributes could not be set");
+    }
+    ctx->staged_attr = optin - int(fa.sharedSizeBytes);
+  }
+  if (*smem > size_t(ctx->staged_attr)) return set_status(X2G_ERR_ARG, "grid rows too wide for the staged sweep");
+  if (ctx->staged_key != long(*smem)) {
+    int per_sm = 0;
+    cudaError_t err =
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k_mcsor_f32s, kStagedThreads, *smem);
+    if (err != cudaSuccess) return cuda_status(err, "occupancy query");
+    if (per_sm < 1) return set_status(X2G_ERR_CUDA, "staged sweep does not fit an SM");
+    ctx->staged_key = long(*smem);
+    ctx->staged_blocks = per_sm * ctx->num_sms;
+  }
+  const int nrun = (g.ntiles + want - 1) / want, nitems = njobs * nrun;
+  *nblocks = nitems < ctx->staged_blocks ? nitems : ctx->staged_blocks;
+  return X2G_OK;
+}
+
 // One launch batch (at most kParamJobs jobs) of launch_relax.
 static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, int nsweeps, bool mixed,
                        bool on_chip) {
@@ -1501,7 +1584,10 @@ static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, 
   const double points = double(njobs) * double(g.nni - 2) * double(g.nmu - 5) * double(nsweeps);
   if (mixed) {
     dim3 gr(grid_blocks((g.nni - 2) * (g.nmu - 5)), njobs);
-    k_residual<<<gr, kThreads, 0, ctx->stream>>>(g, jt, on_chip ? 0 : 1);
+    if (on_chip)
+      k_residual<false><<<gr, kThreads, 0, ctx->stream>>>(g, jt, 0);
+    else
+      k_residual<true><<<gr, kThreads, 0, ctx->stream>>>(g, jt, 1);
     ctx->launches += 1;
   }
   if (ctx->profiling) {
@@ -1540,23 +1626,32 @@ static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, 
     err = cudaMemsetAsync(ctx->bar, 0, 4 * sizeof(unsigned), ctx->stream);
     if (err != cudaSuccess) return cuda_status(err, "barrier reset");
     BarrierDev bar{ctx->bar, ctx->bar + 1, reinterpret_cast<int *>(ctx->bar + 2)};
-    static int max_f64 = -1, max_f32 = -1;
-    int *pmax = mixed ? &max_f32 : &max_f64;
-    if (*pmax < 0) {
-      int per_sm = 0;
-      err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &per_sm, mixed ? (const void *)k_mcsor_f32 : (const void *)k_mcsor_f64, kThreads, 0);
-      if (err != cudaSuccess) return cuda_status(err, "occupancy query");
-      *pmax = per_sm * ctx->num_sms;
-    }
-    const int nitems = njobs * g.ntiles;
-    unsigned nblocks = unsigned(nitems < *pmax ? nitems : *pmax);
-    if (nblocks < 1) nblocks = 1;
     int nj = njobs, ns = nsweeps;
     GridDev gd = g;
-    void *args[] = {&gd, &jt, &nj, &ns, &bar, &nblocks};
-    err = cudaLaunchCooperativeKernel(mixed ? (const void *)k_mcsor_f32 : (const void *)k_mcsor_f64, dim3(nblocks),
-                                      dim3(kThreads), args, 0, ctx->stream);
+    if (mixed) {
+      int G = 1, nblocks = 0;
+      size_t smem = 0;
+      int rc = staged_shape(ctx, g, njobs, &G, &smem, &nblocks);
+      if (rc) return rc;
+      unsigned nb = unsigned(nblocks);
+      void *args[] = {&gd, &jt, &nj, &ns, &G, &bar, &nb};
+      err = cudaLaunchCooperativeKernel((const void *)k_mcsor_f32s, dim3(nb), dim3(kStagedThreads), args, smem,
+                                        ctx->stream);
+    } else {
+      static int max_f64 = -1;
+      if (max_f64 < 0) {
+        int per_sm = 0;
+        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k_mcsor_f64, kThreads, 0);
+        if (err != cudaSuccess) return cuda_status(err, "occupancy query");
+        max_f64 = per_sm * ctx->num_sms;
+      }
+      const int nitems = njobs * g.ntiles;
+      unsigned nblocks = unsigned(nitems < max_f64 ? nitems : max_f64);
+      if (nblocks < 1) nblocks = 1;
+      void *args[] = {&gd, &jt, &nj, &ns, &bar, &nblocks};
+      err = cudaLaunchCooperativeKernel((const void *)k_mcsor_f64, dim3(nblocks), dim3(kThreads), args, 0,
+                                        ctx->stream);
+    }
     if (err != cudaSuccess) return cuda_status(err, "cooperative MCSOR launch");
     ctx->launches += 1;
     if (ctx->profiling) {
@@ -1581,12 +1676,30 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
   const bool on_chip = mixed && cluster_usable(ctx, g);
   // per-job scratch: FP64 rhs of potentials, or the mixed form's FP32
   // correction, residual and omega/lhs
-  const size_t per_job = mixed ? (size_t(g.next) * sizeof(float) + 2 * size_t(g.mxsize) * sizeof(float) + 256)
-                               : (size_t(g.mxsize) * sizeof(double) + 256);
+  const size_t per_job =
+      (mixed ? (size_t(g.next) * sizeof(float) + 2 * size_t(g.mxsize) * sizeof(float) + 256)
+             : (size_t(g.mxsize) * sizeof(double) + 256)) / 256 * 256 + 256;
   char *scratch = static_cast<char *>(ctx_workspace(ctx, per_job * njobs + 256));
   if (!scratch) return set_status(X2G_ERR_ALLOC, "workspace allocation failed");
-  for (int b0 = 0; b0 < njobs; b0 += kParamJobs) {
-    const int nb = (njobs - b0 < kParamJobs) ? njobs - b0 : kParamJobs;
+  // the staged sweep takes as many jobs per launch as keep their corrections
+  // and (residual, omega/lhs) pairs within 3/4 of L2, so that the five colour
+  // phases of every sweep re-read them from L2 rather than HBM
+  int per_launch = kParamJobs;
+  if (mixed && !on_chip) {
+    if (ctx->l2_bytes == 0) {
+      int l2 = 0;
+      if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, ctx->device) != cudaSuccess || l2 <= 0) {
+        (void)cudaGetLastError();
+        l2 = 64 << 20;
+      }
+      ctx->l2_bytes = size_t(l2);
+    }
+    const size_t live = size_t(g.next) * sizeof(float) + size_t(g.nni - 2) * size_t(g.nmu - 5) * sizeof(float2);
+    const size_t fit = ctx->l2_bytes / 4 * 3 / live;
+    per_launch = fit < 1 ? 1 : (fit > size_t(kParamJobs) ? kParamJobs : int(fit));
+  }
+  for (int b0 = 0; b0 < njobs; b0 += per_launch) {
+    const int nb = (njobs - b0 < per_launch) ? njobs - b0 : per_launch;
     JobTable jt{};
     for (int i = 0; i < nb; ++i) {
       JobDev &d = jt.j[i];
@@ -1596,6 +1709,7 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
         d.e32 = reinterpret_cast<float *>(p);
         d.r32 = reinterpret_cast<float *>(p + (size_t(g.next) * sizeof(float) + 127) / 128 * 128);
         d.w32 = d.r32 + g.mxsize;
+        d.rw = reinterpret_cast<float2 *>(d.r32);  // staged sweep: pairs over r32 and w32
       } else {
         d.rhs_buf = reinterpret_cast<double *>(p);
       }

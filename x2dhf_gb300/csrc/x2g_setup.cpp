@@ -276,6 +276,27 @@ std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf
     int t = band_of(g.order[p] / g.n8);
     g.pts[fill[(t * 5 + p % 5) * g.nlev + lev[p]]++] = g.order[p];
   }
+  g.st_pts.clear();
+  g.st_pts.reserve(g.pts.size());
+  g.st_off.assign(size_t(5) * g.nlev * (g.ntiles + 1), 0);
+  for (int c = 0; c < 5; ++c)
+    for (int l = 0; l < g.nlev; ++l) {
+      int *so = &g.st_off[size_t(c * g.nlev + l) * (g.ntiles + 1)];
+      for (int t = 0; t < g.ntiles; ++t) {
+        so[t] = int(g.st_pts.size());
+        const int o = (t * 5 + c) * g.nlev + l;
+        for (int k = g.off[o]; k < g.off[o + 1]; ++k) g.st_pts.push_back(((g.pts[k] / g.n8) << 16) | (g.pts[k] % g.n8));
+      }
+      so[g.ntiles] = int(g.st_pts.size());
+    }
+  for (int G = 1; G <= 4; ++G) {
+    int most = 0;
+    for (int t0 = 0; t0 < g.ntiles; t0 += G) {
+      const int t1 = std::min(t0 + G, g.ntiles);
+      most = std::max(most, g.tile_row1[t1 - 1] - g.tile_row0[t0]);
+    }
+    g.st_rows[G] = most + 8;
+  }
   g.pts_rc.resize(g.pts.size());
   for (size_t k = 0; k < g.pts.size(); ++k) g.pts_rc[k] = ((g.pts[k] / g.n8) << 16) | (g.pts[k] % g.n8);
   // cluster plan for the on-chip FP32 sweep: contiguous tile ranges, ~30
