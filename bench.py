@@ -233,6 +233,8 @@ def run_gpu(args):
             import torch.distributed as dist
             dist.barrier()
 
+    copied = [0, 0, 0]  # host-to-device bytes, device-to-host bytes, timed e2e steps
+
     def timed_solves(prec, k, warm, e2e=False):
         lat, res_last, iters = [], None, []
         for step in range(warm + k):
@@ -243,6 +245,7 @@ def run_gpu(args):
             barrier()
             ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             t0 = time.perf_counter()
+            b0 = ctx.transfer_bytes()
             ev0.record(stream)
             if e2e:
                 case = xg.parse_deck(deck, precision=prec)
@@ -258,6 +261,11 @@ def run_gpu(args):
             if step >= warm:
                 lat.append(max(dev, wall) if e2e else dev)
                 iters.append(res.iterations)
+                if e2e:
+                    b1 = ctx.transfer_bytes()
+                    copied[0] += b1[0] - b0[0]
+                    copied[1] += b1[1] - b0[1]
+                    copied[2] += 1
             res_last = res
             scf.close()
         return lat, res_last, iters
@@ -304,8 +312,10 @@ def run_gpu(args):
     on_chip = xg.host_cluster_plan(c.nnu, c.nmu)[0] > 0
     mx_sorted = sorted(latmx)
     p99 = mx_sorted[min(len(mx_sorted) - 1, int(round(0.99 * (len(mx_sorted) - 1))))]
-    h2d = (c.norb * 2 + 16) * (c.nnu + 8) * (c.nmu + 8) * 8  # orbitals + potentials of the initial guess
-    d2h = c.norb * c.nnu * c.nmu * 8
+    # bytes the library copied per timed e2e step (grid tables up; per-iteration
+    # scalars and the orbitals down), from its own transfer counters
+    h2d = copied[0] // max(1, copied[2])
+    d2h = copied[1] // max(1, copied[2])
     pts_per_launch = ptsmx / nmx if nmx else None
     traffic = CLUSTER_DRAM_BYTES_PER_PT * pts_per_launch if (pts_per_launch and on_chip) else None
     out = {
@@ -342,9 +352,9 @@ def run_gpu(args):
             "bound": "hbm",
             "kernel": ("k_mixed_cluster (mixed-form FP32 correction sweeps, one 16-CTA cluster per relaxation job, "
                        "band resident in shared memory)" if on_chip else
-                       "k_mcsor_f32s (mixed-form FP32 correction sweeps, persistent grid-barrier kernel staging "
-                       "each work item's rows in shared memory: the grid's bands do not fit one cluster's shared "
-                       "memory)"),
+                       "k_mcsor_f32p (mixed-form FP32 correction sweeps, persistent-band cooperative kernel: "
+                       "every block keeps one band of one job in shared memory for the whole launch, halos "
+                       "exchanged through L2; the grid's bands do not fit one cluster's shared memory)"),
             "achieved": sweep_gbs_mx, "peak": hbm, "unit": "GB/s",
             "frac": (sweep_gbs_mx / hbm) if sweep_gbs_mx else None, "traffic": traffic,
             "peak_kind": peak_kind,
@@ -352,11 +362,12 @@ def run_gpu(args):
             "note": ("achieved = 16 algorithmic B per point-update / launch time; the correction lives in shared "
                      "memory during the sweeps, so DRAM traffic is far below it and the launch is bound by the "
                      "colour-phase latency (cluster barrier + shared-memory pipe), not by HBM" if on_chip else
-                     "achieved = 16 algorithmic B per point-update / launch time; every colour phase copies each "
-                     "work item's rows with 4-row halos from L2 into shared memory and streams the item's "
-                     "(residual, omega/lhs) pairs once per sweep; a launch takes only as many jobs as keep their "
-                     "corrections and pairs within 3/4 of L2, so DRAM traffic stays below the algorithmic bytes and "
-                     "the launch is bound by phase latency (grid barrier, staging, level chain), not by HBM"),
+                     "achieved = 16 algorithmic B per point-update / launch time; the correction stays in shared "
+                     "memory for the whole launch (each colour phase reloads only the 4-row halos from L2 and "
+                     "writes back only the points within 4 rows of a shared band edge) and the (residual, "
+                     "omega/lhs) pairs stream once per sweep, so DRAM traffic stays far below the algorithmic "
+                     "bytes and the launch is bound by phase latency (grid barrier, halo round trip, level chain), "
+                     "not by HBM"),
             "sweep_ms_total": msmx, "sweep_launches": nmx, "point_updates": ptsmx,
             "point_updates_per_launch": pts_per_launch,
             "fp64_kernel": {"kernel": "k_mcsor_f64", "achieved_gbs": sweep_gbs_64,

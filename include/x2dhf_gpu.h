@@ -268,6 +268,10 @@ int x2g_scf_nrecords(x2g_scf *scf);
 int x2g_scf_record(x2g_scf *scf, int i, int *iscf, int *iorb, double *ee, double *dee, double *dnorm);
 /* Device launches of this library's kernels so far on the scf's context. */
 long x2g_kernel_launches(x2g_ctx *ctx);
+/* Host-to-device and device-to-host bytes the library has copied so far on
+ * the context (grid tables, function uploads and readbacks, per-iteration
+ * scalars, error words). */
+int x2g_transfer_bytes(x2g_ctx *ctx, long long *h2d, long long *d2h);
 
 /* ------------------------------------------------------------------ */
 /* reference-named entry points (link-compatible with src/c/*.c)       */

@@ -71,7 +71,7 @@ EXPORTS = [
     "x2g_quadrature", "x2g_case_defaults", "x2g_scf_create", "x2g_scf_destroy", "x2g_scf_run",
     "x2g_scf_get_orbital", "x2g_scf_get_coulomb", "x2g_scf_nrecords", "x2g_scf_record",
     "x2g_scf_set_function", "x2g_scf_get_function", "x2g_scf_set_start_values", "x2g_scf_get_start_values",
-    "x2g_kernel_launches", "mcsor_pthread_", "mcsor_tpool_", "coulExch_pthread_", "coulExch_tpool_",
+    "x2g_kernel_launches", "x2g_transfer_bytes", "mcsor_pthread_", "mcsor_tpool_", "coulExch_pthread_", "coulExch_tpool_",
     "tpoolStop4mcsor_", "tpoolStop4pots_", "x2g_host_table", "x2g_host_schedule", "x2g_profile",
     "x2g_relax_noalloc", "x2g_host_cluster_plan", "x2g_set_mixed_on_chip", "x2g_host_cluster_chunks",
     "x2g_convert_selftest",
@@ -133,6 +133,7 @@ def lib():
     L.x2g_set_mixed_on_chip.argtypes = [P, I]
     L.x2g_kernel_launches.restype = C.c_long
     L.x2g_kernel_launches.argtypes = [P]
+    L.x2g_transfer_bytes.argtypes = [P, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
     _lib = L
     return L
 
@@ -352,6 +353,12 @@ class Context:
     @property
     def launches(self):
         return self.L.x2g_kernel_launches(self.h)
+
+    def transfer_bytes(self):
+        """(host-to-device, device-to-host) bytes the library has copied on this context."""
+        a, b = C.c_longlong(), C.c_longlong()
+        _check(self.L.x2g_transfer_bytes(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def set_mixed_on_chip(self, on):
         _check(self.L.x2g_set_mixed_on_chip(self.h, 1 if on else 0))

@@ -80,8 +80,8 @@ int x2g_create(x2g_ctx **out, int device) {
     delete c;
     return cuda_status(e, "cudaStreamCreate");
   }
-  if ((e = cudaMalloc(&c->bar, 4 * sizeof(unsigned))) != cudaSuccess ||
-      (e = cudaMemset(c->bar, 0, 4 * sizeof(unsigned))) != cudaSuccess) {
+  if ((e = cudaMalloc(&c->bar, kBarWords * sizeof(unsigned))) != cudaSuccess ||
+      (e = cudaMemset(c->bar, 0, kBarWords * sizeof(unsigned))) != cudaSuccess) {
     cudaStreamDestroy(c->stream);
     delete c;
     return cuda_status(e, "barrier allocation");
@@ -134,8 +134,9 @@ int x2g_synchronize(x2g_ctx *c) {
   int err = 0;
   e = cudaMemcpy(&err, c->bar + 2, sizeof(int), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_status(e, "error word readback");
+  count_copy(c, 0, sizeof(int));
   if (err) {
-    cudaMemset(c->bar, 0, 4 * sizeof(unsigned));
+    cudaMemset(c->bar, 0, kBarWords * sizeof(unsigned));
     return set_status(err, "device-side barrier wait timed out (kernel returned early)");
   }
   return X2G_OK;
@@ -161,6 +162,13 @@ int x2g_profile(x2g_ctx *c, int enable, int precision, double *ms, double *point
 }
 
 long x2g_kernel_launches(x2g_ctx *c) { return c ? c->launches : 0; }
+
+int x2g_transfer_bytes(x2g_ctx *c, long long *h2d, long long *d2h) {
+  if (!c || !h2d || !d2h) return set_status(X2G_ERR_ARG, "null argument");
+  *h2d = c->h2d_bytes;
+  *d2h = c->d2h_bytes;
+  return X2G_OK;
+}
 
 int x2g_convert_selftest(x2g_ctx *c, long n, unsigned long long seed, unsigned long long *mismatches) {
   if (!c || !mismatches || n < 0) return set_status(X2G_ERR_ARG, "bad argument");
@@ -209,6 +217,7 @@ static int upload(x2g_grid *gr, const void *src, size_t bytes, const void **dst)
   gr->allocs.push_back(p);
   e = cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_status(e, "grid table upload");
+  count_copy(gr->ctx, bytes, 0);
   *dst = p;
   return X2G_OK;
 }
@@ -301,7 +310,7 @@ int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, doubl
   UP(h.pts_rc, pts_rc);
   UP(h.st_pts, st_pts);
   UP(h.st_off, st_off);
-  for (int k = 0; k < 5; ++k) d.st_rows[k] = h.st_rows[k];
+  for (int k = 0; k <= HostGrid::kStagedRuns; ++k) d.st_rows[k] = h.st_rows[k];
   d.cl_size = h.cl_size;
   d.cl_maxrows = h.cl_maxrows;
   d.cl_maxchunks = h.cl_maxchunks;
@@ -422,6 +431,7 @@ int x2g_mcsor_host(x2g_ctx *ctx, x2g_grid *grid, int isym, int kind, double omeg
   cudaMemcpyAsync(du, wk2, eb, cudaMemcpyHostToDevice, ctx->stream);
   cudaMemcpyAsync(dl, lhs, pb, cudaMemcpyHostToDevice, ctx->stream);
   cudaMemcpyAsync(dr, rhs, pb, cudaMemcpyHostToDevice, ctx->stream);
+  count_copy(ctx, eb + 2 * pb, eb);
   x2g_job j{};
   j.u = du;
   j.lhs = dl;
@@ -444,6 +454,7 @@ int x2g_quadrature(x2g_ctx *ctx, x2g_grid *grid, int which, const double *a, con
   launch_triples(ctx, grid->d, &it, 1, dout);
   cudaError_t e = cudaMemcpyAsync(ctx->host_red, dout, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "quadrature readback");
+  count_copy(ctx, 0, sizeof(double));
   int s = x2g_synchronize(ctx);
   if (s != X2G_OK) return s;
   *out = ctx->host_red[0];

@@ -100,6 +100,7 @@ apply_common : {
   cudaMemcpy(const_cast<double *>(d.borb_mu), borb.data(), nmu * sizeof(double), cudaMemcpyHostToDevice);
   cudaMemcpy(const_cast<double *>(d.bpot_mu), bpot.data(), nmu * sizeof(double), cudaMemcpyHostToDevice);
   cudaMemcpy(const_cast<double *>(d.d_nu), dnu.data(), nni * sizeof(double), cudaMemcpyHostToDevice);
+  count_copy(g_ctx, (2 * size_t(nmu) + nni) * sizeof(double), 0);
 }
   return X2G_OK;
 }
@@ -156,6 +157,7 @@ void coulexch_common() {
     std::memcpy(funh, excp + ibexc - 1, mx * sizeof(double));
     double *base = buf + per * k;
     cudaMemcpyAsync(base + g.next, h.data(), 3 * size_t(mx) * sizeof(double), cudaMemcpyHostToDevice, g_ctx->stream);
+    count_copy(g_ctx, 3 * size_t(mx) * sizeof(double), 0);
     launch_putin(g_ctx, g, isym, base + g.next + 2 * size_t(mx), base);
     cudaStreamSynchronize(g_ctx->stream);
     x2g_job &j = jobs[k];
@@ -175,6 +177,7 @@ void coulexch_common() {
     launch_putout(g_ctx, g, base, base + g.next + 2 * size_t(mx));
     cudaMemcpyAsync(out.data(), base + g.next + 2 * size_t(mx), mx * sizeof(double), cudaMemcpyDeviceToHost,
                     g_ctx->stream);
+    count_copy(g_ctx, 0, mx * sizeof(double));
     if (x2g_synchronize(g_ctx)) break;
     std::memcpy(excp + ibexc - 1, out.data(), mx * sizeof(double));
   }

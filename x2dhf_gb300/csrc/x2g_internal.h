@@ -14,6 +14,10 @@ namespace x2g {
 constexpr double kPrecis = 2.220446049250313080847263336181640625e-16;  // epsilon(1d0), initVariables.F90:397
 constexpr double kPi = 3.14159265358979323846264338327950;                // params.F90:94
 constexpr int kMaxLevels = 8;
+// device words of a context's barrier state: [0] arrivals, [1] generation,
+// [2] error word, [3] reduction ticket, then the staged sweep's arrival
+// counters at words 32, 64, ..., 256 (one 128-byte line each)
+constexpr int kBarWords = 288;
 
 // ----------------------------------------------------------------------
 // Host-side grid: every table the relaxation path reads, built with the
@@ -57,9 +61,10 @@ struct HostGrid {
   // colour and level in any run of consecutive tiles are one contiguous
   // range; st_off[(c * nlev + l) * (ntiles + 1) + t] is the start of tile t.
   // st_rows[G] = most rows of any run of G consecutive tiles (G = 1..4), plus
-  // the 4-row halos on both sides
+  // the 4-row halos on both sides (G = 1..kStagedRuns)
+  static constexpr int kStagedRuns = 16;
   std::vector<int> st_pts, st_off;
-  int st_rows[5] = {0, 0, 0, 0, 0};
+  int st_rows[kStagedRuns + 1] = {};
 };
 
 std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf, double z1, double z2, int mpole);
@@ -79,7 +84,7 @@ struct GridDev {
   int cl_size, cl_maxrows, cl_maxchunks, cl_wa, cl_wb, cl_ws;
   const int *cl_tile0, *cl_row0, *cl_pts, *cl_off;
   const int *st_pts, *st_off;
-  int st_rows[5];
+  int st_rows[17];
   // FP32 copies of the coefficient tables for the mixed form
   const float *borb_mu32, *bpot_mu32, *d_nu32;
   // separable stencil weights of the mixed form's FP64 residual: for the
@@ -144,16 +149,17 @@ struct x2g_ctx {
   void *red = nullptr;  // reduction partials
   size_t red_bytes = 0;
   double *host_red = nullptr;  // pinned host buffer for small readbacks
+  long long h2d_bytes = 0, d2h_bytes = 0;  // host<->device bytes copied by the library
   long launches = 0;
   size_t cluster_smem_set = 0;  // dynamic shared memory granted to the cluster kernel
   int no_cluster = 0;           // 1: mixed form uses the grid-barrier FP32 kernel
   int cluster_nonportable = 0;  // cluster kernel allowed more than 8 CTAs
   long cluster_checked_key = -1;  // (shared bytes, cluster size) last checked
   int cluster_ok = 0;             // that cluster shape is schedulable here
-  int staged_attr = 0;            // shared memory cap granted to the staged sweep
-  long staged_key = -1;           // shared bytes of the last staged occupancy query
-  int staged_blocks = 0;          // co-resident staged blocks for that size
-  size_t l2_bytes = 0;            // device L2 size (0: not queried yet)
+  int staged_attr = 0;            // shared memory cap granted to the persistent-band sweep
+  long staged_key = -1;           // shared bytes of its last occupancy query
+  int staged_blocks = 0;          // co-resident blocks for that size
+  int staged_sm_smem = 0;         // shared memory per SM
   // optional per-launch timing of the sweep kernels (CUDA events on stream)
   int profiling = 0;
   struct Pending {
@@ -180,4 +186,10 @@ namespace x2g {
 int set_status(int code, const std::string &msg);
 int cuda_status(cudaError_t e, const char *where);
 void *ctx_workspace(x2g_ctx *ctx, size_t bytes);
+inline void count_copy(x2g_ctx *ctx, size_t h2d, size_t d2h) {
+  if (ctx) {
+    ctx->h2d_bytes += (long long)h2d;
+    ctx->d2h_bytes += (long long)d2h;
+  }
+}
 }  // namespace x2g

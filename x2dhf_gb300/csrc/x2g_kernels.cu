@@ -78,6 +78,57 @@ __device__ bool grid_barrier(const BarrierDev &b, unsigned nblocks) {
   return s_ok != 0;
 }
 
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid-wide barrier on monotonic arrival counts, spread over kArriveLanes
+// counters kArriveStride words apart (zeroed before the launch): block b
+// adds one to counter b % kArriveLanes, and the k-th barrier (k = 1, 2, ...)
+// is passed once every counter q holds k times the number of blocks with
+// residue q.  The release needs no reset and no second round trip; eight
+// lanes of warp 0 poll the eight counters.  Every wait is bounded as in
+// grid_barrier.
+constexpr int kArriveLanes = 8, kArriveStride = 32;
+__device__ bool grid_barrier_counted(const BarrierDev &b, unsigned *lanes, unsigned nblocks, unsigned k) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(lanes + (blockIdx.x % kArriveLanes) * kArriveStride, 1u);
+    }
+    int ok = 1;
+    const unsigned q = threadIdx.x;
+    if (q < kArriveLanes && q < nblocks) {
+      const unsigned target = k * ((nblocks - q + kArriveLanes - 1) / kArriveLanes);
+      const unsigned *cnt = lanes + q * kArriveStride;
+      volatile int *verr = b.err;
+      const unsigned long long t0 = globaltimer();
+      unsigned spins = 0;
+      while (ld_acquire(cnt) < target) {
+        if (*verr) {
+          ok = 0;
+          break;
+        }
+        if ((++spins & 255u) == 0 && globaltimer() - t0 > kBarrierTimeoutNs) {
+          atomicCAS(b.err, 0, X2G_ERR_TIMEOUT);
+          ok = 0;
+          break;
+        }
+        __nanosleep(20);
+      }
+      __threadfence();
+    }
+    ok = __all_sync(0xffffffffu, ok);
+    if (threadIdx.x == 0) s_ok = ok && (*(volatile int *)b.err == 0);
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
 // ----------------------------------------------------------------------
 // One point update, FP64, reference arithmetic order (sormcsor.F90:46-71).
 // ----------------------------------------------------------------------
@@ -317,22 +368,83 @@ __global__ void __launch_bounds__(kThreads) k_mcsor_f64(GridDev g, const __grid_
   }
 }
 
-// Staged persistent FP32 sweep for grids whose bands do not fit one cluster's
-// shared memory.  A work item is a run of G consecutive tiles of one job; in
-// every colour phase its block copies the item's rows with their 4-row halos
-// from the correction (in L2) into shared memory in 16-byte pieces, updates
-// the phase's points level by level there, and writes each new value to
-// shared memory and to the correction.  Points and their (residual,
-// omega/lhs) pairs are read in st_pts order, one coalesced 8-byte load per
-// point and sweep.  Same-colour stencil neighbours never lie in different
-// tiles, so an item's halo rows hold no value that changes in the phase.
-__global__ void __launch_bounds__(kStagedThreads) k_mcsor_f32s(GridDev g, const __grid_constant__ JobTable jobs,
-                                                               int njobs, int nsweeps, int G, BarrierDev bar,
-                                                               unsigned nblocks) {
+// Axis extrapolation of the correction (tile_boundary<float>) for tiles
+// [t0, t1) computed in the band sb held in shared memory (indexed by ext
+// index).
+__device__ void band_boundary(const GridDev &g, float *sb, int t0, int t1, bool even) {
+  const int n8 = g.n8, nni = g.nni;
+  const int nrow7 = (t0 == 0) ? nni - 2 : 0;
+  const int r0 = (t0 == 0) ? 5 : g.tile_row0[t0];
+  const int nside = 2 * (g.tile_row1[t1 - 1] - r0);
+  for (int k = threadIdx.x; k < nrow7 + nside; k += blockDim.x) {
+    int ij, st;
+    if (k < nrow7) {
+      ij = 4 * n8 + 5 + k;
+      st = n8;
+    } else {
+      const int q = k - nrow7, r = r0 + q / 2, side = q % 2;
+      ij = r * n8 + (side == 0 ? 4 : nni + 3);
+      st = (side == 0) ? 1 : -1;
+    }
+    float v = 0.0f;
+    if (even)
+      v = g.exevenf[0] * sb[ij + st] + g.exevenf[1] * sb[ij + 2 * st] + g.exevenf[2] * sb[ij + 3 * st] +
+          g.exevenf[3] * sb[ij + 4 * st] + g.exevenf[4] * sb[ij + 5 * st];
+    sb[ij] = v;
+  }
+  if (t0 == 0) {
+    __syncthreads();
+    if (threadIdx.x < 2) {
+      const int ij = 4 * n8 + (threadIdx.x == 0 ? 4 : nni + 3);
+      const int st = (threadIdx.x == 0) ? 1 : -1;
+      float v = 0.0f;
+      if (even)
+        v = g.exevenf[0] * sb[ij + st] + g.exevenf[1] * sb[ij + 2 * st] + g.exevenf[2] * sb[ij + 3 * st] +
+            g.exevenf[3] * sb[ij + 4 * st] + g.exevenf[4] * sb[ij + 5 * st];
+      sb[ij] = v;
+    }
+  }
+}
+
+// Shared memory of the band of a run of G tiles with its 4-row halos, as
+// whole 16-byte pieces.
+__host__ __device__ inline size_t band_smem_bytes(const GridDev &g, int G) {
+  return ((size_t(g.st_rows[G]) * g.n8 + 8) * sizeof(float) + 15) / 16 * 16;
+}
+
+// Persistent-band FP32 sweep for grids whose bands do not fit one cluster's
+// shared memory.  Block b owns, for the whole launch, one run of G
+// consecutive tiles of one job (rows [row0, row1)) and keeps the
+// correction on those rows, with 4-row halos, in shared memory, as whole
+// 16-byte pieces: piece f holds ext indices 4f..4f+3 at sband[4 (f - f0)].
+// Every colour phase refreshes the two halos from the correction in global
+// memory (L2), updates the phase's points level by level in shared memory,
+// and writes to global memory only the new values within 4 rows of a band
+// edge shared with another block, which are that block's halo; a grid
+// barrier on counted arrivals ends the phase.  The band goes back to global
+// memory after the last sweep.  Same-colour stencil neighbours never lie in
+// different tiles, so the values a phase changes in a neighbour's rows are
+// never read by this block in that phase, and a halo piece that reaches
+// into an own row covers only ghost columns (zero throughout).
+__global__ void __launch_bounds__(kStagedThreads) k_mcsor_f32p(GridDev g, const __grid_constant__ JobTable jobs,
+                                                               int nsweeps, int G, BarrierDev bar,
+                                                               unsigned *lanes) {
   extern __shared__ __align__(16) float sband[];
   const int nrun = (g.ntiles + G - 1) / G;
-  const int nitems = njobs * nrun;
-  const int n8 = g.n8;
+  const int jb = int(blockIdx.x) / nrun, t0 = (int(blockIdx.x) - jb * nrun) * G;
+  const int t1 = (t0 + G < g.ntiles) ? t0 + G : g.ntiles;
+  const JobDev &J = jobs.j[jb];
+  float *e = J.e32;
+  const int n8 = g.n8, nlev = g.nlev;
+  const int row0 = g.tile_row0[t0], row1 = g.tile_row1[t1 - 1];
+  const int f0 = ((row0 - 4) * n8) >> 2, f1 = ((row1 + 4) * n8 + 3) >> 2;
+  const int fa = (row0 * n8 + 3) >> 2, fb = (row1 * n8) >> 2;  // top halo [f0, fa), bottom [fb, f1)
+  const int edge_lo = (t0 > 0) ? row0 + 4 : row0, edge_hi = (t1 < g.ntiles) ? row1 - 4 : row1;
+  const float4 *src = reinterpret_cast<const float4 *>(e);
+  float4 *dst = reinterpret_cast<float4 *>(sband);
+  float *sb = sband - 4 * f0;  // indexed by ext index
+  const float omega1 = J.omega1f;
+  const float *bt = (J.kind >= 1) ? g.bpot_mu32 : g.borb_mu32;
   CoefF cf;
   for (int k = 0; k < 4; ++k) {
     cf.dmu1[k] = g.dmu1f[k];
@@ -340,53 +452,59 @@ __global__ void __launch_bounds__(kStagedThreads) k_mcsor_f32s(GridDev g, const 
     cf.dni1[k] = g.dni1f[k];
     cf.dni2[k] = g.dni2f[k];
   }
+  for (int f = f0 + int(threadIdx.x); f < f1; f += blockDim.x) dst[f - f0] = __ldcg(src + f);
+  __syncthreads();
+  unsigned nbar = 0;
   for (int s = 0; s < nsweeps; ++s) {
     for (int c = 0; c < 5; ++c) {
-      for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
-        const int jb = item / nrun, t0 = (item - jb * nrun) * G;
-        const int t1 = (t0 + G < g.ntiles) ? t0 + G : g.ntiles;
-        const JobDev &J = jobs.j[jb];
-        float *e = J.e32;
-        if (c == 0 && s > 0) {
-          for (int t = t0; t < t1; ++t) tile_boundary<float>(g, e, t, J.isym);
+      if (s > 0 || c > 0) {
+        for (int f = f0 + int(threadIdx.x); f < fa; f += blockDim.x) dst[f - f0] = __ldcg(src + f);
+        for (int f = fb + int(threadIdx.x); f < f1; f += blockDim.x) dst[f - f0] = __ldcg(src + f);
+        if (c == 0) {
           __syncthreads();
+          band_boundary(g, sb, t0, t1, J.isym == 1);
         }
-        // rows [row0 - 4, row1 + 4) as whole 16-byte pieces: piece f holds
-        // ext indices 4f..4f+3, stored at sband[4 (f - f0)]
-        const int f0 = ((g.tile_row0[t0] - 4) * n8) >> 2, f1 = ((g.tile_row1[t1 - 1] + 4) * n8 + 3) >> 2;
-        const float4 *src = reinterpret_cast<const float4 *>(e);
-        float4 *dst = reinterpret_cast<float4 *>(sband);
-        for (int f = f0 + int(threadIdx.x); f < f1; f += blockDim.x) dst[f - f0] = __ldcg(src + f);
         __syncthreads();
-        const float *sb = sband - 4 * f0;  // indexed by ext index
-        const float omega1 = J.omega1f;
-        const float *bt = (J.kind >= 1) ? g.bpot_mu32 : g.borb_mu32;
-        for (int l = 0; l < g.nlev; ++l) {
-          const int *so = g.st_off + (c * g.nlev + l) * (g.ntiles + 1);
-          const int b0 = so[t0], b1 = so[t1];
-          if (b0 == b1) continue;
-          for (int k = b0 + int(threadIdx.x); k < b1; k += blockDim.x) {
-            const int rc = g.st_pts[k];
-            const int row = rc >> 16, col = rc & 0xffff, ij = row * n8 + col;
-            const float2 rw = __ldg(J.rw + k);
-            const float v = relax_f32(sb, ij, n8, cf, bt[row - 4], g.d_nu32[col - 4], rw.y, rw.x, omega1);
-            sband[ij - 4 * f0] = v;
-            e[ij] = v;
+      }
+#pragma unroll 1
+      for (int l = 0; l < nlev; ++l) {
+        const int *so = g.st_off + (c * nlev + l) * (g.ntiles + 1);
+        const int b0 = so[t0], b1 = so[t1];
+        if (b0 == b1) continue;
+        // four points per thread and pass, their list entries loaded
+        // together (points of one colour and level are independent)
+        for (int k0 = b0 + int(threadIdx.x); k0 < b1; k0 += 4 * int(blockDim.x)) {
+          int rc[4];
+          float2 p[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int k = k0 + u * int(blockDim.x);
+            if (k < b1) {
+              rc[u] = __ldg(g.st_pts + k);
+              p[u] = __ldg(J.rw + k);
+            }
           }
-          __syncthreads();
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            if (k0 + u * int(blockDim.x) < b1) {
+              const int row = rc[u] >> 16, col = rc[u] & 0xffff, ij = row * n8 + col;
+              const float v =
+                  relax_f32(sb, ij, n8, cf, bt[row - 4], g.d_nu32[col - 4], p[u].y, p[u].x, omega1);
+              sb[ij] = v;
+              if (row < edge_lo || row >= edge_hi) e[ij] = v;
+            }
+          }
         }
+        __syncthreads();
       }
       if (!(s == nsweeps - 1 && c == 4)) {
-        if (!grid_barrier(bar, nblocks)) return;
+        if (!grid_barrier_counted(bar, lanes, gridDim.x, ++nbar)) return;
       }
     }
   }
-  for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
-    const int jb = item / nrun, t0 = (item - jb * nrun) * G;
-    const int t1 = (t0 + G < g.ntiles) ? t0 + G : g.ntiles;
-    for (int t = t0; t < t1; ++t) tile_boundary<float>(g, jobs.j[jb].e32, t, jobs.j[jb].isym);
-    __syncthreads();
-  }
+  band_boundary(g, sb, t0, t1, J.isym == 1);
+  __syncthreads();
+  for (int ij = row0 * n8 + int(threadIdx.x); ij < row1 * n8; ij += blockDim.x) e[ij] = sb[ij];
 }
 
 // ----------------------------------------------------------------------
@@ -1535,50 +1653,64 @@ static bool cluster_usable(x2g_ctx *ctx, const GridDev &g) {
   return ctx->cluster_ok != 0;
 }
 
-// Launch shape of the staged FP32 sweep for a batch of njobs: G tiles per
-// work item (larger runs re-read fewer halo rows, smaller ones give more
-// items to a batch of few jobs), the shared memory of the item's rows and
-// halos, and as many blocks as fit the device at once (cooperative launch).
-// The function's shared memory cap is raised once to the device's opt-in
-// maximum, as for the cluster kernel.
-static int staged_shape(x2g_ctx *ctx, const GridDev &g, int njobs, int *G, size_t *smem, int *nblocks) {
-  int want = (njobs * g.ntiles) / (2 * ctx->num_sms);
-  want = want < 1 ? 1 : (want > 4 ? 4 : want);
-  *G = want;
-  *smem = (size_t(g.st_rows[want]) * g.n8 + 8) * sizeof(float);
-  *smem = (*smem + 15) / 16 * 16;
+// Launch shape of the persistent-band sweep: the most jobs per launch (at
+// most `most`) and the shortest tile runs G for which every (job, run) gets
+// its own co-resident block (two 512-thread blocks fit an SM's registers;
+// shared memory per SM decides below that).  The function's shared memory
+// cap is raised once to the device's opt-in maximum, as for the cluster
+// kernel.
+static int persistent_shape(x2g_ctx *ctx, const GridDev &g, int most, int *nj, int *G, size_t *smem) {
   if (!ctx->staged_attr) {
     // the cap counts dynamic bytes only: the opt-in maximum less the
     // kernel's static shared memory (the grid barrier's flag)
     int optin = 0;
     cudaFuncAttributes fa{};
     if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device) != cudaSuccess ||
-        cudaFuncGetAttributes(&fa, (const void *)k_mcsor_f32s) != cudaSuccess ||
-        cudaFuncSetAttribute((const void *)k_mcsor_f32s, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncGetAttributes(&fa, (const void *)k_mcsor_f32p) != cudaSuccess ||
+        cudaFuncSetAttribute((const void *)k_mcsor_f32p, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              optin - int(fa.sharedSizeBytes)) != cudaSuccess) {
       (void)cudaGetLastError();
-      return set_status(X2G_ERR_CUDA, "staged sweep attributes could not be set");
+      return set_status(X2G_ERR_CUDA, "persistent sweep attributes could not be set");
     }
     ctx->staged_attr = optin - int(fa.sharedSizeBytes);
-  }
-  if (*smem > size_t(ctx->staged_attr)) return set_status(X2G_ERR_ARG, "grid rows too wide for the staged sweep");
-  if (ctx->staged_key != long(*smem)) {
     int per_sm = 0;
-    cudaError_t err =
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k_mcsor_f32s, kStagedThreads, *smem);
-    if (err != cudaSuccess) return cuda_status(err, "occupancy query");
-    if (per_sm < 1) return set_status(X2G_ERR_CUDA, "staged sweep does not fit an SM");
-    ctx->staged_key = long(*smem);
-    ctx->staged_blocks = per_sm * ctx->num_sms;
+    if (cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device) != cudaSuccess)
+      return set_status(X2G_ERR_CUDA, "device attribute query failed");
+    ctx->staged_sm_smem = per_sm;
   }
-  const int nrun = (g.ntiles + want - 1) / want, nitems = njobs * nrun;
-  *nblocks = nitems < ctx->staged_blocks ? nitems : ctx->staged_blocks;
-  return X2G_OK;
+  for (int n = most; n >= 1; --n)
+    for (int r = 1; r <= HostGrid::kStagedRuns; ++r) {
+      const size_t sm = band_smem_bytes(g, r);
+      if (sm > size_t(ctx->staged_attr)) break;
+      // two blocks per SM (1024 threads) hide more latency than one block
+      // with twice the band
+      int bpsm = int(size_t(ctx->staged_sm_smem) / (sm + 1024));
+      if (bpsm < 2) break;
+      bpsm = 2;
+      const int items = n * ((g.ntiles + r - 1) / r);
+      if (bpsm >= 1 && items <= bpsm * ctx->num_sms) {
+        // confirm with the occupancy calculator (once per shared size)
+        if (ctx->staged_key != long(sm)) {
+          int per = 0;
+          cudaError_t err =
+              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void *)k_mcsor_f32p, kStagedThreads, sm);
+          if (err != cudaSuccess) return cuda_status(err, "occupancy query");
+          ctx->staged_key = long(sm);
+          ctx->staged_blocks = per * ctx->num_sms;
+        }
+        if (items > ctx->staged_blocks) continue;
+        *nj = n;
+        *G = r;
+        *smem = sm;
+        return X2G_OK;
+      }
+    }
+  return set_status(X2G_ERR_ARG, "grid too large for the persistent FP32 sweep");
 }
 
 // One launch batch (at most kParamJobs jobs) of launch_relax.
 static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, int nsweeps, bool mixed,
-                       bool on_chip) {
+                       bool on_chip, int G, size_t smem) {
   cudaError_t err;
   x2g_ctx::Pending pe{};
   const double points = double(njobs) * double(g.nni - 2) * double(g.nmu - 5) * double(nsweeps);
@@ -1629,13 +1761,14 @@ static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, 
     int nj = njobs, ns = nsweeps;
     GridDev gd = g;
     if (mixed) {
-      int G = 1, nblocks = 0;
-      size_t smem = 0;
-      int rc = staged_shape(ctx, g, njobs, &G, &smem, &nblocks);
-      if (rc) return rc;
-      unsigned nb = unsigned(nblocks);
-      void *args[] = {&gd, &jt, &nj, &ns, &G, &bar, &nb};
-      err = cudaLaunchCooperativeKernel((const void *)k_mcsor_f32s, dim3(nb), dim3(kStagedThreads), args, smem,
+      // one block per (job, run of G tiles); arrival counters of
+      // grid_barrier_counted zeroed with the rest
+      err = cudaMemsetAsync(ctx->bar, 0, kBarWords * sizeof(unsigned), ctx->stream);
+      if (err != cudaSuccess) return cuda_status(err, "barrier reset");
+      unsigned *lanes = ctx->bar + kArriveStride;
+      const unsigned nb = unsigned(njobs * ((g.ntiles + G - 1) / G));
+      void *args[] = {&gd, &jt, &ns, &G, &bar, &lanes};
+      err = cudaLaunchCooperativeKernel((const void *)k_mcsor_f32p, dim3(nb), dim3(kStagedThreads), args, smem,
                                         ctx->stream);
     } else {
       static int max_f64 = -1;
@@ -1684,19 +1817,11 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
   // the staged sweep takes as many jobs per launch as keep their corrections
   // and (residual, omega/lhs) pairs within 3/4 of L2, so that the five colour
   // phases of every sweep re-read them from L2 rather than HBM
-  int per_launch = kParamJobs;
+  int per_launch = kParamJobs, G = 0;
+  size_t smem = 0;
   if (mixed && !on_chip) {
-    if (ctx->l2_bytes == 0) {
-      int l2 = 0;
-      if (cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, ctx->device) != cudaSuccess || l2 <= 0) {
-        (void)cudaGetLastError();
-        l2 = 64 << 20;
-      }
-      ctx->l2_bytes = size_t(l2);
-    }
-    const size_t live = size_t(g.next) * sizeof(float) + size_t(g.nni - 2) * size_t(g.nmu - 5) * sizeof(float2);
-    const size_t fit = ctx->l2_bytes / 4 * 3 / live;
-    per_launch = fit < 1 ? 1 : (fit > size_t(kParamJobs) ? kParamJobs : int(fit));
+    int rc = persistent_shape(ctx, g, njobs < kParamJobs ? njobs : kParamJobs, &per_launch, &G, &smem);
+    if (rc) return rc;
   }
   for (int b0 = 0; b0 < njobs; b0 += per_launch) {
     const int nb = (njobs - b0 < per_launch) ? njobs - b0 : per_launch;
@@ -1714,7 +1839,7 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
         d.rhs_buf = reinterpret_cast<double *>(p);
       }
     }
-    int rc = relax_batch(ctx, g, jt, nb, nsweeps, mixed, on_chip);
+    int rc = relax_batch(ctx, g, jt, nb, nsweeps, mixed, on_chip, G, smem);
     if (rc) return rc;
   }
   // barrier error word: checked by the caller at its next synchronisation

@@ -73,6 +73,7 @@ extern "C" int x2g_relax_noalloc(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jo
   int err = 0;
   e = cudaMemcpy(&err, static_cast<char *>(scratch) + 2 * sizeof(unsigned), sizeof(int), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_status(e, "scratch error word readback");
+  count_copy(ctx, 0, sizeof(int));
   if (err) return set_status(err, "device-side barrier wait timed out (kernel returned early)");
   return set_status(X2G_OK, "");
 }

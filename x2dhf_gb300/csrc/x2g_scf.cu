@@ -246,7 +246,8 @@ int upload_ext(x2g_scf *s, double *dst, const std::vector<double> &plain) {
   for (int i = 0; i < g.nmu; i++)
     for (int j = 0; j < g.nni; j++) ext[(i + 4) * g.n8 + j + 4] = plain[i * g.nni + j];
   cudaError_t e = cudaMemcpy(dst, ext.data(), ext.size() * sizeof(double), cudaMemcpyHostToDevice);
-  return e == cudaSuccess ? X2G_OK : cuda_status(e, "initial guess upload");
+  count_copy(s->ctx, ext.size() * sizeof(double), 0);
+  return e == cudaSuccess ? X2G_OK : cuda_status(e, "function upload");
 }
 
 int initial_guess(x2g_scf *s) {
@@ -526,6 +527,7 @@ int etotal(x2g_scf *s) {
   cudaMemcpyAsync(hp.data(), parts, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, s->ctx->stream);
   if (!items.empty())
     cudaMemcpyAsync(ho.data(), out, items.size() * sizeof(double), cudaMemcpyDeviceToHost, s->ctx->stream);
+  count_copy(s->ctx, 0, (hp.size() + items.size()) * sizeof(double));
   int rc = x2g_synchronize(s->ctx);
   if (rc) return rc;
   // spin-pair counts for closed shells (exchContribs.f90 excont/exint)
@@ -579,6 +581,7 @@ int read_scalars(x2g_scf *s) {
   cudaError_t e = cudaMemcpyAsync(s->hsc.data(), s->sc, size_t(x2g_scf::O_CM) * sizeof(double),
                                   cudaMemcpyDeviceToHost, s->ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "scalar readback");
+  count_copy(s->ctx, 0, size_t(x2g_scf::O_CM) * sizeof(double));
   int rc = x2g_synchronize(s->ctx);
   if (rc) return rc;
   for (int i = 1; i <= s->norb; i++) {
@@ -997,6 +1000,7 @@ int x2g_scf_get_orbital(x2g_scf *s, int iorb, double *host) {
   cudaError_t e = cudaMemcpyAsync(ext.data(), s->orb[iorb], ext.size() * sizeof(double), cudaMemcpyDeviceToHost,
                                   s->ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "orbital readback");
+  count_copy(s->ctx, 0, ext.size() * sizeof(double));
   int rc = x2g_synchronize(s->ctx);
   if (rc) return rc;
   for (int i = 0; i < g.nmu; i++)
@@ -1011,6 +1015,7 @@ int x2g_scf_get_coulomb(x2g_scf *s, int iorb, double *host) {
   cudaError_t e = cudaMemcpyAsync(ext.data(), s->coul[iorb], ext.size() * sizeof(double), cudaMemcpyDeviceToHost,
                                   s->ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "potential readback");
+  count_copy(s->ctx, 0, ext.size() * sizeof(double));
   int rc = x2g_synchronize(s->ctx);
   if (rc) return rc;
   for (int i = 0; i < g.nmu; i++)
@@ -1050,6 +1055,7 @@ int x2g_scf_get_function(x2g_scf *s, int kind, int i1, int i2, int which, double
   std::vector<double> ext(g.next);
   cudaError_t e = cudaMemcpyAsync(ext.data(), d, ext.size() * sizeof(double), cudaMemcpyDeviceToHost, s->ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "function readback");
+  count_copy(s->ctx, 0, ext.size() * sizeof(double));
   int rc = x2g_synchronize(s->ctx);
   if (rc) return rc;
   for (int i = 0; i < g.nmu; i++)
@@ -1080,6 +1086,7 @@ int x2g_scf_set_start_values(x2g_scf *s, const double *ee, const double *orbnorm
   for (int ipc = 1; ipc < s->nslots && size_t(ipc) <= kExcLen; ipc++)
     for (int k = 1; k <= 8; k++) h[x2g_scf::O_EX + 8 * size_t(ipc) + (k - 1)] = exc[(k - 1) * kExcLen + ipc - 1];
   e = cudaMemcpy(s->sc, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice);
+  count_copy(s->ctx, h.size() * sizeof(double), h.size() * sizeof(double));
   return e == cudaSuccess ? X2G_OK : cuda_status(e, "start values");
 }
 
@@ -1091,6 +1098,7 @@ int x2g_scf_get_start_values(x2g_scf *s, double *ee, double *orbnorm, double *cm
   std::vector<double> h(s->sc_count);
   cudaError_t e = cudaMemcpy(h.data(), s->sc, h.size() * sizeof(double), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_status(e, "start values");
+  count_copy(s->ctx, 0, h.size() * sizeof(double));
   const int norb = s->norb;
   std::fill(cmulti, cmulti + size_t(X2G_MAXORB) * 8, 0.0);
   std::fill(exc, exc + 8 * kExcLen, 0.0);

@@ -289,7 +289,7 @@ std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf
       }
       so[g.ntiles] = int(g.st_pts.size());
     }
-  for (int G = 1; G <= 4; ++G) {
+  for (int G = 1; G <= HostGrid::kStagedRuns; ++G) {
     int most = 0;
     for (int t0 = 0; t0 < g.ntiles; t0 += G) {
       const int t1 = std::min(t0 + G, g.ntiles);
