@@ -1475,37 +1475,40 @@ __global__ void k_triples(GridDev g, TripleList L, int n, double *partials, doub
   block_sum_finish<kMaxK>(v, partials, out, n, ticket);
 }
 
-// coulMom (scfUtils.F90:490-603)
-__global__ void k_coulmom(GridDev g, const double *psi, int homo, double *partials, double *out, unsigned *ticket) {
+// coulMom (scfUtils.F90:490-603) and exchMom (scfUtils.F90:615-844, with
+// the grid's weighted P_k^q r^k tables) of a batch of items (blockIdx.y =
+// item), each with its own kRedBlocks partial sums and ticket, so every
+// item's sum runs in a fixed order
+constexpr int kMomentItems = 64;
+struct MomentList {
+  MomentItem it[kMomentItems];
+};
+__global__ void k_moments(GridDev g, const __grid_constant__ MomentList L, int homo, double *partials,
+                          unsigned *tickets) {
+  const MomentItem &m = L.it[blockIdx.y];
   double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
-    const int mu = k / g.nni, nu = k - mu * g.nni;
-    const double p = psi[(mu + 4) * g.n8 + nu + 4];
-    const double wk1 = M(M(p, p), g.f4[k]);
-    for (int q = 0; q < g.mpole; ++q) {
-      if (homo && (q % 2 == 0)) continue;
-      v[q] += g.wgt2[k] * M(g.leg[size_t(q) * g.mxsize + k], wk1);
+  if (m.coul) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+      const int mu = k / g.nni, nu = k - mu * g.nni;
+      const double p = m.psa[(mu + 4) * g.n8 + nu + 4];
+      const double wk1 = M(M(p, p), g.f4[k]);
+      for (int q = 0; q < g.mpole; ++q) {
+        if (homo && (q % 2 == 0)) continue;
+        v[q] += g.wgt2[k] * M(g.leg[size_t(q) * g.mxsize + k], wk1);
+      }
     }
-  }
-  block_sum_finish<8>(v, partials, out, g.mpole, ticket);
-}
-
-// exchMom (scfUtils.F90:615-844) with the grid's weighted P_k^q r^k tables
-__global__ void k_exchmom(GridDev g, const double *psa, const double *psb, int idel, double *partials, double *out,
-                          unsigned *ticket) {
-  double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  if (idel <= 4) {
-    const double *T = g.exm + size_t(idel) * 8 * g.mxsize;
+  } else if (m.idel <= 4) {
+    const double *T = g.exm + size_t(m.idel) * 8 * g.mxsize;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
       const int mu = k / g.nni, nu = k - mu * g.nni;
       const int ij = (mu + 4) * g.n8 + nu + 4;
-      const double wk1 = psa[ij] * psb[ij];
+      const double wk1 = m.psa[ij] * m.psb[ij];
 #pragma unroll
       for (int q = 0; q < 8; ++q)
         if (q < g.mpole) v[q] = fma(T[size_t(q) * g.mxsize + k], wk1, v[q]);
     }
   }
-  block_sum_finish<8>(v, partials, out, g.mpole, ticket);
+  block_sum_finish<8>(v, partials + size_t(blockIdx.y) * kRedBlocks * 8, m.out, g.mpole, tickets + blockIdx.y);
 }
 
 // Checks narrow_f64 / widen_f32 against the hardware conversions on n
@@ -2025,16 +2028,16 @@ void launch_triples(x2g_ctx *ctx, const GridDev &g, const TripleItem *items, int
   }
 }
 
-void launch_coulmom(x2g_ctx *ctx, const GridDev &g, const double *psi, int homo, double *out) {
-  double *part = reduction_partials(ctx, 8);
-  k_coulmom<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psi, homo, part, out, ctx->bar + 3);
-  ctx->launches += 1;
+void launch_moments(x2g_ctx *ctx, const GridDev &g, const MomentItem *items, int n, int homo) {
+  for (int b = 0; b < n; b += kMomentItems) {
+    const int m = (n - b < kMomentItems) ? n - b : kMomentItems;
+    double *part = reduction_partials(ctx, 8 * m);
+    MomentList L{};
+    for (int q = 0; q < m; ++q) L.it[q] = items[b + q];
+    k_moments<<<dim3(kRedBlocks, m), kThreads, 0, ctx->stream>>>(g, L, homo, part, ctx->bar + kMomentTickets);
+    ctx->launches += 1;
+  }
 }
 
-void launch_exchmom(x2g_ctx *ctx, const GridDev &g, const double *psa, const double *psb, int idel, double *out) {
-  double *part = reduction_partials(ctx, 8);
-  k_exchmom<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psa, psb, idel, part, out, ctx->bar + 3);
-  ctx->launches += 1;
-}
 
 }  // namespace x2g

@@ -96,8 +96,13 @@ struct TripleItem {
 };
 void launch_triples(x2g_ctx *ctx, const GridDev &g, const TripleItem *items, int n, double *out);
 // multipole moments
-void launch_coulmom(x2g_ctx *ctx, const GridDev &g, const double *psi, int homo, double *out /*[mpole]*/);
-void launch_exchmom(x2g_ctx *ctx, const GridDev &g, const double *psa, const double *psb, int idel,
-                    double *out /*[mpole]*/);
+// a batch of moments, one launch per kMomentItems: coul != 0 is coulMom of
+// psa (psb unused), else exchMom of the pair with idel
+struct MomentItem {
+  const double *psa, *psb;
+  double *out;  // [mpole]
+  int idel, coul;
+};
+void launch_moments(x2g_ctx *ctx, const GridDev &g, const MomentItem *items, int n, int homo);
 
 }  // namespace x2g

@@ -451,13 +451,16 @@ void mpole_moments(x2g_scf *s) {
   if (s->nel == 1) return;
   const GridDev &g = s->grid->d;
   const int homo = s->cs.homonuclear;
+  // all moments of the iteration in one batched launch
+  std::vector<MomentItem> items;
   for (int i = 1; i <= s->norb; i++) {
     if (!s->itouch[i]) continue;
-    launch_coulmom(s->ctx, g, s->orb[i], homo, s->sc + x2g_scf::O_CM + 8 * (i - 1));
+    items.push_back(MomentItem{s->orb[i], s->orb[i], s->sc + x2g_scf::O_CM + 8 * (i - 1), 0, 1});
   }
   for (size_t q = 0; q < s->mm_i1.size(); q++)
-    launch_exchmom(s->ctx, g, s->orb[s->mm_i1[q]], s->orb[s->mm_i2[q]], s->mm_idel[q],
-                   s->sc + x2g_scf::O_EX + 8 * s->mm_ipc[q]);
+    items.push_back(MomentItem{s->orb[s->mm_i1[q]], s->orb[s->mm_i2[q]], s->sc + x2g_scf::O_EX + 8 * s->mm_ipc[q],
+                               s->mm_idel[q], 0});
+  if (!items.empty()) launch_moments(s->ctx, g, items.data(), int(items.size()), homo);
 }
 
 void pot_asympt(x2g_scf *s, int iorb1) {
