@@ -15,11 +15,13 @@ constexpr double kPrecis = 2.220446049250313080847263336181640625e-16;  // epsil
 constexpr double kPi = 3.14159265358979323846264338327950;                // params.F90:94
 constexpr int kMaxLevels = 8;
 // device words of a context's barrier state: [0] arrivals, [1] generation,
-// [2] error word, [3] reduction ticket, then the persistent sweep's arrival
-// counters at words 32, 64, ..., 256 (one 128-byte line each), then the
-// tickets of the batched moment reductions from word 288 (kMomentItems)
-constexpr int kBarWords = 352;
+// [2] error word, [3] reduction ticket, then the tickets of the batched
+// moment reductions from word 288 (kMomentItems), then the persistent
+// sweep's per-block phase counts from word kPhaseWords (kPhaseBlocks, one
+// 128-byte line each)
 constexpr int kMomentTickets = 288;
+constexpr int kPhaseWords = 352, kPhaseBlocks = 320, kPhaseStride = 32;
+constexpr int kBarWords = kPhaseWords + kPhaseBlocks * kPhaseStride;
 
 // ----------------------------------------------------------------------
 // Host-side grid: every table the relaxation path reads, built with the

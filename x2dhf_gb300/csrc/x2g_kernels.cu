@@ -84,31 +84,24 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
   return v;
 }
 
-// Grid-wide barrier on monotonic arrival counts, spread over kArriveLanes
-// counters kArriveStride words apart (zeroed before the launch): block b
-// adds one to counter b % kArriveLanes, and the k-th barrier (k = 1, 2, ...)
-// is passed once every counter q holds k times the number of blocks with
-// residue q.  The release needs no reset and no second round trip; eight
-// lanes of warp 0 poll the eight counters.  Every wait is bounded as in
-// grid_barrier.
-constexpr int kArriveLanes = 8, kArriveStride = 32;
-__device__ bool grid_barrier_counted(const BarrierDev &b, unsigned *lanes, unsigned nblocks, unsigned k) {
+// Neighbour wait of the persistent-band sweep: block b publishes in
+// phase[b] how many colour phases it has finished (release store after its
+// writes), and before reloading its halos for phase k waits until every
+// block whose rows lie within 4 rows of its band (nb[0..5], -1 = none) has
+// finished k phases (acquire loads by lanes 0..5 of warp 0).  The wait is
+// bounded as in grid_barrier.
+__device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ bool wait_neighbours(const BarrierDev &b, const unsigned *phase, int nbq, unsigned k) {
   __shared__ int s_ok;
-  __syncthreads();
   if (threadIdx.x < 32) {
-    if (threadIdx.x == 0) {
-      __threadfence();
-      atomicAdd(lanes + (blockIdx.x % kArriveLanes) * kArriveStride, 1u);
-    }
     int ok = 1;
-    const unsigned q = threadIdx.x;
-    if (q < kArriveLanes && q < nblocks) {
-      const unsigned target = k * ((nblocks - q + kArriveLanes - 1) / kArriveLanes);
-      const unsigned *cnt = lanes + q * kArriveStride;
-      volatile int *verr = b.err;
+    if (nbq >= 0) {
       const unsigned long long t0 = globaltimer();
       unsigned spins = 0;
-      while (ld_acquire(cnt) < target) {
+      volatile int *verr = b.err;
+      while (ld_acquire(phase + size_t(nbq) * kPhaseStride) < k) {
         if (*verr) {
           ok = 0;
           break;
@@ -123,7 +116,7 @@ __device__ bool grid_barrier_counted(const BarrierDev &b, unsigned *lanes, unsig
       __threadfence();
     }
     ok = __all_sync(0xffffffffu, ok);
-    if (threadIdx.x == 0) s_ok = ok && (*(volatile int *)b.err == 0);
+    if (threadIdx.x == 0) s_ok = ok;
   }
   __syncthreads();
   return s_ok != 0;
@@ -428,7 +421,7 @@ __host__ __device__ inline size_t band_smem_bytes(const GridDev &g, int G) {
 // into an own row covers only ghost columns (zero throughout).
 __global__ void __launch_bounds__(kStagedThreads) k_mcsor_f32p(GridDev g, const __grid_constant__ JobTable jobs,
                                                                int nsweeps, int G, BarrierDev bar,
-                                                               unsigned *lanes) {
+                                                               unsigned *phase) {
   extern __shared__ __align__(16) float sband[];
   const int nrun = (g.ntiles + G - 1) / G;
   const int jb = int(blockIdx.x) / nrun, t0 = (int(blockIdx.x) - jb * nrun) * G;
@@ -443,6 +436,20 @@ __global__ void __launch_bounds__(kStagedThreads) k_mcsor_f32p(GridDev g, const 
   const float4 *src = reinterpret_cast<const float4 *>(e);
   float4 *dst = reinterpret_cast<float4 *>(sband);
   float *sb = sband - 4 * f0;  // indexed by ext index
+  // lanes 0..2 watch the runs above, 3..5 the runs below, whose rows reach
+  // into this band's halos
+  int nbq = -1;
+  {
+    const int lane = int(threadIdx.x), run = int(blockIdx.x) - jb * nrun;
+    if (lane < 6) {
+      const int q = (lane < 3) ? run - 1 - lane : run + 1 + (lane - 3);
+      if (q >= 0 && q < nrun) {
+        const int q0 = q * G, q1 = (q0 + G < g.ntiles) ? q0 + G : g.ntiles;
+        const int r0q = g.tile_row0[q0], r1q = g.tile_row1[q1 - 1];
+        if ((lane < 3 && r1q > row0 - 4) || (lane >= 3 && r0q < row1 + 4)) nbq = jb * nrun + q;
+      }
+    }
+  }
   const float omega1 = J.omega1f;
   const float *bt = (J.kind >= 1) ? g.bpot_mu32 : g.borb_mu32;
   CoefF cf;
@@ -454,10 +461,11 @@ __global__ void __launch_bounds__(kStagedThreads) k_mcsor_f32p(GridDev g, const 
   }
   for (int f = f0 + int(threadIdx.x); f < f1; f += blockDim.x) dst[f - f0] = __ldcg(src + f);
   __syncthreads();
-  unsigned nbar = 0;
+  unsigned done = 0;  // colour phases finished
   for (int s = 0; s < nsweeps; ++s) {
     for (int c = 0; c < 5; ++c) {
       if (s > 0 || c > 0) {
+        if (!wait_neighbours(bar, phase, nbq, done)) return;
         for (int f = f0 + int(threadIdx.x); f < fa; f += blockDim.x) dst[f - f0] = __ldcg(src + f);
         for (int f = fb + int(threadIdx.x); f < f1; f += blockDim.x) dst[f - f0] = __ldcg(src + f);
         if (c == 0) {
@@ -497,8 +505,11 @@ __global__ void __launch_bounds__(kStagedThreads) k_mcsor_f32p(GridDev g, const 
         }
         __syncthreads();
       }
-      if (!(s == nsweeps - 1 && c == 4)) {
-        if (!grid_barrier_counted(bar, lanes, gridDim.x, ++nbar)) return;
+      // publish the finished phase (the level loop ended with a block barrier)
+      ++done;
+      if (threadIdx.x == 0) {
+        __threadfence();
+        st_release(phase + size_t(blockIdx.x) * kPhaseStride, done);
       }
     }
   }
@@ -1764,13 +1775,14 @@ static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, 
     int nj = njobs, ns = nsweeps;
     GridDev gd = g;
     if (mixed) {
-      // one block per (job, run of G tiles); arrival counters of
-      // grid_barrier_counted zeroed with the rest
-      err = cudaMemsetAsync(ctx->bar, 0, kBarWords * sizeof(unsigned), ctx->stream);
-      if (err != cudaSuccess) return cuda_status(err, "barrier reset");
-      unsigned *lanes = ctx->bar + kArriveStride;
+      // one block per (job, run of G tiles); phase counts zeroed
       const unsigned nb = unsigned(njobs * ((g.ntiles + G - 1) / G));
-      void *args[] = {&gd, &jt, &ns, &G, &bar, &lanes};
+      if (nb > unsigned(kPhaseBlocks)) return set_status(X2G_ERR_ARG, "too many blocks for the phase counts");
+      err = cudaMemsetAsync(ctx->bar + kPhaseWords, 0, size_t(kPhaseBlocks) * kPhaseStride * sizeof(unsigned),
+                            ctx->stream);
+      if (err != cudaSuccess) return cuda_status(err, "barrier reset");
+      unsigned *phase = ctx->bar + kPhaseWords;
+      void *args[] = {&gd, &jt, &ns, &G, &bar, &phase};
       err = cudaLaunchCooperativeKernel((const void *)k_mcsor_f32p, dim3(nb), dim3(kStagedThreads), args, smem,
                                         ctx->stream);
     } else {
