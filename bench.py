@@ -366,7 +366,7 @@ def run_gpu(args):
                      "memory for the whole launch (each colour phase reloads only the 4-row halos from L2 and "
                      "writes back only the points within 4 rows of a shared band edge) and the (residual, "
                      "omega/lhs) pairs stream once per sweep, so DRAM traffic stays far below the algorithmic "
-                     "bytes and the launch is bound by phase latency (grid barrier, halo round trip, level chain), "
+                     "bytes and the launch is bound by phase latency (neighbour wait, halo round trip, level chain), "
                      "not by HBM"),
             "sweep_ms_total": msmx, "sweep_launches": nmx, "point_updates": ptsmx,
             "point_updates_per_launch": pts_per_launch,
