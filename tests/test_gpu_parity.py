@@ -304,3 +304,41 @@ def test_mixed_staged_sweep_scf_matches_on_chip():
         assert a[:2] == b[:2]
         assert abs(a[2] - b[2]) <= 1e-9 * max(1.0, abs(a[2])), (a, b)
     ctx.close()
+
+
+def test_mixed_persistent_sweep_batches_track_fp64():
+    """20 potentials on 541x721 (no cluster plan): the persistent-band sweep
+    takes them in two launches of at most 16 (the most whose bands fit the
+    GPU's shared memory two blocks per SM), and every result stays within
+    FP32 rounding of the FP64 sweep's change, as for a single job."""
+    torch = pytest.importorskip("torch")
+    import bench
+
+    nnu, nmu, r, rinf = 541, 721, 2.0, 40.0
+    assert xg.host_cluster_plan(nnu, nmu)[0] == 0
+    ctx = xg.Context(0)
+    g = xg.Grid(ctx, nnu, nmu, r, rinf, 1.0, 1.0)
+    dev = torch.device("cuda:0")
+    n8, m8 = nnu + 8, nmu + 8
+    keep, out = [], {}
+    for prec in (xg.FP64, xg.MIXED):
+        jobs, us = [], []
+        for pa, pb in bench.slater_sources(rinf, nnu, nmu, r, 20):
+            ua = torch.zeros(m8, n8, dtype=torch.float64, device=dev)
+            ub = torch.zeros_like(ua)
+            ua[4:nmu + 4, 4:nnu + 4] = torch.from_numpy(pa[0])
+            ub[4:nmu + 4, 4:nnu + 4] = torch.from_numpy(pb[0])
+            u = torch.zeros_like(ua)
+            idel = abs(pa[1] - pb[1])
+            keep += [ua, ub]
+            us.append(u)
+            jobs.append(xg.Job(u=u.data_ptr(), psa=ua.data_ptr(), psb=ub.data_ptr(), omega=1.95,
+                               isym=1 if idel % 2 == 0 else -1, idel=idel, kind=1))
+        xg.relax(ctx, g, jobs, 10, prec)
+        ctx.synchronize()
+        out[prec] = [u.cpu().numpy() for u in us]
+    for a, b in zip(out[xg.FP64], out[xg.MIXED]):
+        change = np.abs(a).max()
+        assert change > 0
+        assert np.abs(a - b).max() <= 1e-5 * change
+    ctx.close()
