@@ -110,17 +110,26 @@ int x2g_host_table(int nnu, int nmu, double r, double rinf, double z1, double z2
 int x2g_host_schedule(int nnu, int nmu, int *npoints, int *ntiles, int *nlevels, int *order, int *tile,
                       int *colour, int *level);
 /* Cluster plan of the on-chip FP32 sweep of the mixed form (no CUDA call):
- * CTAs per relaxation job (0 = grid too large, grid-barrier kernel used),
+ * CTAs per relaxation job (0 = grid too large, persistent-band kernel used),
  * rows of the largest band, shared memory per CTA, band starts row0[C+1]. */
 int x2g_host_cluster_plan(int nnu, int nmu, int *csize, int *maxrows, long *smem, int *row0);
 /* Chunk lists of the on-chip sweep (host only): chunks of up to 4 points of
  * one row at stride 5, packed (band row << 19) | (ext col << 2) | (count-1),
- * and the offsets of each CTA's 5 colours x (levels + 1) segments (level 0
- * off the shared band edges, level 0 near them, levels 1..), plus the end.
- * Null arrays: counts only. */
+ * and the offsets of each CTA's 5 colours x (levels + 2) segments (level 0
+ * off the shared band edges, level 0 near them, level-0 seam points, levels
+ * 1..), plus the end.  Null arrays: counts only. */
 int x2g_host_cluster_chunks(int nnu, int nmu, int *nchunks, int *noff, int *chunks, int *off);
+/* Schedule of the persistent-band FP32 sweep (host only): the scheduled
+ * points regrouped by colour, level and tile, packed (ext row << 16) | ext
+ * col (pts, npoints values); off[(c * nlevels + l) * (ntiles + 1) + t] is
+ * the first point of tile t in colour c, level l (5 * nlevels * (ntiles+1)
+ * values); rows[G] for G = 0..16 the most rows of G consecutive tiles plus
+ * the two 4-row halos (rows[0] unused); tile_row0 / tile_row1 the tiles' ext
+ * row ranges (ntiles values each).  Null arrays are skipped. */
+int x2g_host_band_schedule(int nnu, int nmu, int *npoints, int *ntiles, int *nlevels, int *pts, int *off, int *rows,
+                           int *tile_row0, int *tile_row1);
 /* Mixed form sweep path: 1 (default) on-chip cluster kernel where the grid
- * fits, 0 the grid-barrier FP32 kernel. */
+ * fits, 0 the persistent-band kernel. */
 int x2g_set_mixed_on_chip(x2g_ctx *ctx, int on);
 /* Self-check of the mixed form's integer-pipe FP64<->FP32 conversions
  * against the hardware conversions on n values (edge cases, then hashed bit

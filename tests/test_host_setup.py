@@ -134,3 +134,49 @@ def test_cluster_chunks_cover_schedule(nnu, nmu):
                         else:
                             assert info[p][1] == seg - 2
     assert len(seen) == len(info)
+
+
+@pytest.mark.parametrize("nnu,nmu", [(31, 31), (91, 121), (241, 301), (331, 481), (541, 721), (781, 1201)])
+def test_band_schedule_of_persistent_sweep(nnu, nmu):
+    """The persistent-band sweep's schedule: every scheduled point once,
+    grouped by colour, level and tile exactly as the sweep schedule assigns
+    them; run heights with halos; the 16-byte pieces of a band's halos reach
+    into its own rows only on ghost columns; every row inside another band's
+    halo lies within 4 rows of its own band's edge (written back each
+    phase); at most three runs on either side reach into a band's halos."""
+    pts, off, rows, r0, r1, nlev = xg.host_band_schedule(nnu, nmu)
+    order, ij, tile, colour, lev = xg.host_schedule(nnu, nmu)
+    n8, m8 = nnu + 8, nmu + 8
+    nt = len(r0)
+    assert r0[0] == 4 and r1[-1] == nmu and (r0[1:] == r1[:-1]).all()
+    ext = (pts >> 16) * n8 + (pts & 0xFFFF)
+    assert np.array_equal(np.sort(ext), np.sort(ij))
+    where = {int(p): (int(t), int(c), int(l)) for p, t, c, l in zip(ij, tile, colour, lev)}
+    offs = off.reshape(5, nlev, nt + 1)
+    for c in range(5):
+        for l in range(nlev):
+            for t in range(nt):
+                for k in range(offs[c, l, t], offs[c, l, t + 1]):
+                    assert where[int(ext[k])] == (t, c, l)
+    assert offs[-1, -1, -1] == len(pts) and offs[0, 0, 0] == 0
+    for G in range(1, 17):
+        runs = [(int(r0[t0]), int(r1[min(t0 + G, nt) - 1])) for t0 in range(0, nt, G)]
+        assert rows[G] == max(b - a for a, b in runs) + 8
+        for k, (a, b) in enumerate(runs):
+            f0, f1 = ((a - 4) * n8) >> 2, ((b + 4) * n8 + 3) >> 2
+            fa, fb = (a * n8 + 3) >> 2, (b * n8) >> 2
+            assert f0 >= 0 and 4 * f1 <= n8 * m8 and 4 * (f1 - f0) <= rows[G] * n8 + 8
+            assert all(q // n8 == a and q % n8 < 4 for q in range(a * n8, 4 * fa))
+            assert all(q // n8 == b - 1 and q % n8 >= nnu + 4 for q in range(4 * fb, b * n8))
+            lo = a + 4 if k > 0 else a
+            hi = b - 4 if k < len(runs) - 1 else b
+            for j, (c0, c1) in enumerate(runs):
+                if j == k:
+                    continue
+                for x in list(range(c1, c1 + 4)) + list(range(c0 - 4, c0)):
+                    if a <= x < b:
+                        assert x < lo or x >= hi
+            up = [j for j in range(k) if runs[j][1] > a - 4]
+            dn = [j for j in range(k + 1, len(runs)) if runs[j][0] < b + 4]
+            assert up == list(range(k - len(up), k)) and dn == list(range(k + 1, k + 1 + len(dn)))
+            assert len(up) <= 3 and len(dn) <= 3

@@ -73,7 +73,7 @@ EXPORTS = [
     "x2g_scf_set_function", "x2g_scf_get_function", "x2g_scf_set_start_values", "x2g_scf_get_start_values",
     "x2g_kernel_launches", "x2g_transfer_bytes", "mcsor_pthread_", "mcsor_tpool_", "coulExch_pthread_", "coulExch_tpool_",
     "tpoolStop4mcsor_", "tpoolStop4pots_", "x2g_host_table", "x2g_host_schedule", "x2g_profile",
-    "x2g_relax_noalloc", "x2g_host_cluster_plan", "x2g_set_mixed_on_chip", "x2g_host_cluster_chunks",
+    "x2g_relax_noalloc", "x2g_host_cluster_plan", "x2g_set_mixed_on_chip", "x2g_host_cluster_chunks", "x2g_host_band_schedule",
     "x2g_convert_selftest",
 ]
 
@@ -127,6 +127,7 @@ def lib():
     L.x2g_host_table.argtypes = [I, I, D, D, D, D, I, dp]
     ip = C.POINTER(C.c_int)
     L.x2g_host_schedule.argtypes = [I, I, ip, ip, ip, ip, ip, ip, ip]
+    L.x2g_host_band_schedule.argtypes = [I, I, ip, ip, ip, ip, ip, ip, ip, ip]
     L.x2g_profile.argtypes = [P, I, I, dp, dp, C.POINTER(C.c_long)]
     L.x2g_host_cluster_plan.argtypes = [I, I, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_long),
                                         C.POINTER(C.c_int)]
@@ -312,6 +313,20 @@ def host_schedule(nnu, nmu):
     _check(L.x2g_host_schedule(nnu, nmu, C.byref(n), C.byref(t), C.byref(l),
                                list_order.ctypes.data_as(C.POINTER(C.c_int)), None, None, None))
     return list_order, arrs[0], arrs[1], arrs[2], arrs[3]
+
+
+def host_band_schedule(nnu, nmu):
+    """(pts, off, rows, tile_row0, tile_row1, nlevels) of the persistent-band sweep (no GPU needed)."""
+    L = lib()
+    n, t, lv = C.c_int(), C.c_int(), C.c_int()
+    _check(L.x2g_host_band_schedule(nnu, nmu, C.byref(n), C.byref(t), C.byref(lv), None, None, None, None, None))
+    pts = np.zeros(n.value, np.int32)
+    off = np.zeros(5 * lv.value * (t.value + 1), np.int32)
+    rows = np.zeros(17, np.int32)
+    r0, r1 = np.zeros(t.value, np.int32), np.zeros(t.value, np.int32)
+    ip = [a.ctypes.data_as(C.POINTER(C.c_int)) for a in (pts, off, rows, r0, r1)]
+    _check(L.x2g_host_band_schedule(nnu, nmu, C.byref(n), C.byref(t), C.byref(lv), *ip))
+    return pts, off, rows, r0, r1, lv.value
 
 
 def host_cluster_chunks(nnu, nmu):

@@ -310,7 +310,7 @@ int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, doubl
   UP(h.pts_rc, pts_rc);
   UP(h.st_pts, st_pts);
   UP(h.st_off, st_off);
-  for (int k = 0; k <= HostGrid::kStagedRuns; ++k) d.st_rows[k] = h.st_rows[k];
+  for (int k = 0; k <= HostGrid::kBandRuns; ++k) d.st_rows[k] = h.st_rows[k];
   d.cl_size = h.cl_size;
   d.cl_maxrows = h.cl_maxrows;
   d.cl_maxchunks = h.cl_maxchunks;

@@ -60,15 +60,16 @@ struct HostGrid {
   // has cl_size * 5 * (nlev + 2) + 1 chunk offsets; cl_wa/wb/ws warps per
   // CTA work on the three kinds
   std::vector<int> cl_pts, cl_off;
-  // staged FP32 sweep of grids beyond one cluster: the same points regrouped
-  // [colour][level][tile] (st_pts, packed (ext row << 16) | ext col), so that the points of one
-  // colour and level in any run of consecutive tiles are one contiguous
-  // range; st_off[(c * nlev + l) * (ntiles + 1) + t] is the start of tile t.
-  // st_rows[G] = most rows of any run of G consecutive tiles (G = 1..4), plus
-  // the 4-row halos on both sides (G = 1..kStagedRuns)
-  static constexpr int kStagedRuns = 16;
+  // persistent-band FP32 sweep of grids beyond one cluster: the same points
+  // regrouped [colour][level][tile] (st_pts, packed (ext row << 16) | ext
+  // col), so that the points of one colour and level in any run of
+  // consecutive tiles are one contiguous range; st_off[(c * nlev + l) *
+  // (ntiles + 1) + t] is the start of tile t.  st_rows[G] = most rows of any
+  // run of G consecutive tiles plus the 4-row halos on both sides (G =
+  // 1..kBandRuns)
+  static constexpr int kBandRuns = 16;
   std::vector<int> st_pts, st_off;
-  int st_rows[kStagedRuns + 1] = {};
+  int st_rows[kBandRuns + 1] = {};
 };
 
 std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf, double z1, double z2, int mpole);
@@ -117,7 +118,7 @@ struct JobDev {
   double *rhs_buf;  // materialised rhs for potentials
   float *e32;       // mixed: FP32 extended correction
   float *r32, *w32; // mixed: FP32 residual and omega / diagonal
-  float2 *rw;       // mixed, staged sweep: (residual, omega / diagonal) in st_pts order
+  float2 *rw;       // mixed, persistent-band sweep: (residual, omega / diagonal) in st_pts order
   double omega;
   double idel2;
   float omegaf, omega1f;  // omega and 1 - omega rounded to FP32 on the host
@@ -160,10 +161,10 @@ struct x2g_ctx {
   int cluster_nonportable = 0;  // cluster kernel allowed more than 8 CTAs
   long cluster_checked_key = -1;  // (shared bytes, cluster size) last checked
   int cluster_ok = 0;             // that cluster shape is schedulable here
-  int staged_attr = 0;            // shared memory cap granted to the persistent-band sweep
-  long staged_key = -1;           // shared bytes of its last occupancy query
-  int staged_blocks = 0;          // co-resident blocks for that size
-  int staged_sm_smem = 0;         // shared memory per SM
+  int band_attr = 0;            // shared memory cap granted to the persistent-band sweep
+  long band_key = -1;           // shared bytes of its last occupancy query
+  int band_blocks = 0;          // co-resident blocks for that size
+  int band_sm_smem = 0;         // shared memory per SM
   // optional per-launch timing of the sweep kernels (CUDA events on stream)
   int profiling = 0;
   struct Pending {

@@ -18,7 +18,7 @@ namespace x2g {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kStagedThreads = 512;
+constexpr int kBandThreads = 512;
 constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
 
 __device__ __forceinline__ double A(double a, double b) { return __dadd_rn(a, b); }
@@ -154,7 +154,7 @@ struct CoefF {
 };
 
 // FP32 correction sweep point update (same operator, FMA allowed) on a band
-// of the correction staged in shared memory; w is omega / lhs of the point,
+// of the correction held in shared memory; w is omega / lhs of the point,
 // formed once per relaxation call.  Returns the new value.
 __device__ __forceinline__ float relax_f32(const float *__restrict__ e, int ij, int n8, const CoefF &c, float b,
                                            float d, float w, float r, float omega1) {
@@ -419,7 +419,7 @@ __host__ __device__ inline size_t band_smem_bytes(const GridDev &g, int G) {
 // different tiles, so the values a phase changes in a neighbour's rows are
 // never read by this block in that phase, and a halo piece that reaches
 // into an own row covers only ghost columns (zero throughout).
-__global__ void __launch_bounds__(kStagedThreads) k_mcsor_f32p(GridDev g, const __grid_constant__ JobTable jobs,
+__global__ void __launch_bounds__(kBandThreads) k_mcsor_f32p(GridDev g, const __grid_constant__ JobTable jobs,
                                                                int nsweeps, int G, BarrierDev bar,
                                                                unsigned *phase) {
   extern __shared__ __align__(16) float sband[];
@@ -921,7 +921,8 @@ __device__ __forceinline__ double ghost_read(const GridDev &g, const double *u, 
 // FP32 with omega / lhs; the stencil uses the grid's separable weights (one
 // FMA per neighbour) and reads the ghost cells as mirrored interior values,
 // so u needs no ghost refresh first.  kPacked: the points are taken in
-// st_pts order and stored as (r, w) pairs in that order (staged sweep);
+// st_pts order and stored as (r, w) pairs in that order (persistent-band
+// sweep);
 // otherwise r32 / w32 are plain nni x nmu arrays (cluster sweep).
 template <bool kPacked>
 __global__ void k_residual(GridDev g, const __grid_constant__ JobTable jobs, int zero_e) {
@@ -1674,7 +1675,7 @@ static bool cluster_usable(x2g_ctx *ctx, const GridDev &g) {
 // cap is raised once to the device's opt-in maximum, as for the cluster
 // kernel.
 static int persistent_shape(x2g_ctx *ctx, const GridDev &g, int most, int *nj, int *G, size_t *smem) {
-  if (!ctx->staged_attr) {
+  if (!ctx->band_attr) {
     // the cap counts dynamic bytes only: the opt-in maximum less the
     // kernel's static shared memory (the grid barrier's flag)
     int optin = 0;
@@ -1686,33 +1687,33 @@ static int persistent_shape(x2g_ctx *ctx, const GridDev &g, int most, int *nj, i
       (void)cudaGetLastError();
       return set_status(X2G_ERR_CUDA, "persistent sweep attributes could not be set");
     }
-    ctx->staged_attr = optin - int(fa.sharedSizeBytes);
+    ctx->band_attr = optin - int(fa.sharedSizeBytes);
     int per_sm = 0;
     if (cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device) != cudaSuccess)
       return set_status(X2G_ERR_CUDA, "device attribute query failed");
-    ctx->staged_sm_smem = per_sm;
+    ctx->band_sm_smem = per_sm;
   }
   for (int n = most; n >= 1; --n)
-    for (int r = 1; r <= HostGrid::kStagedRuns; ++r) {
+    for (int r = 1; r <= HostGrid::kBandRuns; ++r) {
       const size_t sm = band_smem_bytes(g, r);
-      if (sm > size_t(ctx->staged_attr)) break;
+      if (sm > size_t(ctx->band_attr)) break;
       // two blocks per SM (1024 threads) hide more latency than one block
       // with twice the band
-      int bpsm = int(size_t(ctx->staged_sm_smem) / (sm + 1024));
+      int bpsm = int(size_t(ctx->band_sm_smem) / (sm + 1024));
       if (bpsm < 2) break;
       bpsm = 2;
       const int items = n * ((g.ntiles + r - 1) / r);
       if (bpsm >= 1 && items <= bpsm * ctx->num_sms) {
         // confirm with the occupancy calculator (once per shared size)
-        if (ctx->staged_key != long(sm)) {
+        if (ctx->band_key != long(sm)) {
           int per = 0;
           cudaError_t err =
-              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void *)k_mcsor_f32p, kStagedThreads, sm);
+              cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void *)k_mcsor_f32p, kBandThreads, sm);
           if (err != cudaSuccess) return cuda_status(err, "occupancy query");
-          ctx->staged_key = long(sm);
-          ctx->staged_blocks = per * ctx->num_sms;
+          ctx->band_key = long(sm);
+          ctx->band_blocks = per * ctx->num_sms;
         }
-        if (items > ctx->staged_blocks) continue;
+        if (items > ctx->band_blocks) continue;
         *nj = n;
         *G = r;
         *smem = sm;
@@ -1783,7 +1784,7 @@ static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, 
       if (err != cudaSuccess) return cuda_status(err, "barrier reset");
       unsigned *phase = ctx->bar + kPhaseWords;
       void *args[] = {&gd, &jt, &ns, &G, &bar, &phase};
-      err = cudaLaunchCooperativeKernel((const void *)k_mcsor_f32p, dim3(nb), dim3(kStagedThreads), args, smem,
+      err = cudaLaunchCooperativeKernel((const void *)k_mcsor_f32p, dim3(nb), dim3(kBandThreads), args, smem,
                                         ctx->stream);
     } else {
       static int max_f64 = -1;
@@ -1829,9 +1830,8 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
              : (size_t(g.mxsize) * sizeof(double) + 256)) / 256 * 256 + 256;
   char *scratch = static_cast<char *>(ctx_workspace(ctx, per_job * njobs + 256));
   if (!scratch) return set_status(X2G_ERR_ALLOC, "workspace allocation failed");
-  // the staged sweep takes as many jobs per launch as keep their corrections
-  // and (residual, omega/lhs) pairs within 3/4 of L2, so that the five colour
-  // phases of every sweep re-read them from L2 rather than HBM
+  // the persistent-band sweep takes as many jobs per launch as give every
+  // (job, run of tiles) its own co-resident block
   int per_launch = kParamJobs, G = 0;
   size_t smem = 0;
   if (mixed && !on_chip) {
@@ -1849,7 +1849,7 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
         d.e32 = reinterpret_cast<float *>(p);
         d.r32 = reinterpret_cast<float *>(p + (size_t(g.next) * sizeof(float) + 127) / 128 * 128);
         d.w32 = d.r32 + g.mxsize;
-        d.rw = reinterpret_cast<float2 *>(d.r32);  // staged sweep: pairs over r32 and w32
+        d.rw = reinterpret_cast<float2 *>(d.r32);  // persistent-band sweep: pairs over r32 and w32
       } else {
         d.rhs_buf = reinterpret_cast<double *>(p);
       }

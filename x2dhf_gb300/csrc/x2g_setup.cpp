@@ -289,7 +289,7 @@ std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf
       }
       so[g.ntiles] = int(g.st_pts.size());
     }
-  for (int G = 1; G <= HostGrid::kStagedRuns; ++G) {
+  for (int G = 1; G <= HostGrid::kBandRuns; ++G) {
     int most = 0;
     for (int t0 = 0; t0 < g.ntiles; t0 += G) {
       const int t1 = std::min(t0 + G, g.ntiles);
@@ -514,6 +514,22 @@ extern "C" int x2g_host_cluster_plan(int nnu, int nmu, int *csize, int *maxrows,
 // Chunk lists of the on-chip sweep: nchunks packed chunks and noff segment
 // offsets (CTA-major, 5 colours x (nlevels + 1) segments per CTA, plus the
 // end).  Call with null arrays for the counts.
+extern "C" int x2g_host_band_schedule(int nnu, int nmu, int *npoints, int *ntiles, int *nlevels, int *pts, int *off,
+                                      int *rows, int *tile_row0, int *tile_row1) {
+  x2g::HostGrid g;
+  std::string msg = x2g::build_host_grid(g, nnu, nmu, 2.0, 40.0, 1.0, 1.0, 4);
+  if (!msg.empty()) return X2G_ERR_SCHEDULE;
+  if (npoints) *npoints = int(g.st_pts.size());
+  if (ntiles) *ntiles = g.ntiles;
+  if (nlevels) *nlevels = g.nlev;
+  if (pts) std::copy(g.st_pts.begin(), g.st_pts.end(), pts);
+  if (off) std::copy(g.st_off.begin(), g.st_off.end(), off);
+  if (rows) std::copy(g.st_rows, g.st_rows + x2g::HostGrid::kBandRuns + 1, rows);
+  if (tile_row0) std::copy(g.tile_row0.begin(), g.tile_row0.end(), tile_row0);
+  if (tile_row1) std::copy(g.tile_row1.begin(), g.tile_row1.end(), tile_row1);
+  return X2G_OK;
+}
+
 extern "C" int x2g_host_cluster_chunks(int nnu, int nmu, int *nchunks, int *noff, int *chunks, int *off) {
   x2g::HostGrid g;
   std::string msg = x2g::build_host_grid(g, nnu, nmu, 2.0, 40.0, 1.0, 1.0, 4);
