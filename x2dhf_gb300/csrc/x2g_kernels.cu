@@ -410,15 +410,18 @@ __host__ __device__ inline size_t band_smem_bytes(const GridDev &g, int G) {
 // consecutive tiles of one job (rows [row0, row1)) and keeps the
 // correction on those rows, with 4-row halos, in shared memory, as whole
 // 16-byte pieces: piece f holds ext indices 4f..4f+3 at sband[4 (f - f0)].
-// Every colour phase refreshes the two halos from the correction in global
-// memory (L2), updates the phase's points level by level in shared memory,
-// and writes to global memory only the new values within 4 rows of a band
-// edge shared with another block, which are that block's halo; a grid
-// barrier on counted arrivals ends the phase.  The band goes back to global
-// memory after the last sweep.  Same-colour stencil neighbours never lie in
-// different tiles, so the values a phase changes in a neighbour's rows are
-// never read by this block in that phase, and a halo piece that reaches
-// into an own row covers only ghost columns (zero throughout).
+// Every colour phase waits until the blocks within halo reach have
+// finished the previous phase (wait_neighbours; this also means they are
+// done reading this band's edge rows), refreshes the two halos from the
+// correction in global memory (L2), updates the phase's points level by
+// level in shared memory, writes to global memory only the new values
+// within 4 rows of a band edge shared with another block (that block's
+// halo), and publishes its finished phase count.  No grid-wide barrier.
+// The band goes back to global memory after the last sweep.  Same-colour
+// stencil neighbours never lie in different tiles, so the values a phase
+// changes in a neighbour's rows are never read by this block in that phase,
+// and a halo piece that reaches into an own row covers only ghost columns
+// (zero throughout).
 __global__ void __launch_bounds__(kBandThreads) k_mcsor_f32p(GridDev g, const __grid_constant__ JobTable jobs,
                                                                int nsweeps, int G, BarrierDev bar,
                                                                unsigned *phase) {
