@@ -40,6 +40,10 @@ FLOPS_PER_PT = 54.0
 # correction, residual and omega/lhs stay in shared memory, so DRAM sees only
 # the band load (the u += e writeback was still in L2 when the launch ended)
 CLUSTER_DRAM_BYTES_PER_PT = 2765824.0 / 1566040.0
+# the same for the persistent-band sweep of grids beyond one cluster, from
+# ncu of two 6-job, 10-sweep launches on 781x1201 (71.38 + 1.57 MB read + write
+# per launch, 55 901 040 point-updates)
+BAND_DRAM_BYTES_PER_PT = (71379200.0 + 1573120.0) / 55901040.0
 
 
 def n2_deck(grid="337 481 40.0"):
@@ -317,7 +321,8 @@ def run_gpu(args):
     h2d = copied[0] // max(1, copied[2])
     d2h = copied[1] // max(1, copied[2])
     pts_per_launch = ptsmx / nmx if nmx else None
-    traffic = CLUSTER_DRAM_BYTES_PER_PT * pts_per_launch if (pts_per_launch and on_chip) else None
+    traffic = ((CLUSTER_DRAM_BYTES_PER_PT if on_chip else BAND_DRAM_BYTES_PER_PT) * pts_per_launch
+               if pts_per_launch else None)
     out = {
         "metric": metric,
         "value": value,
