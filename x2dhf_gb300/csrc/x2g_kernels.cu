@@ -361,6 +361,26 @@ __global__ void __launch_bounds__(kThreads) k_mcsor_f64(GridDev g, const __grid_
   }
 }
 
+// float -> double by bit manipulation on the integer pipes (GB300 issues
+// conversion instructions on its narrow FP64 pipe); exact for normal floats,
+// infinities and NaNs; float subnormals (|e| < 1.2e-38, far below any
+// correction that matters) become signed zero
+__device__ __forceinline__ double widen_f32(float f) {
+  const unsigned b = __float_as_uint(f), ex = (b >> 23) & 0xffu, m = b & 0x7fffffu;
+  const unsigned sign = b & 0x80000000u;
+  if (ex == 0) return __hiloint2double(int(sign), 0);
+  const unsigned dex = (ex == 0xffu) ? 0x7ffu : ex + 896u;
+  return __hiloint2double(int(sign | (dex << 20) | (m >> 3)), int(m << 29));
+}
+
+// FP64 axis extrapolation of one point from its 5 neighbours at stride st
+// (sormcsor.F90:94-129 order)
+__device__ __forceinline__ double extrap64(const GridDev &g, const double *u, int ij, int st) {
+  return A(A(A(A(M(g.exeven[0], u[ij + st]), M(g.exeven[1], u[ij + 2 * st])), M(g.exeven[2], u[ij + 3 * st])),
+             M(g.exeven[3], u[ij + 4 * st])),
+           M(g.exeven[4], u[ij + 5 * st]));
+}
+
 // Axis extrapolation of the correction (tile_boundary<float>) for tiles
 // [t0, t1) computed in the band sb held in shared memory (indexed by ext
 // index).
@@ -417,11 +437,12 @@ __host__ __device__ inline size_t band_smem_bytes(const GridDev &g, int G) {
 // level in shared memory, writes to global memory only the new values
 // within 4 rows of a band edge shared with another block (that block's
 // halo), and publishes its finished phase count.  No grid-wide barrier.
-// The band goes back to global memory after the last sweep.  Same-colour
+// Same-colour
 // stencil neighbours never lie in different tiles, so the values a phase
 // changes in a neighbour's rows are never read by this block in that phase,
 // and a halo piece that reaches into an own row covers only ghost columns
-// (zero throughout).
+// (zero throughout).  The kernel ends with u += e and the FP64 axis values
+// of u on the band's rows, so the correction never returns to global memory.
 __global__ void __launch_bounds__(kBandThreads) k_mcsor_f32p(GridDev g, const __grid_constant__ JobTable jobs,
                                                                int nsweeps, int G, BarrierDev bar,
                                                                unsigned *phase) {
@@ -516,9 +537,48 @@ __global__ void __launch_bounds__(kBandThreads) k_mcsor_f32p(GridDev g, const __
       }
     }
   }
-  band_boundary(g, sb, t0, t1, J.isym == 1);
+  // u += e on the band's interior rows, then the FP64 axis values of u on
+  // the band's rows (sormcsor.F90:94-129; the axis points read only the
+  // band's own rows)
+  double *u = J.u;
+  const int ra = (row0 > 5) ? row0 : 5, ncol = g.nni - 2, total = (row1 - ra) * ncol;
+  for (int k0 = threadIdx.x; k0 < total; k0 += 8 * int(blockDim.x)) {
+    // eight loads of u in flight per thread before the adds
+    int ij[8];
+    double uv[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int k = k0 + q * int(blockDim.x);
+      ij[q] = -1;
+      if (k < total) {
+        ij[q] = (ra + k / ncol) * n8 + 5 + k % ncol;
+        uv[q] = __ldcg(u + ij[q]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (ij[q] >= 0) u[ij[q]] = uv[q] + widen_f32(sb[ij[q]]);
+  }
   __syncthreads();
-  for (int ij = row0 * n8 + int(threadIdx.x); ij < row1 * n8; ij += blockDim.x) e[ij] = sb[ij];
+  const bool even = (J.isym == 1);
+  const int nrow7 = (t0 == 0) ? g.nni - 2 : 0, nside = 2 * (row1 - ra);
+  for (int k = threadIdx.x; k < nrow7 + nside; k += blockDim.x) {
+    if (k < nrow7) {
+      const int ij = 4 * n8 + 5 + k;
+      u[ij] = even ? extrap64(g, u, ij, n8) : 0.0;
+    } else {
+      const int q = k - nrow7, r = ra + q / 2, side = q % 2;
+      const int ij = r * n8 + (side == 0 ? 4 : g.nni + 3);
+      u[ij] = even ? extrap64(g, u, ij, side == 0 ? 1 : -1) : 0.0;
+    }
+  }
+  if (t0 == 0) {
+    __syncthreads();
+    if (threadIdx.x < 2) {
+      const int ij = 4 * n8 + (threadIdx.x == 0 ? 4 : g.nni + 3);
+      u[ij] = even ? extrap64(g, u, ij, threadIdx.x == 0 ? 1 : -1) : 0.0;
+    }
+  }
 }
 
 // ----------------------------------------------------------------------
@@ -574,26 +634,6 @@ size_t cluster_smem_bytes(const GridDev &g) {
 // distributed-shared writes, wait acquires every CTA's released writes
 __device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
 __device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
-
-// float -> double by bit manipulation on the integer pipes (GB300 issues
-// conversion instructions on its narrow FP64 pipe); exact for normal floats,
-// infinities and NaNs; float subnormals (|e| < 1.2e-38, far below any
-// correction that matters) become signed zero
-__device__ __forceinline__ double widen_f32(float f) {
-  const unsigned b = __float_as_uint(f), ex = (b >> 23) & 0xffu, m = b & 0x7fffffu;
-  const unsigned sign = b & 0x80000000u;
-  if (ex == 0) return __hiloint2double(int(sign), 0);
-  const unsigned dex = (ex == 0xffu) ? 0x7ffu : ex + 896u;
-  return __hiloint2double(int(sign | (dex << 20) | (m >> 3)), int(m << 29));
-}
-
-// FP64 axis extrapolation of one point from its 5 neighbours at stride st
-// (sormcsor.F90:94-129 order)
-__device__ __forceinline__ double extrap64(const GridDev &g, const double *u, int ij, int st) {
-  return A(A(A(A(M(g.exeven[0], u[ij + st]), M(g.exeven[1], u[ij + 2 * st])), M(g.exeven[2], u[ij + 3 * st])),
-             M(g.exeven[3], u[ij + 4 * st])),
-           M(g.exeven[4], u[ij + 5 * st]));
-}
 
 // (row, col) of the points k, k+T, k+2T, ... of a band's interior listed
 // row by row from (ra, 5) with ncols columns per row, advanced without
@@ -988,44 +1028,6 @@ __global__ void k_residual(GridDev g, const __grid_constant__ JobTable jobs, int
   }
 }
 
-__global__ void k_update(GridDev g, const __grid_constant__ JobTable jobs) {
-  const JobDev &J = jobs.j[blockIdx.y];
-  const int nint = (g.nni - 2) * (g.nmu - 5);
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nint; k += gridDim.x * blockDim.x) {
-    const int mu = 1 + k / (g.nni - 2), nu = 1 + k % (g.nni - 2);
-    const int ij = (mu + 4) * g.n8 + nu + 4;
-    J.u[ij] += double(J.e32[ij]);
-  }
-}
-
-// Axis extrapolation of the FP64 function after the update (one block per job).
-__global__ void k_extrap_jobs(GridDev g, const __grid_constant__ JobTable jobs) {
-  const JobDev &J = jobs.j[blockIdx.x];
-  double *u = J.u;
-  const int n8 = g.n8, nni = g.nni;
-  const bool even = (J.isym == 1);
-  const int nrow7 = nni - 2, nside = 2 * (g.nmu - 5);
-  auto ex = [&](int ij, int s) {
-    return A(A(A(A(M(g.exeven[0], u[ij + s]), M(g.exeven[1], u[ij + 2 * s])), M(g.exeven[2], u[ij + 3 * s])),
-               M(g.exeven[3], u[ij + 4 * s])),
-             M(g.exeven[4], u[ij + 5 * s]));
-  };
-  for (int k = threadIdx.x; k < nrow7 + nside; k += blockDim.x) {
-    if (k < nrow7) {
-      const int ij = 4 * n8 + 5 + k;
-      u[ij] = even ? ex(ij, n8) : 0.0;
-    } else {
-      const int q = k - nrow7, r = 5 + q / 2, side = q % 2;
-      const int ij = r * n8 + (side == 0 ? 4 : nni + 3);
-      u[ij] = even ? ex(ij, side == 0 ? 1 : -1) : 0.0;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x < 2) {
-    const int ij = 4 * n8 + (threadIdx.x == 0 ? 4 : nni + 3);
-    u[ij] = even ? ex(ij, threadIdx.x == 0 ? 1 : -1) : 0.0;
-  }
-}
 
 // ----------------------------------------------------------------------
 // Elementwise kernels of the SCF path
@@ -1810,12 +1812,8 @@ static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, 
       cudaEventRecord(pe.b, ctx->stream);
       ctx->pending.push_back(pe);
     }
-    if (mixed) {
-      dim3 gu(grid_blocks((g.nni - 2) * (g.nmu - 5)), njobs);
-      k_update<<<gu, kThreads, 0, ctx->stream>>>(g, jt);
-      k_extrap_jobs<<<njobs, kThreads, 0, ctx->stream>>>(g, jt);
-      ctx->launches += 2;
-    }
+    // the mixed form's update u += e and the axis of u are the
+    // persistent-band sweep's epilogue
   }
   return X2G_OK;
 }
