@@ -199,6 +199,22 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def workload_config(name, case=None):
+    """The `config` of a workload's JSON line, shared by both arms."""
+    out = {"workload": f"{name}: " + WORKLOAD_TEXT[name],
+           "convergence": "orbital-energy change < 1e-12 for 4 consecutive SCF iterations",
+           "parallelism": "replicas only (independent SCF solves per GPU)"}
+    try:
+        import x2dhf_gb300 as xg
+
+        c = case if case is not None else xg.parse_deck(WORKLOADS[name]())
+        out["grid"] = [c.nnu, c.nmu]
+        out["points_per_sweep"] = (c.nnu - 2) * (c.nmu - 5)
+    except Exception:  # the reference arm may run without the library built
+        pass
+    return out
+
+
 def max_over_ranks(values, world, device):
     """Element-wise maximum of per-rank timings over all ranks (replicas run
     the same work independently; no collective touches the data path)."""
@@ -302,7 +318,6 @@ def run_gpu(args):
     hbm, peak_kind = peaks()
     grid_pts = None
     c = xg.parse_deck(deck)
-    mx_pts = (c.nnu - 2) * (c.nmu - 5)
     # per-launch figures of the dominant kernel of the headline (mixed) run
     sweep_gbs_mx = ptsmx * BYTES_PER_PT[1] / (msmx / 1e3) / 1e9 if msmx > 0 else None
     sweep_gbs_64 = pts64 * BYTES_PER_PT[0] / (ms64 / 1e3) / 1e9 if ms64 > 0 else None
@@ -336,21 +351,16 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "f32 sweeps + f64 defect correction (value); f64 (fp64 leg)",
         "data": "synthetic: hydrogenic LCAO start of the reference's own input deck, no dataset",
-        "config": {
-            "workload": f"{args.workload}: " + WORKLOAD_TEXT[args.workload],
-            "grid": [c.nnu, c.nmu],
-            "points_per_sweep": mx_pts,
-            "convergence": "orbital-energy change < 1e-12 for 4 consecutive SCF iterations",
-            "l2": "512 MiB buffer written between timed solves (L2 flushed)",
-            "parallelism": "replicas only (independent SCF solves per GPU)",
-        },
-        "latency_s": {"p50": statistics.median(latmx), "p99": p99, "fp64_p50": statistics.median(lat64)},
-        "fp64": {"value": fp64_value, "unit": unit, "iterations": it64,
+        "config": dict(workload_config(args.workload, c),
+                       l2="512 MiB buffer written between timed solves (L2 flushed)"),
+        "latency_s": {"p50": statistics.median(latmx), "p99": p99,
+                      "fp64_p50": statistics.median(lat64) if run64 else None},
+        "fp64": {"value": fp64_value if run64 else None, "unit": unit, "iterations": it64,
                  "total_energy": res64.total_energy if res64 else None, "sweeps": res64.sweeps if res64 else None},
         "mixed": {"iterations": itmx, "total_energy": resmx.total_energy if resmx else None,
                   "sweeps": resmx.sweeps if resmx else None,
                   "dE_vs_fp64": abs(resmx.total_energy - res64.total_energy) if (resmx and res64) else None,
-                  "speedup_vs_fp64": value / fp64_value},
+                  "speedup_vs_fp64": value / fp64_value if run64 else None},
         "e2e": {"value": e2e_value, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches_mx,
         "roofline": {
@@ -569,7 +579,7 @@ def run_reference(args):
             "unit": unit, "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / v,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic: hydrogenic LCAO start of the reference's input", "impl": "reference",
-            "config": {"workload": f"{args.workload}: " + WORKLOAD_TEXT[args.workload]},
+            "config": dict(workload_config(args.workload), iterations_per_step=n),
             "cpu_baseline": {"value": v, "unit": unit, "cores": nthreads, "kind": kind,
                              "sample": f"per step: setup + prepSCF + 1 iteration, then {min(args.cpu_iters, 4)} "
                                        f"timed SCF iterations on {nthreads} threads"},
@@ -587,7 +597,7 @@ def run_reference(args):
         "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * solve_s, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic: hydrogenic LCAO start of the reference's input", "impl": "reference",
-        "config": {"workload": args.workload, "iterations_per_solve": iters},
+        "config": dict(workload_config(args.workload), iterations_per_solve=iters),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": kind,
                          "sample": f"per step: setup + prepSCF + {1 + args.cpu_iters} SCF iterations on "
                                    f"{nthreads} threads, extrapolated to {iters} iterations/solve"},
