@@ -86,7 +86,7 @@ int x2g_create(x2g_ctx **out, int device) {
     delete c;
     return cuda_status(e, "barrier allocation");
   }
-  c->red_bytes = size_t(160) * 16 * sizeof(double) + 64 * sizeof(double);
+  c->red_bytes = size_t(608) * 16 * sizeof(double) + 64 * sizeof(double);  // most reduction blocks x partials
   if ((e = cudaMalloc(&c->red, c->red_bytes)) != cudaSuccess ||
       (e = cudaMallocHost(&c->host_red, 1024 * sizeof(double))) != cudaSuccess) {
     cudaFree(c->bar);

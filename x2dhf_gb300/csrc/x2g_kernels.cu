@@ -1334,7 +1334,15 @@ __global__ void k_zero(double *p, size_t n) {
 // Deterministic reductions: fixed grid -> per-block partials -> the last
 // block to finish sums the partials in block order.
 // ----------------------------------------------------------------------
-constexpr int kRedBlocks = 160;
+constexpr int kRedBlocks = 160, kRedBlocksMax = 608;
+// blocks of a single-launch reduction over the grid: 160 up to ~160k
+// points, one per 1024 points above that (more loads in flight on large
+// grids), at most 608; fixed per grid, so every sum runs in the same order
+// on every call
+inline int red_blocks(const GridDev &g) {
+  const int b = g.mxsize / 1024;
+  return b < kRedBlocks ? kRedBlocks : (b > kRedBlocksMax ? kRedBlocksMax : b);
+}
 constexpr int kMaxK = 16;
 
 template <int K>
@@ -1494,7 +1502,7 @@ __global__ void k_triples(GridDev g, TripleList L, int n, double *partials, doub
 
 // coulMom (scfUtils.F90:490-603) and exchMom (scfUtils.F90:615-844, with
 // the grid's weighted P_k^q r^k tables) of a batch of items (blockIdx.y =
-// item), each with its own kRedBlocks partial sums and ticket, so every
+// item), each with its own gridDim.x partial sums and ticket, so every
 // item's sum runs in a fixed order
 constexpr int kMomentItems = 64;
 struct MomentList {
@@ -1525,7 +1533,7 @@ __global__ void k_moments(GridDev g, const __grid_constant__ MomentList L, int h
         if (q < g.mpole) v[q] = fma(T[size_t(q) * g.mxsize + k], wk1, v[q]);
     }
   }
-  block_sum_finish<8>(v, partials + size_t(blockIdx.y) * kRedBlocks * 8, m.out, g.mpole, tickets + blockIdx.y);
+  block_sum_finish<8>(v, partials + size_t(blockIdx.y) * gridDim.x * 8, m.out, g.mpole, tickets + blockIdx.y);
 }
 
 // Checks narrow_f64 / widen_f32 against the hardware conversions on n
@@ -1577,7 +1585,7 @@ inline int grid_blocks(int n) {
 // ======================================================================
 
 static double *reduction_partials(x2g_ctx *ctx, int K) {
-  size_t need = size_t(kRedBlocks) * K * sizeof(double) + 64 * sizeof(double);
+  size_t need = size_t(kRedBlocksMax) * K * sizeof(double) + 64 * sizeof(double);
   if (ctx->red_bytes < need) {
     if (ctx->red) cudaFree(ctx->red);
     ctx->red = nullptr;
@@ -2001,7 +2009,7 @@ void launch_zero(x2g_ctx *ctx, double *p, size_t n) {
 
 void launch_norm(x2g_ctx *ctx, const GridDev &g, const double *psi, double *out) {
   double *part = reduction_partials(ctx, 1);
-  k_norm<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psi, part, out, ctx->bar + 3);
+  k_norm<<<red_blocks(g), kThreads, 0, ctx->stream>>>(g, psi, part, out, ctx->bar + 3);
   ctx->launches += 1;
 }
 
@@ -2012,7 +2020,7 @@ void launch_overlaps(x2g_ctx *ctx, const GridDev &g, const double *psi, const do
     const int m = (n - b < kMaxK) ? n - b : kMaxK;
     PtrList L{};
     for (int q = 0; q < m; ++q) L.p[q] = others[b + q];
-    k_overlaps<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psi, L, m, part, out + b, ctx->bar + 3);
+    k_overlaps<<<red_blocks(g), kThreads, 0, ctx->stream>>>(g, psi, L, m, part, out + b, ctx->bar + 3);
     ctx->launches += 1;
   }
 }
@@ -2020,13 +2028,14 @@ void launch_overlaps(x2g_ctx *ctx, const GridDev &g, const double *psi, const do
 void launch_eahf(x2g_ctx *ctx, const GridDev &g, const double *psi, int isym, int m, const double *coulp,
                  const double *exchp, double *ee_out, double *parts, bool exact) {
   double *part = reduction_partials(ctx, 5);
-  double *sums = part + size_t(kRedBlocks) * 5;
+  const int nb = red_blocks(g);
+  double *sums = part + size_t(nb) * 5;
   if (exact)
-    k_eahf<true><<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psi, isym, m, coulp, exchp, part, sums, ee_out, parts,
-                                                           ctx->bar + 3);
+    k_eahf<true><<<nb, kThreads, 0, ctx->stream>>>(g, psi, isym, m, coulp, exchp, part, sums, ee_out, parts,
+                                                   ctx->bar + 3);
   else
-    k_eahf<false><<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, psi, isym, m, coulp, exchp, part, sums, ee_out,
-                                                            parts, ctx->bar + 3);
+    k_eahf<false><<<nb, kThreads, 0, ctx->stream>>>(g, psi, isym, m, coulp, exchp, part, sums, ee_out, parts,
+                                                    ctx->bar + 3);
   ctx->launches += 1;
 }
 
@@ -2036,7 +2045,7 @@ void launch_triples(x2g_ctx *ctx, const GridDev &g, const TripleItem *items, int
     const int m = (n - b < kMaxK) ? n - b : kMaxK;
     TripleList L{};
     for (int q = 0; q < m; ++q) L.it[q] = items[b + q];
-    k_triples<<<kRedBlocks, kThreads, 0, ctx->stream>>>(g, L, m, part, out + b, ctx->bar + 3);
+    k_triples<<<red_blocks(g), kThreads, 0, ctx->stream>>>(g, L, m, part, out + b, ctx->bar + 3);
     ctx->launches += 1;
   }
 }
@@ -2047,7 +2056,7 @@ void launch_moments(x2g_ctx *ctx, const GridDev &g, const MomentItem *items, int
     double *part = reduction_partials(ctx, 8 * m);
     MomentList L{};
     for (int q = 0; q < m; ++q) L.it[q] = items[b + q];
-    k_moments<<<dim3(kRedBlocks, m), kThreads, 0, ctx->stream>>>(g, L, homo, part, ctx->bar + kMomentTickets);
+    k_moments<<<dim3(red_blocks(g), m), kThreads, 0, ctx->stream>>>(g, L, homo, part, ctx->bar + kMomentTickets);
     ctx->launches += 1;
   }
 }
