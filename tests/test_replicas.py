@@ -61,3 +61,4 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch):
     monkeypatch.setenv("RANK", "1")
     args = argparse.Namespace(workload="n2", warmup=3, steps=1, cpu_iters=1)
     assert bench.run_reference(args) is None
+
