@@ -1683,14 +1683,13 @@ static bool cluster_usable(x2g_ctx *ctx, const GridDev &g) {
 
 // Launch shape of the persistent-band sweep: the most jobs per launch (at
 // most `most`) and the shortest tile runs G for which every (job, run) gets
-// its own co-resident block (two 512-thread blocks fit an SM's registers;
-// shared memory per SM decides below that).  The function's shared memory
-// cap is raised once to the device's opt-in maximum, as for the cluster
-// kernel.
+// its own co-resident block at two 512-thread blocks per SM (the band's
+// shared memory must fit twice per SM).  The function's shared memory cap
+// is raised once to the device's opt-in maximum, as for the cluster kernel.
 static int persistent_shape(x2g_ctx *ctx, const GridDev &g, int most, int *nj, int *G, size_t *smem) {
   if (!ctx->band_attr) {
     // the cap counts dynamic bytes only: the opt-in maximum less the
-    // kernel's static shared memory (the grid barrier's flag)
+    // kernel's static shared memory (the neighbour wait's flag)
     int optin = 0;
     cudaFuncAttributes fa{};
     if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device) != cudaSuccess ||
