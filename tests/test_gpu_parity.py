@@ -122,11 +122,11 @@ def test_mixed_relaxation_tracks_fp64(ctx):
 
 
 @pytest.mark.parametrize("name", ["he_set01", "ne_set01", "h2_set01"])
-def test_mixed_on_chip_matches_grid_barrier_path(ctx, name):
-    """The cluster (distributed shared memory) FP32 sweep and the grid-barrier
-    FP32 sweep run the same schedule; the on-chip kernel multiplies by a
-    precomputed omega/lhs where the other divides, so they agree to FP32
-    rounding of the correction (the same bound as mixed vs FP64 above)."""
+def test_mixed_on_chip_matches_persistent_band_path(ctx, name):
+    """The cluster (distributed shared memory) FP32 sweep and the
+    persistent-band FP32 sweep run the same schedule on the same (residual,
+    omega/lhs) pairs, so they agree to FP32 rounding of the correction (the
+    same bound as mixed vs FP64 above)."""
     torch = pytest.importorskip("torch")
     deck = golden_deck(name)
     oc = Case(deck)
@@ -283,12 +283,12 @@ def test_initial_guess_lih_matches_oracle():
     _initial_functions_match(golden_deck("lih_set01"))
 
 
-def test_mixed_staged_sweep_scf_matches_on_chip():
+def test_mixed_persistent_sweep_scf_matches_on_chip():
     """KF on 241x301 in the mixed form, once with the cluster sweep and once
-    with the staged grid-barrier sweep (batches of 32 potentials run as runs
-    of several tiles per work item, single orbitals one tile per item): both
-    sweep the same schedule, so the SCF records agree to the FP32 rounding
-    of the corrections, far below the FP64 defect-corrected energies."""
+    with the persistent-band sweep (batches of 32 potentials in bands of
+    several tiles per block, single orbitals one tile per block): both sweep
+    the same schedule, so the SCF records agree to the FP32 rounding of the
+    corrections, far below the FP64 defect-corrected energies."""
     deck = _all_mcsor(_kf_small(golden_deck("kf_set01")))
     ctx = xg.Context(0)
     recs = []

@@ -157,7 +157,7 @@ struct x2g_ctx {
   long long h2d_bytes = 0, d2h_bytes = 0;  // host<->device bytes copied by the library
   long launches = 0;
   size_t cluster_smem_set = 0;  // dynamic shared memory granted to the cluster kernel
-  int no_cluster = 0;           // 1: mixed form uses the grid-barrier FP32 kernel
+  int no_cluster = 0;           // 1: mixed form uses the persistent-band FP32 kernel
   int cluster_nonportable = 0;  // cluster kernel allowed more than 8 CTAs
   long cluster_checked_key = -1;  // (shared bytes, cluster size) last checked
   int cluster_ok = 0;             // that cluster shape is schedulable here

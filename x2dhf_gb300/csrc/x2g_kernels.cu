@@ -1781,7 +1781,8 @@ static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, 
       ctx->pending.push_back(pe);
     }
   } else {
-    // persistent cooperative kernel with grid barriers
+    // persistent cooperative kernels: the FP64 sweep with grid barriers,
+    // the mixed form's persistent-band sweep with neighbour waits
     err = cudaMemsetAsync(ctx->bar, 0, 4 * sizeof(unsigned), ctx->stream);
     if (err != cudaSuccess) return cuda_status(err, "barrier reset");
     BarrierDev bar{ctx->bar, ctx->bar + 1, reinterpret_cast<int *>(ctx->bar + 2)};
