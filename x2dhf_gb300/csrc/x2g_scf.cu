@@ -276,8 +276,9 @@ int initial_guess(x2g_scf *s) {
       const int kk = s->k2[i1][i2];
       double *second = (i1 != i2 && s->m[i1] != 0 && s->m[i2] != 0) ? s->exch[2 * kk + 1] : nullptr;
       k_guess_exchange<<<blocks, 256, 0, st>>>(g, h.r, c.co1[i1 - 1], c.co2[i1 - 1], s->exch[2 * kk], second);
+      s->ctx->launches += 1;
     }
-  s->ctx->launches += 2 * s->norb;
+  s->ctx->launches += 2 * s->norb;  // orbitals and Coulomb potentials
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   return e == cudaSuccess ? X2G_OK : cuda_status(e, "initial guess");
