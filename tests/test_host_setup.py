@@ -180,3 +180,14 @@ def test_band_schedule_of_persistent_sweep(nnu, nmu):
             dn = [j for j in range(k + 1, len(runs)) if runs[j][0] < b + 4]
             assert up == list(range(k - len(up), k)) and dn == list(range(k + 1, k + 1 + len(dn)))
             assert len(up) <= 3 and len(dn) <= 3
+
+
+@pytest.mark.parametrize("nnu,nmu", [(0, 0), (5, 5), (31, 11), (11, 31)])
+def test_degenerate_grids_are_refused(nnu, nmu):
+    """Grids too small for the 8th-order stencil's 4-point margins and the
+    axis extrapolation are refused with a status code by every host-side
+    schedule builder (no exception escapes the C ABI, nothing is built)."""
+    for f in (xg.host_schedule, xg.host_band_schedule, xg.host_cluster_chunks):
+        with pytest.raises(xg.X2GError) as err:
+            f(nnu, nmu)
+        assert err.value.code == 6
