@@ -128,6 +128,16 @@ int x2g_host_cluster_chunks(int nnu, int nmu, int *nchunks, int *noff, int *chun
  * row ranges (ntiles values each).  Null arrays are skipped. */
 int x2g_host_band_schedule(int nnu, int nmu, int *npoints, int *ntiles, int *nlevels, int *pts, int *off, int *rows,
                            int *tile_row0, int *tile_row1);
+/* Longest time one block of a persistent sweep waits for the others (its
+ * grid barrier or its neighbours' phase counts) before the launch gives up:
+ * the block records X2G_ERR_TIMEOUT in the context's error word and every
+ * block returns, so a stalled launch never hangs the GPU.  The error word
+ * stays set, and later launches on the context leave at their first wait,
+ * until x2g_synchronize (or the call's own readback) reports it and clears
+ * it.  Default 2 s; 0 makes any wait that is not met at once fail (for
+ * testing the error path).  Applies to launches queued after the call.  The
+ * reference has no device waits (its threads join, src/c/mcsor_pthread.c:87). */
+int x2g_set_wait_limit(x2g_ctx *ctx, double seconds);
 /* Mixed form sweep path: 1 (default) on-chip cluster kernel where the grid
  * fits, 0 the persistent-band kernel. */
 int x2g_set_mixed_on_chip(x2g_ctx *ctx, int on);
@@ -177,8 +187,10 @@ int x2g_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, int 
  * the library (held by every GPU that loads it until the process exits),
  * looked up with cudaGetSymbolAddress on the first call on each device:
  * make that first call before any stream capture.  A batch needing more
- * than 32 MiB (256 B + 256 B-aligned job table + one nnu*nmu FP64
- * right-hand side per job) is rejected with X2G_ERR_ARG.  Every call shares
+ * than 32 MiB (256 B + a job table of 112 B per job rounded up to 256 B +
+ * one nnu*nmu FP64 right-hand side per job, each rounded up to 256 B) is
+ * rejected with X2G_ERR_ARG.  Batches above 32 jobs run as several launches;
+ * a device wait timeout in any of them is returned as X2G_ERR_TIMEOUT.  Every call shares
  * the array and the call returns only after its kernel has finished; calls
  * that overlap on the GPU (other threads, other contexts on the same
  * device) would race on the shared scratch and must be serialised by the
@@ -231,6 +243,17 @@ typedef struct {
   int start;                    /* 0: hydrogenic LCAO guess (orbpot hydrogen); 1: functions, moments and
                                    Lagrange multipliers loaded by the caller before the first run
                                    (orbpot old: x2g_scf_set_function, x2g_scf_set_start_values) */
+  /* relaxation scheme of the orbitals / the potentials (relaxDriver, doSCF.F90:943-1011):
+   * 1 MCSOR (the mcsor or mcsor-o card sets it for orbitals, mcsor-ce for
+   * potentials, inputInterface.F90:1910-2028), 0 list-order SOR (the
+   * reference's default, sormcsor.F90:20-132) */
+  int orb_scheme, pot_scheme;
+  /* 0: the reference's order, the potentials of orbital i relaxed just
+   * before orbital i (relaxDriver); 1: every Coulomb and exchange potential
+   * of an SCF iteration relaxed in one batched launch from the orbitals at
+   * the start of the iteration, then the orbitals in the reference's order.
+   * Same fixed point, different trajectory (no reference counterpart). */
+  int batch_potentials;
 } x2g_case;
 
 typedef struct {

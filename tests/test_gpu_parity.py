@@ -244,7 +244,7 @@ def _initial_functions_match(deck, rtol=1e-13):
     largest value."""
     oc = Case(deck)
     ctx = xg.Context(0)
-    s = xg.SCF(ctx, xg.parse_deck(deck))
+    s = xg.SCF(ctx, xg.parse_deck(_all_mcsor(deck)))
     m = [int(s.case.m[i]) for i in range(s.case.norb)]
     checked = 0
     for i in range(1, s.case.norb + 1):
@@ -341,4 +341,16 @@ def test_mixed_persistent_sweep_batches_track_fp64():
         change = np.abs(a).max()
         assert change > 0
         assert np.abs(a - b).max() <= 1e-5 * change
+    ctx.close()
+
+
+def test_sor_deck_is_refused_not_silently_relaxed_with_mcsor():
+    """A deck without the mcsor cards asks for the reference's list-order
+    SOR; the GPU SCF refuses it (X2G_ERR_UNSUPPORTED) instead of running
+    MCSOR in its place."""
+    ctx = xg.Context(0)
+    for deck in (golden_deck("h2_set01"), golden_deck("he_set02")):
+        with pytest.raises(xg.X2GError) as ei:
+            xg.SCF(ctx, xg.parse_deck(deck))
+        assert ei.value.code == 8 and "SOR" in str(ei.value)
     ctx.close()

@@ -191,3 +191,23 @@ def test_degenerate_grids_are_refused(nnu, nmu):
         with pytest.raises(xg.X2GError) as err:
             f(nnu, nmu)
         assert err.value.code == 6
+
+
+def test_parse_deck_relaxation_schemes_follow_the_cards():
+    """read_mcsor / read_mcsor_o / read_mcsor_ce (inputInterface.F90:
+    1910-2028): SOR by default; mcsor and mcsor-o select MCSOR for the
+    orbitals, mcsor-ce for the potentials, and a later mcsor card puts the
+    potentials back on SOR."""
+    def schemes(deck):
+        c = xg.parse_deck(deck)
+        return c.orb_scheme, c.pot_scheme
+
+    base = [ln for ln in golden_deck("h2_set01").splitlines() if ln.strip().lower() != "stop"]
+    assert schemes("\n".join(base + ["stop"])) == (0, 0)
+    assert schemes("\n".join(base + ["mcsor", "stop"])) == (1, 0)
+    assert schemes("\n".join(base + ["mcsor-o", "stop"])) == (1, 0)
+    assert schemes("\n".join(base + ["mcsor-ce", "stop"])) == (0, 1)
+    assert schemes("\n".join(base + ["mcsor", "mcsor-ce", "stop"])) == (1, 1)
+    assert schemes("\n".join(base + ["mcsor-ce", "mcsor", "stop"])) == (1, 0)
+    c = xg.parse_deck("\n".join(base + ["mcsor-ce 1 7", "stop"]))
+    assert c.maxsor_pot == 7

@@ -46,6 +46,7 @@ class Case(C.Structure):
         ("maxsor_orb", C.c_int), ("maxsor_pot", C.c_int),
         ("omega_orb", C.c_double), ("omega_pot", C.c_double), ("recalc_mm", C.c_double),
         ("mpole", C.c_int), ("homonuclear", C.c_int), ("precision", C.c_int), ("start", C.c_int),
+        ("orb_scheme", C.c_int), ("pot_scheme", C.c_int), ("batch_potentials", C.c_int),
     ]
 
 
@@ -74,7 +75,7 @@ EXPORTS = [
     "x2g_kernel_launches", "x2g_transfer_bytes", "mcsor_pthread_", "mcsor_tpool_", "coulExch_pthread_", "coulExch_tpool_",
     "tpoolStop4mcsor_", "tpoolStop4pots_", "x2g_host_table", "x2g_host_schedule", "x2g_profile",
     "x2g_relax_noalloc", "x2g_host_cluster_plan", "x2g_set_mixed_on_chip", "x2g_host_cluster_chunks", "x2g_host_band_schedule",
-    "x2g_convert_selftest",
+    "x2g_convert_selftest", "x2g_set_wait_limit",
 ]
 
 _lib = None
@@ -132,6 +133,7 @@ def lib():
     L.x2g_host_cluster_plan.argtypes = [I, I, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_long),
                                         C.POINTER(C.c_int)]
     L.x2g_set_mixed_on_chip.argtypes = [P, I]
+    L.x2g_set_wait_limit.argtypes = [P, D]
     L.x2g_kernel_launches.restype = C.c_long
     L.x2g_kernel_launches.argtypes = [P]
     L.x2g_transfer_bytes.argtypes = [P, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
@@ -157,12 +159,17 @@ def round_grid(n):
     return lib().x2g_round_grid(int(n))
 
 
-def parse_deck(text, precision=FP64):
-    """Parse a reference input deck into an x2g_case (closed-shell HF)."""
+def parse_deck(text, precision=FP64, batch_potentials=False):
+    """Parse a reference input deck into an x2g_case (closed-shell HF).
+
+    The relaxation schemes follow the deck's cards as in the reference: SOR
+    unless mcsor / mcsor-o (orbitals) or mcsor-ce (potentials) is given.
+    batch_potentials selects the batched potential mode (x2g_case)."""
     L = lib()
     c = Case()
     L.x2g_case_defaults(C.byref(c))
     c.precision = precision
+    c.batch_potentials = 1 if batch_potentials else 0
     lines = [ln.split("!")[0].replace(",", " ").split() for ln in text.splitlines()]
     lines = [[t.lower() for t in ln] for ln in lines if ln]
     i = 0
@@ -257,11 +264,23 @@ def parse_deck(text, precision=FP64):
             for name, x in zip(("nscf2skip", "nenlast", "nnolast"), v):
                 setattr(c, name, x)
         elif lab in ("mcsor", "mcsor-o"):
+            # read_mcsor / read_mcsor_o (inputInterface.F90:1910-1990): MCSOR
+            # for the orbitals; the mcsor card also puts the potentials back
+            # on SOR (lpotmcsor=.false.)
+            c.orb_scheme = 1
+            if lab == "mcsor":
+                c.pot_scheme = 0
             v = [int(x) for x in nums(ln[1:])]
             if len(v) > 1:
                 c.maxsor_orb = v[1]
             if lab == "mcsor" and len(v) > 2:
                 c.maxsor_pot = v[2]
+        elif lab == "mcsor-ce":
+            # read_mcsor_ce (inputInterface.F90:1992-2028): MCSOR for the potentials
+            c.pot_scheme = 1
+            v = [int(x) for x in nums(ln[1:])]
+            if len(v) > 1:
+                c.maxsor_pot = v[1]
         elif lab == "omega":
             v = nums(ln[1:])
             if v and abs(v[0]) > 0:
@@ -374,6 +393,11 @@ class Context:
         a, b = C.c_longlong(), C.c_longlong()
         _check(self.L.x2g_transfer_bytes(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def set_wait_limit(self, seconds):
+        """Longest device-side wait of a persistent sweep block before the
+        launch reports X2G_ERR_TIMEOUT (default 2 s; 0 fails any wait)."""
+        _check(self.L.x2g_set_wait_limit(self.h, float(seconds)))
 
     def set_mixed_on_chip(self, on):
         _check(self.L.x2g_set_mixed_on_chip(self.h, 1 if on else 0))

@@ -175,6 +175,12 @@ int x2g_convert_selftest(x2g_ctx *c, long n, unsigned long long seed, unsigned l
   return convert_selftest(c, n, seed, mismatches);
 }
 
+int x2g_set_wait_limit(x2g_ctx *c, double seconds) {
+  if (!c || !(seconds >= 0.0) || seconds > 3600.0) return set_status(X2G_ERR_ARG, "wait limit must be in [0, 3600] s");
+  c->wait_limit_ns = (unsigned long long)(seconds * 1e9);
+  return set_status(X2G_OK, "");
+}
+
 int x2g_set_mixed_on_chip(x2g_ctx *c, int on) {
   if (!c) return set_status(X2G_ERR_ARG, "null context");
   c->no_cluster = on ? 0 : 1;

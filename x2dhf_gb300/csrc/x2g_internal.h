@@ -133,12 +133,18 @@ struct JobTable {
   JobDev j[kParamJobs];
 };
 
-// Grid barrier state in device memory.
+// Grid barrier state in device memory.  The error word is sticky: a
+// launch that finds it set leaves at its first wait, and only the host's
+// readback (x2g_synchronize) clears it, so an error of one launch of a
+// multi-launch call survives the launches after it.
 struct BarrierDev {
   unsigned int *count;
   unsigned int *gen;
-  int *err;  // first error code (0 = none), phase where it happened
+  int *err;                     // first error code (0 = none)
+  unsigned long long limit_ns;  // longest wait of one block; 0: a wait not met at its first check fails
 };
+
+constexpr unsigned long long kDefaultWaitLimitNs = 2000000000ull;  // 2 s
 
 }  // namespace x2g
 
@@ -165,6 +171,8 @@ struct x2g_ctx {
   long band_key = -1;           // shared bytes of its last occupancy query
   int band_blocks = 0;          // co-resident blocks for that size
   int band_sm_smem = 0;         // shared memory per SM
+  int f64_blocks = -1;          // co-resident blocks of the cooperative FP64 sweep on this device
+  unsigned long long wait_limit_ns = x2g::kDefaultWaitLimitNs;  // device-side wait limit (x2g_set_wait_limit)
   // optional per-launch timing of the sweep kernels (CUDA events on stream)
   int profiling = 0;
   struct Pending {

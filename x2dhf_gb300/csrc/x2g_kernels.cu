@@ -19,7 +19,6 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kBandThreads = 512;
-constexpr unsigned long long kBarrierTimeoutNs = 2000000000ull;  // 2 s
 
 __device__ __forceinline__ double A(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double S(double a, double b) { return __dsub_rn(a, b); }
@@ -37,9 +36,16 @@ __device__ __forceinline__ unsigned long long globaltimer() {
   return t;
 }
 
+// Whether a wait that started at t0 has run out: checked every 256 spins,
+// or at every spin when the limit is 0 (a wait not met at once fails).
+__device__ __forceinline__ bool wait_expired(const BarrierDev &b, unsigned spins, unsigned long long t0) {
+  return (b.limit_ns == 0 || (spins & 255u) == 0) && globaltimer() - t0 >= b.limit_ns;
+}
+
 // Grid-wide barrier for a cooperative launch.  Every wait is bounded: after
-// kBarrierTimeoutNs the block records X2G_ERR_TIMEOUT and all blocks leave
-// the kernel at their next barrier.  Returns false when the kernel must stop.
+// b.limit_ns the block records X2G_ERR_TIMEOUT and all blocks leave the
+// kernel at their next barrier; a launch that finds the error word already
+// set leaves at its first barrier.  Returns false when the kernel must stop.
 __device__ bool grid_barrier(const BarrierDev &b, unsigned nblocks) {
   __shared__ int s_ok;
   __syncthreads();
@@ -62,7 +68,7 @@ __device__ bool grid_barrier(const BarrierDev &b, unsigned nblocks) {
           ok = 0;
           break;
         }
-        if ((++spins & 255u) == 0 && globaltimer() - t0 > kBarrierTimeoutNs) {
+        if (wait_expired(b, ++spins, t0)) {
           atomicCAS(b.err, 0, X2G_ERR_TIMEOUT);
           ok = 0;
           break;
@@ -88,8 +94,9 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
 // phase[b] how many colour phases it has finished (release store after its
 // writes), and before reloading its halos for phase k waits until every
 // block whose rows lie within 4 rows of its band (nb[0..5], -1 = none) has
-// finished k phases (acquire loads by lanes 0..5 of warp 0).  The wait is
-// bounded as in grid_barrier.
+// finished k phases (acquire loads by lanes 0..5 of warp 0), while lane 6
+// reads the error word once, so that a launch started after an error leaves
+// at its first wait.  The wait is bounded as in grid_barrier.
 __device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -97,16 +104,18 @@ __device__ bool wait_neighbours(const BarrierDev &b, const unsigned *phase, int 
   __shared__ int s_ok;
   if (threadIdx.x < 32) {
     int ok = 1;
-    if (nbq >= 0) {
+    volatile int *verr = b.err;
+    if (threadIdx.x == 6) {
+      if (*verr) ok = 0;
+    } else if (nbq >= 0) {
       const unsigned long long t0 = globaltimer();
       unsigned spins = 0;
-      volatile int *verr = b.err;
       while (ld_acquire(phase + size_t(nbq) * kPhaseStride) < k) {
         if (*verr) {
           ok = 0;
           break;
         }
-        if ((++spins & 255u) == 0 && globaltimer() - t0 > kBarrierTimeoutNs) {
+        if (wait_expired(b, ++spins, t0)) {
           atomicCAS(b.err, 0, X2G_ERR_TIMEOUT);
           ok = 0;
           break;
@@ -1735,6 +1744,18 @@ static int persistent_shape(x2g_ctx *ctx, const GridDev &g, int most, int *nj, i
   return set_status(X2G_ERR_ARG, "grid too large for the persistent FP32 sweep");
 }
 
+// Co-resident blocks of the cooperative FP64 sweep on the context's device
+// (asked once per context).
+static int f64_block_limit(x2g_ctx *ctx) {
+  if (ctx->f64_blocks > 0) return X2G_OK;
+  int per_sm = 0;
+  cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k_mcsor_f64, kThreads, 0);
+  if (err != cudaSuccess) return cuda_status(err, "occupancy query");
+  if (per_sm < 1) return set_status(X2G_ERR_CUDA, "cooperative FP64 sweep cannot be resident");
+  ctx->f64_blocks = per_sm * ctx->num_sms;
+  return X2G_OK;
+}
+
 // One launch batch (at most kParamJobs jobs) of launch_relax.
 static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, int nsweeps, bool mixed,
                        bool on_chip, int G, size_t smem) {
@@ -1782,10 +1803,12 @@ static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, 
     }
   } else {
     // persistent cooperative kernels: the FP64 sweep with grid barriers,
-    // the mixed form's persistent-band sweep with neighbour waits
-    err = cudaMemsetAsync(ctx->bar, 0, 4 * sizeof(unsigned), ctx->stream);
+    // the mixed form's persistent-band sweep with neighbour waits.  Only the
+    // arrival count and generation are reset: the error word keeps an
+    // earlier launch's timeout until x2g_synchronize reports it
+    err = cudaMemsetAsync(ctx->bar, 0, 2 * sizeof(unsigned), ctx->stream);
     if (err != cudaSuccess) return cuda_status(err, "barrier reset");
-    BarrierDev bar{ctx->bar, ctx->bar + 1, reinterpret_cast<int *>(ctx->bar + 2)};
+    BarrierDev bar{ctx->bar, ctx->bar + 1, reinterpret_cast<int *>(ctx->bar + 2), ctx->wait_limit_ns};
     int nj = njobs, ns = nsweeps;
     GridDev gd = g;
     if (mixed) {
@@ -1800,15 +1823,10 @@ static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, 
       err = cudaLaunchCooperativeKernel((const void *)k_mcsor_f32p, dim3(nb), dim3(kBandThreads), args, smem,
                                         ctx->stream);
     } else {
-      static int max_f64 = -1;
-      if (max_f64 < 0) {
-        int per_sm = 0;
-        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k_mcsor_f64, kThreads, 0);
-        if (err != cudaSuccess) return cuda_status(err, "occupancy query");
-        max_f64 = per_sm * ctx->num_sms;
-      }
+      int rc = f64_block_limit(ctx);
+      if (rc) return rc;
       const int nitems = njobs * g.ntiles;
-      unsigned nblocks = unsigned(nitems < max_f64 ? nitems : max_f64);
+      unsigned nblocks = unsigned(nitems < ctx->f64_blocks ? nitems : ctx->f64_blocks);
       if (nblocks < 1) nblocks = 1;
       void *args[] = {&gd, &jt, &nj, &ns, &bar, &nblocks};
       err = cudaLaunchCooperativeKernel((const void *)k_mcsor_f64, dim3(nblocks), dim3(kThreads), args, 0,
@@ -1872,7 +1890,9 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
 
 // Scratch layout of launch_relax_in_scratch: 4 barrier words, a reserved
 // region the size of a job table, then one plain right-hand-side buffer per
-// job (256-byte aligned).
+// job (256-byte aligned).  The job-table size is part of the documented
+// limit of x2g_relax_noalloc.
+static_assert(sizeof(JobDev) == 112, "x2g_relax_noalloc documents 112-byte job-table entries");
 size_t relax_scratch_bytes(const GridDev &g, int njobs) {
   const size_t head = 256;
   const size_t table = (sizeof(JobDev) * size_t(njobs) + 255) / 256 * 256;
@@ -1890,20 +1910,32 @@ int launch_relax_in_scratch(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, i
   unsigned *barw = reinterpret_cast<unsigned *>(base);
   char *rhs0 = base + 256 + (sizeof(JobDev) * size_t(njobs) + 255) / 256 * 256;
   const size_t plain = (size_t(g.mxsize) * sizeof(double) + 255) / 256 * 256;
-  int per_sm = 0;
-  cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k_mcsor_f64, kThreads, 0);
-  if (err != cudaSuccess) return cuda_status(err, "occupancy query");
+  for (int b0 = 0; b0 < njobs; b0 += kParamJobs) {
+    const int nb = (njobs - b0 < kParamJobs) ? njobs - b0 : kParamJobs;
+    JobTable jt{};
+    for (int i = 0; i < nb; ++i)
+      if (!make_job(jobs[b0 + i], jt.j[i])) return set_status(X2G_ERR_ARG, "bad relaxation job");
+  }
+  int rc = f64_block_limit(ctx);
+  if (rc) return rc;
+  // the error word is cleared once per call; between launches only the
+  // arrival count and generation, so that a timeout of one launch is still
+  // there when the caller reads it after the last
+  cudaError_t err = cudaMemsetAsync(barw, 0, 4 * sizeof(unsigned), ctx->stream);
+  if (err != cudaSuccess) return cuda_status(err, "scratch barrier reset");
   for (int b0 = 0; b0 < njobs; b0 += kParamJobs) {
     const int nb = (njobs - b0 < kParamJobs) ? njobs - b0 : kParamJobs;
     JobTable jt{};
     for (int i = 0; i < nb; ++i) {
-      if (!make_job(jobs[b0 + i], jt.j[i])) return set_status(X2G_ERR_ARG, "bad relaxation job");
+      make_job(jobs[b0 + i], jt.j[i]);
       jt.j[i].rhs_buf = reinterpret_cast<double *>(rhs0 + plain * size_t(b0 + i));
     }
-    err = cudaMemsetAsync(barw, 0, 4 * sizeof(unsigned), ctx->stream);
-    if (err != cudaSuccess) return cuda_status(err, "scratch barrier reset");
-    BarrierDev bar{barw, barw + 1, reinterpret_cast<int *>(barw + 2)};
-    const int nitems = nb * g.ntiles, cap = per_sm * ctx->num_sms;
+    if (b0 > 0) {
+      err = cudaMemsetAsync(barw, 0, 2 * sizeof(unsigned), ctx->stream);
+      if (err != cudaSuccess) return cuda_status(err, "scratch barrier reset");
+    }
+    BarrierDev bar{barw, barw + 1, reinterpret_cast<int *>(barw + 2), ctx->wait_limit_ns};
+    const int nitems = nb * g.ntiles, cap = ctx->f64_blocks;
     unsigned nblocks = unsigned(nitems < cap ? nitems : cap);
     if (nblocks < 1) nblocks = 1;
     int nj = nb, ns = nsweeps;

@@ -829,6 +829,11 @@ int x2g_scf_create(x2g_ctx *ctx, const x2g_case *c, x2g_scf **out) {
       return set_status(X2G_ERR_UNSUPPORTED, "open-shell configurations with several orbitals are not supported");
   }
   if (c->precision != X2G_FP64 && c->precision != X2G_MIXED) return set_status(X2G_ERR_ARG, "unknown precision");
+  if (c->orb_scheme != 1 || c->pot_scheme != 1)
+    return set_status(X2G_ERR_UNSUPPORTED,
+                      "list-order SOR (a deck without the mcsor-o/mcsor and mcsor-ce cards) is not available on the "
+                      "GPU: set orb_scheme = pot_scheme = 1 (MCSOR)");
+  if (c->batch_potentials != 0 && c->batch_potentials != 1) return set_status(X2G_ERR_ARG, "bad batch_potentials");
   if (c->maxsor_orb < 1 || c->maxsor_pot < 1) return set_status(X2G_ERR_ARG, "sweep counts must be positive");
   auto *s = new x2g_scf();
   s->ctx = ctx;
