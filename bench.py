@@ -20,6 +20,7 @@ import argparse
 import faulthandler
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -199,20 +200,41 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def workload_config(name, case=None):
-    """The `config` of a workload's JSON line, shared by both arms."""
-    out = {"workload": f"{name}: " + WORKLOAD_TEXT[name],
-           "convergence": "orbital-energy change < 1e-12 for 4 consecutive SCF iterations",
-           "parallelism": "replicas only (independent SCF solves per GPU)"}
-    try:
-        import x2dhf_gb300 as xg
+def round_grid(n):
+    """The reference's grid rounding (nnucalc/nmucalc, src/inputInterface.F90:
+    2961-3095): n = 1 (mod 6) and n - 6 = 0 (mod 5) enforced alternately,
+    always rounding down.  Plain Python, so that the reference arm loads
+    nothing of this repository's GPU library."""
+    if n < 7:
+        return 0
+    while True:
+        while (n - 1) % 6 != 0:
+            n -= 1
+        nt = n
+        while ((n - 6) // 5) * 5 != n - 6:
+            n -= 1
+        if n > 1 and n != nt:
+            continue
+        return n
 
-        c = case if case is not None else xg.parse_deck(WORKLOADS[name]())
-        out["grid"] = [c.nnu, c.nmu]
-        out["points_per_sweep"] = (c.nnu - 2) * (c.nmu - 5)
-    except Exception:  # the reference arm may run without the library built
-        pass
-    return out
+
+def deck_grid(deck):
+    """(N_nu, N_mu) of a deck whose grid card gives both counts, rounded."""
+    for ln in deck.splitlines():
+        t = ln.split("!")[0].split()
+        if t and t[0].lower() == "grid":
+            return round_grid(int(t[1])), round_grid(int(float(t[2])))
+    raise ValueError("deck has no grid card")
+
+
+def workload_config(name):
+    """The `config` of a workload's JSON line, identical in both arms."""
+    nnu, nmu = deck_grid(WORKLOADS[name]())
+    return {"workload": f"{name}: " + WORKLOAD_TEXT[name],
+            "convergence": "orbital-energy change < 1e-12 for 4 consecutive SCF iterations",
+            "parallelism": "replicas only (independent SCF solves per GPU)",
+            "grid": [nnu, nmu], "points_per_sweep": (nnu - 2) * (nmu - 5),
+            "l2": "GPU arm: 512 MiB buffer written between timed steps (L2 flushed); CPU arm: host caches as they are"}
 
 
 def max_over_ranks(values, world, device):
@@ -297,20 +319,27 @@ def run_gpu(args):
     lat64, res64, it64, ms64, pts64, n64 = [1.0], None, [], 0.0, 0.0, 0
     latmx, resmx, itmx, msmx, ptsmx, nmx, launches_mx = [1.0], None, [], 0.0, 0.0, 0, 0
     late2e = [1.0]
+    ctx.profile(0, xg.FP64)  # the timed steps run without the library's per-launch events
     with sampler:
         if run64:
-            ctx.profile(2, xg.FP64)
             lat64, res64, it64 = timed_solves(xg.FP64, args.steps, args.warmup)
-            ms64, pts64, n64 = ctx.profile(-1, xg.FP64)
         if runmx:
-            ctx.profile(2, xg.MIXED)
             l0 = ctx.launches
             # launches of the timed mixed solves (the warm-up ones counted out)
             latmx, resmx, itmx = timed_solves(xg.MIXED, args.steps, args.warmup)
             launches_mx = int((ctx.launches - l0) * args.steps / (args.steps + args.warmup))
-            msmx, ptsmx, nmx = ctx.profile(-1, xg.MIXED)
-            ctx.profile(0, xg.FP64)
             late2e, rese2e, _ = timed_solves(xg.MIXED, max(1, args.steps // 2), 1, e2e=True)
+    # roofline figures: one more step of each form with the library's
+    # per-launch CUDA events on (recorded on its own stream), not timed
+    if runmx:
+        ctx.profile(2, xg.MIXED)
+        timed_solves(xg.MIXED, 1, 0)
+        msmx, ptsmx, nmx = ctx.profile(-1, xg.MIXED)
+    if run64:
+        ctx.profile(2, xg.FP64)
+        timed_solves(xg.FP64, 1, 0)
+        ms64, pts64, n64 = ctx.profile(-1, xg.FP64)
+    ctx.profile(0, xg.FP64)
     # max over ranks: the slowest replica sets the pace
     tot64, totmx, tote2e = max_over_ranks([sum(lat64), sum(latmx), sum(late2e)], world, f"cuda:{local}")
     if rank != 0:
@@ -351,8 +380,7 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "f32 sweeps + f64 defect correction (value); f64 (fp64 leg)",
         "data": "synthetic: hydrogenic LCAO start of the reference's own input deck, no dataset",
-        "config": dict(workload_config(args.workload, c),
-                       l2="512 MiB buffer written between timed solves (L2 flushed)"),
+        "config": workload_config(args.workload),
         "latency_s": {"p50": statistics.median(latmx), "p99": p99,
                       "fp64_p50": statistics.median(lat64) if run64 else None},
         "fp64": {"value": fp64_value if run64 else None, "unit": unit, "iterations": it64,
@@ -394,10 +422,10 @@ def run_gpu(args):
         "clocks": sampler.summary(),
     }
     if not args.no_cpu_baseline:
-        if args.workload in FIXED_ITERS:
-            out["cpu_baseline"] = cpu_baseline_iterations(deck, min(args.cpu_iters, 4))
-        else:
-            out["cpu_baseline"] = cpu_baseline(deck, REF_ITERATIONS[args.workload], args.cpu_iters)
+        nthreads = min(16, os.cpu_count() or 1)
+        out["cpu_baseline"] = cpu_baseline(args.workload, deck,
+                                           min(args.cpu_iters, 4) if args.workload in FIXED_ITERS else args.cpu_iters,
+                                           nthreads)
     return out
 
 
@@ -503,19 +531,23 @@ def C_double_pair(xg, nnu, nmu):
     return a.value, b.value
 
 
-# SCF iterations of a full solve by the reference algorithm: the
-# reference's own C relaxation kernels (MCSOR potentials through sorpt_ on
-# the colour lists, orbitals through mcsor_pthread_ on 8 threads) under the
-# oracle's SCF driver, run to its convergence exit on an x86 host.  The
-# multi-threaded reference MCSOR races at the colour seams, so another run
-# can stop a few iterations apart.
-REF_ITERATIONS = {"n2": 973, "h2": 313}
+# Full solves by the reference's own C relaxation kernels under the
+# oracle's SCF driver, written by oracle/ref_solves.py: the iteration count
+# that scales a bounded sample of SCF iterations to one solve
+REF_SOLVES = os.path.join(ROOT, "oracle", "ref_solves.json")
+# workloads whose full solve on the host cores fits one bench step
+REF_FULL_SOLVE = {"h2"}
+
+
+def ref_solve_record(name):
+    with open(REF_SOLVES) as f:
+        return json.load(f)[name]
 
 
 def _ref_backend(deck, nthreads):
     """The reference's own C relaxation backend (oracle/_ref, built from the
-    x2dhf sources) under the oracle's SCF driver; falls back to the oracle
-    port when the reference sources could not be built."""
+    x2dhf sources) under the oracle's SCF driver; the oracle port when the
+    reference sources could not be built."""
     from oracle import pyoracle, pyref
 
     pyoracle.build()
@@ -525,7 +557,8 @@ def _ref_backend(deck, nthreads):
 
 
 def cpu_sample(deck, sample_iters, nthreads):
-    """prepSCF + 1 iteration, then `sample_iters` timed SCF iterations."""
+    """prepSCF + 1 iteration, then `sample_iters` timed SCF iterations:
+    (setup seconds, seconds per iteration, backend kind)."""
     t0 = time.perf_counter()
     c, kind = _ref_backend(deck, nthreads)
     c.steps(1)
@@ -535,74 +568,159 @@ def cpu_sample(deck, sample_iters, nthreads):
     return (t1 - t0), (t2 - t1) / sample_iters, kind
 
 
-def cpu_baseline(deck, iterations_per_solve, sample_iters):
-    """The reference's C relaxation kernels (coulExch_pthread_ one thread per
-    potential, mcsor_pthread_ on all host cores) under the oracle's SCF
-    driver, on a bounded sample of SCF iterations of the same case,
-    extrapolated with the solve's iteration count."""
-    nthreads = min(16, os.cpu_count() or 1)
-    setup, per_iter, kind = cpu_sample(deck, sample_iters, nthreads)
-    solve_s = setup + per_iter * max(0, iterations_per_solve - 1)
-    return {"value": 1.0 / solve_s, "unit": UNIT, "cores": nthreads, "kind": kind,
-            "sample": f"setup + prepSCF + 1 iteration ({setup:.2f} s), then {sample_iters} SCF iterations "
-                      f"({per_iter:.3f} s/iteration) on {nthreads} threads; extrapolated to "
-                      f"{iterations_per_solve} iterations/solve"}
+def cpu_full_solve(deck, nthreads):
+    """One full SCF solve to the driver's convergence exit: (seconds, iterations, kind)."""
+    t0 = time.perf_counter()
+    c, kind = _ref_backend(deck, nthreads)
+    c.steps(1 << 30)
+    recs = c.records()
+    return time.perf_counter() - t0, (recs[-1][0] if recs else 0), kind
 
 
-def cpu_baseline_iterations(deck, sample_iters):
-    """SCF iterations/s of the reference's C relaxation kernels under the
-    oracle's SCF driver, on a bounded sample of iterations of the same case."""
-    nthreads = min(16, os.cpu_count() or 1)
-    setup, per_iter, kind = cpu_sample(deck, sample_iters, nthreads)
-    return {"value": 1.0 / per_iter, "unit": "SCF iterations/s", "cores": nthreads, "kind": kind,
-            "sample": f"setup + prepSCF + 1 iteration ({setup:.2f} s), then {sample_iters} SCF iterations "
-                      f"({per_iter:.3f} s/iteration) on {nthreads} threads"}
+def host_cpu():
+    model = platform.processor() or platform.machine()
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith(("model name", "cpu part")):
+                    model = ln.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    return {"nproc": os.cpu_count(), "model": model, "machine": platform.machine()}
+
+
+def cpu_kernel_rates(names, max_threads, reps=3):
+    """Sweeps/s of the reference's own C kernels on each workload's grid
+    (survey measurement plan): sorpt_ on one thread over the "middle" list
+    (list-order SOR of a potential, src/c/sorpt.c:11-121) and on the colour
+    lists, and mcsor_pthread_ (src/c/mcsor_pthread.c:32) on 1, 2, 4, ...
+    threads for an orbital.  One call is maxsor2 = 10 sweeps."""
+    import numpy as np
+    from oracle import pyoracle, pyref
+
+    pyoracle.build()
+    if not pyref.available():
+        return None
+    out = []
+    for name in names:
+        oc = pyoracle.Case(WORKLOADS[name]())
+        rk = pyref.RefKernels(oc)
+        npts = (oc.nni - 2) * (oc.nmu - 5)
+        f1, f2 = oc.fock(1)
+        lhs_o, rhs_o = f1 + oc.coeffs()[5], f2
+        u_o = oc.putin(1, oc.orbital(1))
+        in1, in2, idel, isym = oc.pot_info(1, 1)
+        lhs_p = oc.suppl(7)
+        rhs_p = oc.orbital(in1) * oc.orbital(in2) * oc.suppl(9)
+        u_p = oc.putin(isym, oc.pot(1, 1))
+        oo, op = oc.omega()
+
+        def rate(fn):
+            fn()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                fn()
+            return 10 * reps / (time.perf_counter() - t0)
+
+        row = {"workload": name, "grid": [oc.nni, oc.nmu], "points_per_sweep": npts,
+               "sorpt_sor_1t_sweeps_per_s": rate(lambda: rk.sorpt(isym, op, u_p, lhs_p, rhs_p, False)),
+               "sorpt_colour_1t_sweeps_per_s": rate(lambda: rk.sorpt(isym, op, u_p, lhs_p, rhs_p, True)),
+               "mcsor_pthread_sweeps_per_s": {}}
+        t = 1
+        while t <= max_threads:
+            row["mcsor_pthread_sweeps_per_s"][str(t)] = rate(lambda: rk.mcsor(1, t, oo, u_o, lhs_o, rhs_o))
+            t *= 2
+        best = max(row["mcsor_pthread_sweeps_per_s"].values())
+        row["best_point_updates_per_s"] = best * npts
+        out.append(row)
+        del rk, oc
+    return out
+
+
+CPU_KERNEL_GRIDS = ("h2", "n2", "kf")
+
+
+def cpu_baseline(name, deck, sample_iters, nthreads, kernels=True):
+    """The reference's C relaxation kernels (one thread per potential,
+    mcsor_pthread_ on `nthreads` threads) under the oracle's SCF driver on a
+    bounded sample of the same workload, plus the per-kernel sweep rates."""
+    if name in FIXED_ITERS:
+        setup, per_iter, kind = cpu_sample(deck, sample_iters, nthreads)
+        out = {"value": 1.0 / per_iter, "unit": "SCF iterations/s", "cores": nthreads, "kind": kind,
+               "sample": f"setup + prepSCF + 1 iteration ({setup:.2f} s), then {sample_iters} timed SCF "
+                         f"iterations ({per_iter:.3f} s/iteration) on {nthreads} threads"}
+    elif name in REF_FULL_SOLVE:
+        wall, iters, kind = cpu_full_solve(deck, nthreads)
+        out = {"value": 1.0 / wall, "unit": UNIT, "cores": nthreads, "kind": kind,
+               "sample": f"one full SCF solve ({iters} iterations, {wall:.2f} s) on {nthreads} threads"}
+    else:
+        rec = ref_solve_record(name)
+        setup, per_iter, kind = cpu_sample(deck, sample_iters, nthreads)
+        solve_s = setup + per_iter * (rec["iterations"] - 1)
+        out = {"value": 1.0 / solve_s, "unit": UNIT, "cores": nthreads, "kind": kind,
+               "sample": f"setup + prepSCF + 1 iteration ({setup:.2f} s), then {sample_iters} SCF iterations "
+                         f"({per_iter:.3f} s/iteration) on {nthreads} threads; scaled to the "
+                         f"{rec['iterations']} iterations of a full reference solve (oracle/ref_solves.json)",
+               "extrapolated": True}
+    out["host"] = host_cpu()
+    if kernels:
+        out["kernels"] = cpu_kernel_rates(CPU_KERNEL_GRIDS, nthreads)
+    return out
 
 
 def run_reference(args):
+    """The reference's own CPU implementation of the path on the host cores,
+    on the GPU arm's workload, metric, unit and config.  A step is one full
+    SCF solve where that fits (h2), else a bounded sample of SCF iterations
+    whose rate is scaled to one solve by the iteration count of a full
+    reference solve (oracle/ref_solves.json); ms_per_step is always the
+    time the step actually took."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return None
-    deck = WORKLOADS[args.workload]()
+    name = args.workload
+    deck = WORKLOADS[name]()
     nthreads = min(16, os.cpu_count() or 1)
-    if args.workload in FIXED_ITERS:
-        n = FIXED_ITERS[args.workload]
-        rates, kind = [], "port"
-        for step in range(args.warmup + args.steps):
-            setup, per_iter, kind = cpu_sample(deck, min(args.cpu_iters, 4), nthreads)
-            if step >= args.warmup:
-                rates.append(1.0 / per_iter)
-        v = statistics.median(rates)
-        unit = "SCF iterations/s"
-        return {
-            "metric": f"SCF iterations/s over the first {n} iterations: mixed vs FP64 MCSOR, 1 GB300", "value": v,
-            "unit": unit, "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / v,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic: hydrogenic LCAO start of the reference's input", "impl": "reference",
-            "config": dict(workload_config(args.workload), iterations_per_step=n),
-            "cpu_baseline": {"value": v, "unit": unit, "cores": nthreads, "kind": kind,
-                             "sample": f"per step: setup + prepSCF + 1 iteration, then {min(args.cpu_iters, 4)} "
-                                       f"timed SCF iterations on {nthreads} threads"},
-            "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        }
-    iters = REF_ITERATIONS[args.workload]
-    lat, kind = [], "port"
+    walls, vals, kind, note = [], [], "port", ""
     for step in range(args.warmup + args.steps):
-        setup, per_iter, kind = cpu_sample(deck, args.cpu_iters, nthreads)
+        t0 = time.perf_counter()
+        if name in FIXED_ITERS:
+            setup, per_iter, kind = cpu_sample(deck, min(args.cpu_iters, 4), nthreads)
+            v = 1.0 / per_iter
+            note = (f"per step: setup + prepSCF + 1 iteration, then {min(args.cpu_iters, 4)} timed SCF iterations "
+                    f"on {nthreads} threads")
+        elif name in REF_FULL_SOLVE:
+            wall, iters, kind = cpu_full_solve(deck, nthreads)
+            v = 1.0 / wall
+            note = f"per step: one full SCF solve ({iters} iterations) on {nthreads} threads"
+        else:
+            rec = ref_solve_record(name)
+            setup, per_iter, kind = cpu_sample(deck, args.cpu_iters, nthreads)
+            v = 1.0 / (setup + per_iter * (rec["iterations"] - 1))
+            note = (f"per step: setup + prepSCF + {1 + args.cpu_iters} SCF iterations on {nthreads} threads; the "
+                    f"solve rate scales the timed iterations to the {rec['iterations']} iterations of a full "
+                    f"reference solve (oracle/ref_solves.json)")
         if step >= args.warmup:
-            lat.append(setup + per_iter * (iters - 1))
-    solve_s = statistics.median(lat)
-    v = 1.0 / solve_s
-    return {
-        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * solve_s, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic: hydrogenic LCAO start of the reference's input", "impl": "reference",
-        "config": dict(workload_config(args.workload), iterations_per_solve=iters),
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": kind,
-                         "sample": f"per step: setup + prepSCF + {1 + args.cpu_iters} SCF iterations on "
-                                   f"{nthreads} threads, extrapolated to {iters} iterations/solve"},
-        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            walls.append(time.perf_counter() - t0)
+            vals.append(v)
+    unit = "SCF iterations/s" if name in FIXED_ITERS else UNIT
+    metric = (f"SCF iterations/s over the first {FIXED_ITERS[name]} iterations: mixed vs FP64 MCSOR, 1 GB300"
+              if name in FIXED_ITERS else METRIC)
+    value = (args.steps / sum(walls)) if name in REF_FULL_SOLVE else statistics.median(vals)
+    out = {
+        "metric": metric, "value": value, "unit": unit, "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(walls) / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic: hydrogenic LCAO start of the reference's input",
+        "impl": "reference", "config": workload_config(name),
+        "cpu_baseline": {"value": value, "unit": unit, "cores": nthreads, "kind": kind, "sample": note,
+                         "host": host_cpu()},
+        "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if name not in FIXED_ITERS and name not in REF_FULL_SOLVE:
+        out["extrapolated"] = {"from": "timed SCF iterations of each step", "iterations_per_solve":
+                               ref_solve_record(name)["iterations"], "source": "oracle/ref_solves.json"}
+    return out
 
 
 def main():

@@ -13,9 +13,13 @@
 # (coulExch_pthread_ / relax_single_pot_pthread_, which writes past a stack
 # array at relax_single_pot_pthread.c:47) is linked but not called: the
 # shim's x2r_coulexch drives sorpt_ one thread per potential.
+#
+# Usage: build_ref.sh [x2dhf-tree]; the tree defaults to $X2DHF_REF, else to
+# the read-only mount where this build environment provides the reference.
+# Without a tree the previously staged sources are compiled.
 set -e
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${X2DHF_REF:-/root/reference}"
+REF="${1:-${X2DHF_REF:-/root/reference}}"
 OUT="$HERE/_ref"
 mkdir -p "$OUT/src"
 FILES="sorpt.c sorpt.h params.h mcsor_pthread.c mcsor_single_colour_pthread.c coulExch_pthread.c relax_single_pot_pthread.c"

@@ -1,7 +1,7 @@
 """Extract the reference's own golden vectors for the (MC)SOR/SCF path.
 
 Reads test-sets/<system>/set-NN/{input.data,reference.lst} from an x2dhf
-checkout (default /root/reference) and writes, per case, the input deck and a
+checkout (its root is the required first argument) and writes, per case, the input deck and a
 JSON file with every per-iteration orbital-energy line (scf iteration,
 orbital label, orbital energy, energy difference, 1-norm), the final total
 energy and the (MC)SOR sweep count printed by the reference program.
@@ -58,7 +58,9 @@ def extract(lst):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        raise SystemExit("usage: make_golden.py <x2dhf source tree>")
+    root = sys.argv[1]
     out = os.path.dirname(os.path.abspath(__file__))
     for name, rel in CASES.items():
         d = os.path.join(root, "test-sets", rel)
