@@ -139,7 +139,9 @@ int x2g_host_band_schedule(int nnu, int nmu, int *npoints, int *ntiles, int *nle
  * reference has no device waits (its threads join, src/c/mcsor_pthread.c:87). */
 int x2g_set_wait_limit(x2g_ctx *ctx, double seconds);
 /* Mixed form sweep path: 1 (default) on-chip cluster kernel where the grid
- * fits, 0 the persistent-band kernel. */
+ * fits, 0 the persistent-band kernel, 2 the cluster kernel for batches that
+ * fit its co-resident clusters and the persistent-band kernel for larger
+ * batches that it holds in one launch. */
 int x2g_set_mixed_on_chip(x2g_ctx *ctx, int on);
 /* Self-check of the mixed form's integer-pipe FP64<->FP32 conversions
  * against the hardware conversions on n values (edge cases, then hashed bit
@@ -249,11 +251,15 @@ typedef struct {
    * reference's default, sormcsor.F90:20-132) */
   int orb_scheme, pot_scheme;
   /* 0: the reference's order, the potentials of orbital i relaxed just
-   * before orbital i (relaxDriver); 1: every Coulomb and exchange potential
-   * of an SCF iteration relaxed in one batched launch from the orbitals at
-   * the start of the iteration, then the orbitals in the reference's order.
-   * Same fixed point, different trajectory (no reference counterpart). */
-  int batch_potentials;
+   * before orbital i (relaxDriver, doSCF.F90:943-1011); 1: every Coulomb and
+   * exchange potential of an SCF iteration relaxed in one batched launch
+   * from the orbitals at the start of the iteration, then the orbitals in
+   * the reference's order; 2: as 1, then every orbital relaxed in one
+   * batched launch with the Fock operators of the state after the
+   * potentials, before the norms, orthogonalisation and energies in the
+   * reference's order.  Same fixed point, different trajectory (no
+   * reference counterpart). */
+  int batch_mode;
 } x2g_case;
 
 typedef struct {

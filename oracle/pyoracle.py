@@ -76,6 +76,7 @@ def lib():
         L.x2o_mpole_moments.argtypes = [P, I]
         L.x2o_pot_asympt.argtypes = [P, I]
         L.x2o_cmulti.argtypes = [P, dp]
+        L.x2o_set_batch_potentials.argtypes = [P, I]
         _lib = L
     return _lib
 
@@ -113,6 +114,12 @@ class Case:
     @property
     def mxsize(self):
         return self.nni * self.nmu
+
+    def set_batch_potentials(self, mode=1):
+        """1: all potentials of an SCF iteration relaxed from its starting
+        orbitals; 2: then all orbitals from the state after them; 0: the
+        reference's order."""
+        self.L.x2o_set_batch_potentials(self.h, int(mode))
 
     def run(self, verbose=0):
         return self.L.x2o_run_scf(self.h, verbose)

@@ -59,6 +59,8 @@ struct x2o_state {
   int lhomonucl, lbreakCi;
   int maxsororb[2], maxsorpot[2];
   int hydrogen_start, old_start;
+  int batch_pots; /* 1: all potentials of an iteration from its starting orbitals; 2: and then all orbitals
+                     from the state after the potentials (no reference counterpart) */
 
   /* ---------------- grid ---------------- */
   int mxnmu, mxsize, nni8, mxsize8;
@@ -1767,8 +1769,8 @@ static void add_record(x2o_state *s, int iscf, int iorb) {
 
 static const char *bondname(const x2o_state *s, int i) { return s->bond[i]; }
 
-/* relaxDriver: src/doSCF.F90:943-1011 (serial build) */
-static void relax_driver(x2o_state *s, int iorb) {
+/* the potentials of orbital iorb's batch (relaxDriver's first half) */
+static void relax_pots_of(x2o_state *s, int iorb) {
   if (s->nexchpots[iorb] != 0 && !s->lfixexch) {
     if (s->pot_hook) {
       s->nsor4pot += (long)s->nexchpots[iorb] * s->maxsorpot[0] * s->maxsorpot[1];
@@ -1777,7 +1779,34 @@ static void relax_driver(x2o_state *s, int iorb) {
       for (int k = 1; k <= s->nexchpots[iorb]; k++) x2o_relax_pot(s, iorb, k, s->lpotmcsor ? 1 : 0);
     }
   }
-  if (!s->lfixorb) x2o_relax_orb(s, iorb, s->lorbmcsor ? 1 : 0);
+}
+
+/* relaxDriver: src/doSCF.F90:943-1011 (serial build); in the batched mode
+ * the potentials were relaxed before the orbital loop */
+static void relax_driver(x2o_state *s, int iorb) {
+  if (!s->batch_pots) relax_pots_of(s, iorb);
+  if (!s->lfixorb && s->batch_pots != 2) x2o_relax_orb(s, iorb, s->lorbmcsor ? 1 : 0);
+}
+
+/* batched orbitals (mode 2): every orbital relaxed with the Fock operator
+ * of the state after the potentials, i.e. from the other orbitals' values at
+ * that point; the relaxed orbitals replace the old ones together */
+static void relax_all_orbitals(x2o_state *s) {
+  const int norb = s->norb;
+  double *keep[MAXORB + 1], *fresh[MAXORB + 1];
+  for (int i = 1; i <= norb; i++) {
+    const int iorb = norb - i + 1;
+    keep[iorb] = s->psi[iorb];
+    fresh[iorb] = dalloc(s->mxsize);
+    memcpy(fresh[iorb], keep[iorb], sizeof(double) * s->mxsize);
+    s->psi[iorb] = fresh[iorb];
+    x2o_relax_orb(s, iorb, s->lorbmcsor ? 1 : 0);
+    s->psi[iorb] = keep[iorb];
+  }
+  for (int iorb = 1; iorb <= norb; iorb++) {
+    memcpy(keep[iorb], fresh[iorb], sizeof(double) * s->mxsize);
+    free(fresh[iorb]);
+  }
 }
 
 /* prepSCF: src/doSCF.F90:24-174 */
@@ -1831,10 +1860,23 @@ static int scf_iteration(x2o_state *s) {
   int norb = s->norb;
   int iscf = ++s->iscf;
   int iasympt = norb;
+  if (s->batch_pots) {
+    /* batched mode (no reference counterpart): every potential's boundary
+     * values, then every orbital's potential batch, all from the orbitals at
+     * the start of the iteration; the orbitals follow in relaxDriver order */
+    for (int i = 1; i <= norb; i++) {
+      int iorb = norb - i + 1;
+      s->itouch[iorb] = 1;
+      if (iasympt != 0 && s->ifixorb[iorb] == 0) { x2o_pot_asympt(s, iorb); iasympt--; }
+    }
+    s->isstart = 1; s->isstop = s->ngrid1; s->isstep = 1;
+    for (int i = 1; i <= norb; i++) relax_pots_of(s, norb - i + 1);
+    if (s->batch_pots == 2 && !s->lfixorb) relax_all_orbitals(s);
+  }
   for (int i = 1; i <= norb; i++) {
     int iorb = norb - i + 1;
     s->itouch[iorb] = 1;
-    if (iasympt != 0 && s->ifixorb[iorb] == 0) { x2o_pot_asympt(s, iorb); iasympt--; }
+    if (!s->batch_pots && iasympt != 0 && s->ifixorb[iorb] == 0) { x2o_pot_asympt(s, iorb); iasympt--; }
     s->isstart = 1; s->isstop = s->ngrid1; s->isstep = 1;
     if (s->altSweeps && (iorb % 2 != 0)) { s->isstart = s->ngrid1; s->isstop = 1; s->isstep = -1; }
     relax_driver(s, iorb);
@@ -2061,6 +2103,9 @@ void x2o_cmulti(const x2o_state *s, double *out) {
   for (int k = 1; k <= s->mpole; k++)
     for (int i = 1; i <= s->norb; i++) out[(k - 1) * s->norb + (i - 1)] = s->cmulti[i + (k - 1) * s->norb];
 }
+
+/* batched-potential mode on (1) or off (0, the reference's order) */
+void x2o_set_batch_potentials(x2o_state *s, int on) { s->batch_pots = (on >= 0 && on <= 2) ? on : 0; }
 
 void x2o_set_hooks(x2o_state *s, void (*pot_hook)(void *, int),
                    void (*orb_hook)(void *, int, int, double *, double *, double *), void *ud) {

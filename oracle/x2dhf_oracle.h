@@ -115,6 +115,13 @@ void x2o_pot_asympt(x2o_state *s, int iorb);
 /* multipole moments: cmulti[(k-1)*norb + iorb-1], exchange moments by pair */
 void x2o_cmulti(const x2o_state *s, double *out);
 
+/* Batched modes (no reference counterpart): 1 relaxes every potential of an
+ * SCF iteration from the orbitals at the start of the iteration, before the
+ * orbital loop; 2 then also relaxes every orbital with the Fock operator of
+ * the state after the potentials before the norms, orthogonalisation and
+ * energies of the orbital loop; 0 (default) is relaxDriver's order. */
+void x2o_set_batch_potentials(x2o_state *s, int on);
+
 /* Replace the relaxations by external kernels (the reference's own C backend
  * in the timed reference run): pot_hook(ud, iorb) relaxes every potential of
  * orbital iorb in the potential block; orb_hook(ud, iorb, isym, wk2, lhs,

@@ -36,6 +36,39 @@ INPUT_ONLY = {
     "co_set01": "co-elprop/set-01",  # CO, 1 pi + 5 sigma (14 electrons)
 }
 
+# outputs whose first run starts from the hydrogenic LCAO guess: the total
+# energy the reference prints after initialisation (prepSCF) pins the start
+# (orbitals, Thomas-Fermi Coulomb and 1/r exchange guesses, norms,
+# orthogonalisation, multipole moments, orbital energies, EtotalHF).  The
+# 2023 runs (the *-elprop sets, ne2/set-03) come from an earlier program
+# version whose start differs from the sources; they are kept as the
+# record of that, n2-elprop/set-01 among them.
+INITIAL_ENERGY_SETS = ["h2/set-01", "he/set-01", "ne/set-01", "na/set-01", "al/set-01", "lih/set-01",
+                       "alf/set-02", "gaf/set-01", "he2-elprop/set-01", "ca/set-02"]
+EARLIER_VERSION_SETS = ["n2-elprop/set-01", "ne-elprop/set-01", "co-elprop/set-01", "fh-elprop/set-01"]
+
+
+def first_run(lst):
+    """(echoed input deck, run date, first printed total energy) of the
+    output's first run."""
+    body = lst.split("... start of input data ...", 1)[1]
+    echo = body.split("... end of input data", 1)[0].splitlines()[1:]
+    deck = "\n".join(ln[2:] if ln.startswith("  ") else ln for ln in echo).rstrip() + "\n"
+    date = re.search(r"start:\s+(\S+)", lst)
+    etot = re.search(r"total energy:\s+(-?\d\.\d+E[+-]\d+)", body)
+    return deck, date.group(1) if date else None, float(etot.group(1))
+
+
+def initial_energies(root):
+    out = {}
+    for group, sets in (("current", INITIAL_ENERGY_SETS), ("earlier_version", EARLIER_VERSION_SETS)):
+        for rel in sets:
+            with open(os.path.join(root, "test-sets", rel, "reference.lst"), errors="replace") as f:
+                deck, date, etot = first_run(f.read())
+            out[rel] = {"deck": deck, "date": date, "initial_total_energy": etot, "group": group}
+    return out
+
+
 LINE = re.compile(r"^\s*(\d+)\s+(\d+)\s+(sigma|pi|delta|phi)\s*([gu]?)\s+"
                   r"(-?\d\.\d+E[+-]\d+)\s+(-?\d\.\d+E[+-]\d+)\s+(-?\d\.\d+E[+-]\d+)")
 
@@ -79,6 +112,9 @@ def main():
             json.dump({"source": f"test-sets/{rel}/reference.lst", "records": recs,
                        "total_energy": etot, "sweeps": sweeps}, f, indent=0)
         print(f"{name}: {len(recs)} records, E={etot}, sweeps={sweeps}")
+    with open(os.path.join(out, "initial_energies.json"), "w") as f:
+        json.dump(initial_energies(root), f, indent=1)
+    print("initial_energies.json: printed initial total energies")
     for name, (rel, prefix) in CHECKPOINTS.items():
         os.makedirs(os.path.join(out, name), exist_ok=True)
         for ext in ("dat", "orb", "coul", "exch"):

@@ -151,15 +151,16 @@ def test_mixed_on_chip_matches_persistent_band_path(ctx, name):
     assert np.abs(out[0] - out[1]).max() <= 1e-5 * change
 
 
-def _scf_records_match(name, niter, transform=None, tol=1e-11):
+def _scf_records_match(name, niter, transform=None, tol=1e-11, batch_mode=0):
     deck = golden_deck(name)
     if transform:
         deck = transform(deck)
     deck = _all_mcsor(deck)
     oc = Case(deck)
+    oc.set_batch_potentials(batch_mode)
     oc.steps(niter)
     ctx = xg.Context(0)
-    s = xg.SCF(ctx, xg.parse_deck(deck))
+    s = xg.SCF(ctx, xg.parse_deck(deck, batch_mode=batch_mode))
     s.run(niter)
     ro, rg = oc.records(), s.records()
     assert len(ro) == len(rg)
@@ -201,6 +202,20 @@ def test_scf_kf_trajectory_matches_oracle():
     """11 orbitals incl. pi-pi exchange pairs (two potentials each),
     heteronuclear: 72 potentials per SCF iteration."""
     _scf_records_match("kf_set01", 5, _kf_small)
+
+
+@pytest.mark.parametrize("batch_mode", [1, 2])
+def test_scf_batched_trajectory_matches_oracle(batch_mode):
+    """All potentials of an iteration in one launch (1), and all orbitals in
+    one more (2): the GPU follows the oracle's run of the same mode."""
+    _scf_records_match("ne_set01", 25, batch_mode=batch_mode)
+
+
+@pytest.mark.parametrize("batch_mode", [1, 2])
+def test_scf_kf_batched_trajectory_matches_oracle(batch_mode):
+    """KF's 72 potentials in one call (three launches of at most 32 jobs)
+    and its 11 orbitals in one launch."""
+    _scf_records_match("kf_set01", 5, _kf_small, batch_mode=batch_mode)
 
 
 def test_scf_he_converged_energy_vs_golden():
@@ -353,4 +368,29 @@ def test_sor_deck_is_refused_not_silently_relaxed_with_mcsor():
         with pytest.raises(xg.X2GError) as ei:
             xg.SCF(ctx, xg.parse_deck(deck))
         assert ei.value.code == 8 and "SOR" in str(ei.value)
+    ctx.close()
+
+
+def test_gpu_start_matches_printed_initial_energies():
+    """The GPU's hydrogenic start and prepSCF (device-evaluated LCAO
+    orbitals and potential guesses, norms, orthogonalisation, moments,
+    orbital energies, total energy) against the total energy the reference
+    printed after its own start, for the closed-shell outputs of the current
+    program version: He, Ne, Ca atoms and H2, He2, LiH, AlF, GaF (9 to 15
+    orbitals for the fluorides)."""
+    g = golden_json("initial_energies")
+    ctx = xg.Context(0)
+    checked = 0
+    for rel, v in g.items():
+        if v["group"] != "current":
+            continue
+        case = xg.parse_deck(_all_mcsor(v["deck"]))
+        if any(case.occ[i] not in (2.0, 4.0) for i in range(case.norb)) and case.norb > 1:
+            continue  # open shells: outside the closed-shell GPU path
+        s = xg.SCF(ctx, case)
+        e, ref = s.run(0).total_energy, v["initial_total_energy"]
+        assert abs(e - ref) <= 2e-11 * abs(ref) + 1e-13, (rel, e, ref)
+        s.close()
+        checked += 1
+    assert checked == 8
     ctx.close()

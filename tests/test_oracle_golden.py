@@ -71,3 +71,40 @@ def test_oracle_mesh_lists():
     assert ((rows - 4 - 1) * nni + (cols - 4) == i2).all()
     assert rows.min() == 6 and rows.max() == nmu and cols.min() == 6 and cols.max() == nni + 3
     assert i7.size == nni - 2 and i6a.size == nmu - 4 and i6b.size == nmu - 4
+
+
+def _initial_energy(deck):
+    c = Case(deck)
+    c.steps(0)
+    return c.etotal()[0]
+
+
+def test_oracle_start_matches_printed_initial_energies():
+    """The total energy the reference prints right after its hydrogenic
+    start (prepSCF: LCAO orbitals, Thomas-Fermi Coulomb and 1/r exchange
+    guesses, norms, orthogonalisation, multipole moments, orbital energies)
+    for ten outputs of the current program version: atoms (He, Ne, Na, Al,
+    Ca) and homo- and heteronuclear diatomics (H2, He2, LiH, AlF, GaF)."""
+    g = golden_json("initial_energies")
+    checked = 0
+    for rel, v in g.items():
+        if v["group"] != "current":
+            continue
+        e, ref = _initial_energy(v["deck"]), v["initial_total_energy"]
+        assert abs(e - ref) <= 2e-11 * abs(ref) + 1e-13, (rel, e, ref)
+        checked += 1
+    assert checked == 10
+
+
+def test_earlier_version_outputs_start_elsewhere():
+    """The 2023 outputs (n2-elprop/set-01, whose trajectory n2_set01.json
+    holds, and the other *-elprop sets) were written by an earlier program
+    version: their printed initial energies lie Eh away from what the
+    reference's sources (and the oracle) give for the same echoed input, so
+    they pin only the converged energy, not the SCF trajectory."""
+    g = golden_json("initial_energies")
+    for rel, v in g.items():
+        if v["group"] == "earlier_version":
+            assert v["date"].startswith("2023")
+            assert abs(_initial_energy(v["deck"]) - v["initial_total_energy"]) > 1.0, rel
+    assert g["n2-elprop/set-01"]["group"] == "earlier_version"

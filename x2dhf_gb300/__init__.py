@@ -46,7 +46,7 @@ class Case(C.Structure):
         ("maxsor_orb", C.c_int), ("maxsor_pot", C.c_int),
         ("omega_orb", C.c_double), ("omega_pot", C.c_double), ("recalc_mm", C.c_double),
         ("mpole", C.c_int), ("homonuclear", C.c_int), ("precision", C.c_int), ("start", C.c_int),
-        ("orb_scheme", C.c_int), ("pot_scheme", C.c_int), ("batch_potentials", C.c_int),
+        ("orb_scheme", C.c_int), ("pot_scheme", C.c_int), ("batch_mode", C.c_int),
     ]
 
 
@@ -159,17 +159,19 @@ def round_grid(n):
     return lib().x2g_round_grid(int(n))
 
 
-def parse_deck(text, precision=FP64, batch_potentials=False):
+def parse_deck(text, precision=FP64, batch_mode=0):
     """Parse a reference input deck into an x2g_case (closed-shell HF).
 
     The relaxation schemes follow the deck's cards as in the reference: SOR
     unless mcsor / mcsor-o (orbitals) or mcsor-ce (potentials) is given.
-    batch_potentials selects the batched potential mode (x2g_case)."""
+    batch_mode: 0 the reference's relaxation order, 1 all potentials of an
+    SCF iteration in one launch, 2 then all orbitals in one launch too
+    (x2g_case.batch_mode)."""
     L = lib()
     c = Case()
     L.x2g_case_defaults(C.byref(c))
     c.precision = precision
-    c.batch_potentials = 1 if batch_potentials else 0
+    c.batch_mode = int(batch_mode)
     lines = [ln.split("!")[0].replace(",", " ").split() for ln in text.splitlines()]
     lines = [[t.lower() for t in ln] for ln in lines if ln]
     i = 0
@@ -400,7 +402,9 @@ class Context:
         _check(self.L.x2g_set_wait_limit(self.h, float(seconds)))
 
     def set_mixed_on_chip(self, on):
-        _check(self.L.x2g_set_mixed_on_chip(self.h, 1 if on else 0))
+        """Mixed-form sweep path: True cluster kernel, False persistent-band
+        kernel, "auto" cluster kernel up to its co-resident clusters."""
+        _check(self.L.x2g_set_mixed_on_chip(self.h, 2 if on == "auto" else (1 if on else 0)))
 
     def convert_selftest(self, n, seed=1):
         """Mismatches of the integer-pipe FP64<->FP32 conversions against the hardware ones."""

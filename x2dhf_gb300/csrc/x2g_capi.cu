@@ -182,8 +182,9 @@ int x2g_set_wait_limit(x2g_ctx *c, double seconds) {
 }
 
 int x2g_set_mixed_on_chip(x2g_ctx *c, int on) {
-  if (!c) return set_status(X2G_ERR_ARG, "null context");
-  c->no_cluster = on ? 0 : 1;
+  if (!c || on < 0 || on > 2) return set_status(X2G_ERR_ARG, "on must be 0, 1 or 2");
+  c->no_cluster = (on == 0) ? 1 : 0;
+  c->auto_band = (on == 2) ? 1 : 0;
   return X2G_OK;
 }
 

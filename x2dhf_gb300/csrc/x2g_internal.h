@@ -164,6 +164,8 @@ struct x2g_ctx {
   long launches = 0;
   size_t cluster_smem_set = 0;  // dynamic shared memory granted to the cluster kernel
   int no_cluster = 0;           // 1: mixed form uses the persistent-band FP32 kernel
+  int auto_band = 0;            // 1: batches beyond the co-resident clusters take the persistent-band kernel
+  int cluster_active = 0;       // clusters of the cluster kernel co-resident on the device (last shape checked)
   int cluster_nonportable = 0;  // cluster kernel allowed more than 8 CTAs
   long cluster_checked_key = -1;  // (shared bytes, cluster size) last checked
   int cluster_ok = 0;             // that cluster shape is schedulable here

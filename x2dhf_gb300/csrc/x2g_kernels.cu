@@ -1682,8 +1682,10 @@ static bool cluster_usable(x2g_ctx *ctx, const GridDev &g) {
       q.numAttrs = 1;
       int nclusters = 0;
       if (cudaOccupancyMaxActiveClusters(&nclusters, (const void *)k_mixed_cluster, &q) == cudaSuccess &&
-          nclusters > 0)
+          nclusters > 0) {
         ctx->cluster_ok = 1;
+        ctx->cluster_active = nclusters;
+      }
     }
     (void)cudaGetLastError();
   }
@@ -1849,7 +1851,16 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
   if (nsweeps <= 0) return set_status(X2G_ERR_ARG, "nsweeps must be positive");
   const GridDev &g = grid->d;
   const bool mixed = (precision == X2G_MIXED);
-  const bool on_chip = mixed && cluster_usable(ctx, g);
+  bool on_chip = mixed && cluster_usable(ctx, g);
+  if (on_chip && ctx->auto_band && njobs > ctx->cluster_active) {
+    // more jobs than co-resident clusters: the cluster kernel would run in
+    // waves, while the persistent-band kernel may hold the whole batch
+    int nj = 0, G1 = 0;
+    size_t sm1 = 0;
+    const int want = njobs < kParamJobs ? njobs : kParamJobs;
+    if (persistent_shape(ctx, g, want, &nj, &G1, &sm1) == X2G_OK && nj >= want) on_chip = false;
+    set_status(X2G_OK, "");
+  }
   // per-job scratch: FP64 rhs of potentials, or the mixed form's FP32
   // correction, residual and omega/lhs
   const size_t per_job =

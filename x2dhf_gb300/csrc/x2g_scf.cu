@@ -42,6 +42,8 @@ struct x2g_scf {
   std::vector<int> ilc;
   std::vector<double *> orb, coul, coulp, exchp, exch;  // device arrays
   double *lhs = nullptr, *rhs = nullptr, *fa = nullptr, *edecay = nullptr;
+  // batch_mode 2: per-orbital Fock outputs (lhs, rhs, fock1/f1 tail, decay)
+  std::vector<double *> blhs, brhs, bfa, bedecay;
   double *sc = nullptr;  // device scalars
   // scalar block offsets (doubles)
   enum { O_EE = 0, O_NORM = 64, O_OVL = 128, O_CM = 128 + 64 * 64, O_EX = O_CM + 64 * 8 };
@@ -338,18 +340,20 @@ void exchange_weights(x2g_scf *s) {
 // ---------------------------------------------------------------------
 // device operations of one SCF step
 // ---------------------------------------------------------------------
-int fock(x2g_scf *s, int iorb) {
+// fockHF of orbital iorb into lhs (fock1 + diag), rhs (fock2) and fa
+// (fock1/f1 on the last 5 mu rows)
+int fock_into(x2g_scf *s, int iorb, double *lhs, double *rhs, double *fa) {
   const GridDev &g = s->grid->d;
   FockArgs a{};
   a.m = s->m[iorb];
   a.nel1 = (s->nel == 1);
   a.exact = (s->cs.precision == X2G_FP64);
   a.ee = s->sc + x2g_scf::O_EE + iorb;
-  a.lhs = s->lhs;
-  a.rhs = s->rhs;
+  a.lhs = lhs;
+  a.rhs = rhs;
   a.coulp = s->coulp[iorb];
   a.exchp = s->exchp[iorb];
-  a.fa = s->fa;
+  a.fa = fa;
   int n = 0;
   for (int j = 1; j <= s->norb; j++) {
     FockTerm &t = a.t[n++];
@@ -378,20 +382,37 @@ int fock(x2g_scf *s, int iorb) {
   return X2G_OK;
 }
 
-int relax_potentials(x2g_scf *s, int iorb) {
-  const auto &P = s->pots[iorb];
-  std::vector<x2g_job> jobs(P.size());
-  for (size_t k = 0; k < P.size(); k++) {
-    x2g_job &j = jobs[k];
-    j.u = P[k].target;
-    j.psa = s->orb[P[k].in1];
-    j.psb = s->orb[P[k].in2];
+int fock(x2g_scf *s, int iorb) { return fock_into(s, iorb, s->lhs, s->rhs, s->fa); }
+
+void potential_jobs(x2g_scf *s, int iorb, std::vector<x2g_job> &jobs) {
+  for (const PotSlot &P : s->pots[iorb]) {
+    x2g_job j{};
+    j.u = P.target;
+    j.psa = s->orb[P.in1];
+    j.psb = s->orb[P.in2];
     j.omega = s->omega_pot;
-    j.isym = P[k].isym;
-    j.idel = P[k].idel;
+    j.isym = P.isym;
+    j.idel = P.idel;
     j.kind = 1;
+    jobs.push_back(j);
   }
-  s->nsor4pot += long(P.size()) * s->cs.maxsor_pot;
+}
+
+// coulExchSOR/MCSOR of one orbital's batch (relaxPots.F90:8-114)
+int relax_potentials(x2g_scf *s, int iorb) {
+  std::vector<x2g_job> jobs;
+  potential_jobs(s, iorb, jobs);
+  s->nsor4pot += long(jobs.size()) * s->cs.maxsor_pot;
+  return launch_relax(s->ctx, s->grid, jobs.data(), int(jobs.size()), s->cs.maxsor_pot, s->cs.precision);
+}
+
+// Batched mode: every orbital's batch (each Coulomb and exchange potential
+// of the iteration once) in one launch, all from the orbitals at the start
+// of the iteration, in relaxDriver's orbital order
+int relax_all_potentials(x2g_scf *s) {
+  std::vector<x2g_job> jobs;
+  for (int i = 1; i <= s->norb; i++) potential_jobs(s, s->norb - i + 1, jobs);
+  s->nsor4pot += long(jobs.size()) * s->cs.maxsor_pot;
   return launch_relax(s->ctx, s->grid, jobs.data(), int(jobs.size()), s->cs.maxsor_pot, s->cs.precision);
 }
 
@@ -410,6 +431,32 @@ int relax_orbital(x2g_scf *s, int iorb) {
   int rc = launch_relax(s->ctx, s->grid, &j, 1, s->cs.maxsor_orb, s->cs.precision);
   if (rc) return rc;
   launch_asympt_set(s->ctx, g, s->orb[iorb], s->edecay);
+  return X2G_OK;
+}
+
+// batch_mode 2: the Fock operators of every orbital from the state after
+// the potentials (no orbital has changed yet), then all orbitals relaxed in
+// one launch, each with its own lhs, rhs and asymptotic decay
+int relax_all_orbitals(x2g_scf *s) {
+  const GridDev &g = s->grid->d;
+  std::vector<x2g_job> jobs;
+  for (int i = 1; i <= s->norb; i++) {
+    const int iorb = s->norb - i + 1;
+    fock_into(s, iorb, s->blhs[iorb], s->brhs[iorb], s->bfa[iorb]);
+    launch_asympt_get(s->ctx, g, s->bfa[iorb], s->bedecay[iorb]);
+    x2g_job j{};
+    j.u = s->orb[iorb];
+    j.lhs = s->blhs[iorb];
+    j.rhs = s->brhs[iorb];
+    j.omega = s->omega_orb;
+    j.isym = s->isymOrb[iorb];
+    j.kind = 0;
+    jobs.push_back(j);
+  }
+  s->nsor4orb += long(jobs.size()) * s->cs.maxsor_orb;
+  int rc = launch_relax(s->ctx, s->grid, jobs.data(), int(jobs.size()), s->cs.maxsor_orb, s->cs.precision);
+  if (rc) return rc;
+  for (int iorb = 1; iorb <= s->norb; iorb++) launch_asympt_set(s->ctx, g, s->orb[iorb], s->bedecay[iorb]);
   return X2G_OK;
 }
 
@@ -634,16 +681,35 @@ int scf_iteration(x2g_scf *s, int *rc) {
   const int iscf = ++s->iscf;
   int iasympt = norb;
   *rc = X2G_OK;
+  const bool batched = (s->cs.batch_mode >= 1);
+  if (batched) {
+    // the boundary values of every potential first (they depend only on the
+    // multipole moments, which change only between iterations), then all
+    // potentials of the iteration in one relaxation launch
+    for (int i = 1; i <= norb; i++) {
+      const int iorb = norb - i + 1;
+      s->itouch[iorb] = 1;
+      if (iasympt != 0 && s->ifixorb[iorb] == 0) {
+        pot_asympt(s, iorb);
+        iasympt--;
+      }
+    }
+    if ((*rc = relax_all_potentials(s))) return 1;
+    if (s->cs.batch_mode == 2 && !s->lfixorb)
+      if ((*rc = relax_all_orbitals(s))) return 1;
+  }
   for (int i = 1; i <= norb; i++) {
     const int iorb = norb - i + 1;
-    s->itouch[iorb] = 1;
-    if (iasympt != 0 && s->ifixorb[iorb] == 0) {
-      pot_asympt(s, iorb);
-      iasympt--;
+    if (!batched) {
+      s->itouch[iorb] = 1;
+      if (iasympt != 0 && s->ifixorb[iorb] == 0) {
+        pot_asympt(s, iorb);
+        iasympt--;
+      }
+      // relaxDriver (doSCF.F90:943-1011)
+      if ((*rc = relax_potentials(s, iorb))) return 1;
     }
-    // relaxDriver (doSCF.F90:943-1011)
-    if ((*rc = relax_potentials(s, iorb))) return 1;
-    if (!s->lfixorb)
+    if (!s->lfixorb && s->cs.batch_mode != 2)
       if ((*rc = relax_orbital(s, iorb))) return 1;
     if (s->ifixorb[iorb] == 0 && s->cs.homonuclear) {
       // norm scaling and setCiOrb in one pass
@@ -833,7 +899,7 @@ int x2g_scf_create(x2g_ctx *ctx, const x2g_case *c, x2g_scf **out) {
     return set_status(X2G_ERR_UNSUPPORTED,
                       "list-order SOR (a deck without the mcsor-o/mcsor and mcsor-ce cards) is not available on the "
                       "GPU: set orb_scheme = pot_scheme = 1 (MCSOR)");
-  if (c->batch_potentials != 0 && c->batch_potentials != 1) return set_status(X2G_ERR_ARG, "bad batch_potentials");
+  if (c->batch_mode < 0 || c->batch_mode > 2) return set_status(X2G_ERR_ARG, "batch_mode must be 0, 1 or 2");
   if (c->maxsor_orb < 1 || c->maxsor_pot < 1) return set_status(X2G_ERR_ARG, "sweep counts must be positive");
   auto *s = new x2g_scf();
   s->ctx = ctx;
@@ -899,6 +965,18 @@ int x2g_scf_create(x2g_ctx *ctx, const x2g_case *c, x2g_scf **out) {
   ok &= (s->rhs = dalloc(s, mx)) != nullptr;
   ok &= (s->fa = dalloc(s, 5 * size_t(s->grid->h.nni))) != nullptr;
   ok &= (s->edecay = dalloc(s, 4 * size_t(s->grid->h.nni))) != nullptr;
+  if (c->batch_mode == 2) {
+    s->blhs.assign(s->norb + 1, nullptr);
+    s->brhs.assign(s->norb + 1, nullptr);
+    s->bfa.assign(s->norb + 1, nullptr);
+    s->bedecay.assign(s->norb + 1, nullptr);
+    for (int i = 1; i <= s->norb; i++) {
+      ok &= (s->blhs[i] = dalloc(s, mx)) != nullptr;
+      ok &= (s->brhs[i] = dalloc(s, mx)) != nullptr;
+      ok &= (s->bfa[i] = dalloc(s, 5 * size_t(s->grid->h.nni))) != nullptr;
+      ok &= (s->bedecay[i] = dalloc(s, 4 * size_t(s->grid->h.nni))) != nullptr;
+    }
+  }
   s->nslots = norb * (norb + 1) + 2;
   s->sc_count = size_t(x2g_scf::O_EX) + 8 * size_t(s->nslots) + 2048;
   ok &= (s->sc = dalloc(s, s->sc_count)) != nullptr;
