@@ -53,6 +53,8 @@ extern "C" {
 /* precision forms */
 #define X2G_FP64 0   /* plain: FP64 MCSOR, reference colour order, bit-exact sweeps    */
 #define X2G_MIXED 1  /* FP32 sweeps on CUDA cores + FP64 defect correction per call      */
+#define X2G_SOR 2    /* FP64 list-order SOR over the reference's "middle" point list (sor,
+                        src/sormcsor.F90:20-132, the reference's default): bit-exact */
 
 typedef struct x2g_ctx x2g_ctx;    /* one GPU, one stream, owned device memory */
 typedef struct x2g_grid x2g_grid;  /* prolate-spheroidal grid + operator tables + sweep schedule */
@@ -138,6 +140,15 @@ int x2g_host_band_schedule(int nnu, int nmu, int *npoints, int *ntiles, int *nle
  * testing the error path).  Applies to launches queued after the call.  The
  * reference has no device waits (its threads join, src/c/mcsor_pthread.c:87). */
 int x2g_set_wait_limit(x2g_ctx *ctx, double seconds);
+/* Schedule of the list-order SOR wavefront (host only, no CUDA call): the
+ * interior points grouped by SOR level (1 + the largest level of their
+ * stencil neighbours earlier in the "middle" list), packed (ext row << 16) |
+ * ext col (pts, npoints values; off, nlev + 1 offsets), the axis points
+ * grouped by the level their extrapolation follows (bpts; boff, nblev + 1
+ * offsets), and delta, the level shift between successive sweeps: sweep s
+ * of a level-l point runs at step l + s * delta.  Null arrays are skipped. */
+int x2g_host_sor_schedule(int nnu, int nmu, int *npoints, int *nlev, int *nblev, int *delta, int *pts, int *off,
+                          int *bpts, int *boff);
 /* Mixed form sweep path: 1 (default) on-chip cluster kernel where the grid
  * fits, 0 the persistent-band kernel, 2 the cluster kernel for batches that
  * fit its co-resident clusters and the persistent-band kernel for larger
@@ -175,8 +186,9 @@ typedef struct {
 } x2g_job;
 
 /* Relax `njobs` independent functions on the same grid with `nsweeps`
- * micro-sweeps each, in one persistent cooperative launch on the context's
- * stream.  `jobs` is a HOST array.  precision: X2G_FP64 or X2G_MIXED. */
+ * micro-sweeps each, in one persistent launch on the context's stream (jobs
+ * beyond 32 in further launches).  `jobs` is a HOST array.  precision:
+ * X2G_FP64 or X2G_MIXED (MCSOR forms) or X2G_SOR (list-order SOR, FP64). */
 int x2g_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, int nsweeps, int precision);
 
 /* Relaxation that allocates no device memory (this entry point has no

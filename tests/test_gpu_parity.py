@@ -359,16 +359,6 @@ def test_mixed_persistent_sweep_batches_track_fp64():
     ctx.close()
 
 
-def test_sor_deck_is_refused_not_silently_relaxed_with_mcsor():
-    """A deck without the mcsor cards asks for the reference's list-order
-    SOR; the GPU SCF refuses it (X2G_ERR_UNSUPPORTED) instead of running
-    MCSOR in its place."""
-    ctx = xg.Context(0)
-    for deck in (golden_deck("h2_set01"), golden_deck("he_set02")):
-        with pytest.raises(xg.X2GError) as ei:
-            xg.SCF(ctx, xg.parse_deck(deck))
-        assert ei.value.code == 8 and "SOR" in str(ei.value)
-    ctx.close()
 
 
 def test_gpu_start_matches_printed_initial_energies():
@@ -394,3 +384,83 @@ def test_gpu_start_matches_printed_initial_energies():
         checked += 1
     assert checked == 8
     ctx.close()
+
+
+@pytest.mark.parametrize("name,iorb,kind", [("he_set01", 1, 0), ("h2_set01", 1, 0), ("ne_set01", 1, 0),
+                                            ("ne_set01", 4, 0), ("ne_set01", 2, 1), ("ne_set01", 1, 1)])
+@pytest.mark.parametrize("nsweeps", [1, 10])
+def test_sor_bitexact(ctx, name, iorb, kind, nsweeps):
+    """List-order SOR on the GPU (pipelined wavefront) against the oracle's
+    sequential SOR over the middle list, orbitals (kind 0, explicit lhs/rhs)
+    and potentials (kind 1, rhs = psa psb g formed on the device)."""
+    torch = pytest.importorskip("torch")
+    deck = golden_deck(name)
+    oc = Case(deck)
+    c, g = _grid(ctx, deck)
+    dev = torch.device("cuda:0")
+    if kind == 0:
+        f1, f2 = oc.fock(iorb)
+        lhs, rhs = f1 + oc.coeffs()[5], f2.copy()
+        isym = -1 if c.m[iorb - 1] % 2 else 1
+        uext = oc.putin(isym, oc.orbital(iorb))
+        omega = oc.omega()[0]
+        ref = oc.sweep(0, isym, nsweeps, omega, uext, lhs, rhs, oc.suppl(0), oc.suppl(2))
+        u, dl, dr = (torch.tensor(x, device=dev) for x in (uext, lhs, rhs))
+        jobs = [xg.Job(u=u.data_ptr(), lhs=dl.data_ptr(), rhs=dr.data_ptr(), omega=omega, isym=isym, kind=0)]
+    else:
+        in1, in2, idel, isym = oc.pot_info(iorb, 1)
+        rhs = (oc.orbital(in1) * oc.orbital(in2)) * oc.suppl(9)
+        lhs = oc.suppl(7).copy() if idel == 0 else oc.suppl(7) + float(idel * idel) * oc.suppl(3)
+        uext = oc.putin(isym, oc.pot(iorb, 1))
+        omega = oc.omega()[1]
+        ref = oc.sweep(0, isym, nsweeps, omega, uext, lhs, rhs, oc.suppl(1), oc.suppl(2))
+        orbs = {i: torch.tensor(oc.putin(1 if c.m[i - 1] % 2 == 0 else -1, oc.orbital(i)), device=dev)
+                for i in (in1, in2)}
+        u = torch.tensor(uext, device=dev)
+        jobs = [xg.Job(u=u.data_ptr(), psa=orbs[in1].data_ptr(), psb=orbs[in2].data_ptr(), omega=omega, isym=isym,
+                       idel=idel, kind=1)]
+    torch.cuda.synchronize()
+    xg.relax(ctx, g, jobs, nsweeps, xg.SOR)
+    ctx.synchronize()
+    got = u.cpu().numpy()
+    n8 = c.nnu + 8
+    # the relaxed function: interior, axis rows/columns and the fixed rows
+    sl = np.s_[4:c.nmu + 4, 4:c.nnu + 4]
+    a, b = got.reshape(c.nmu + 8, n8)[sl], ref.reshape(c.nmu + 8, n8)[sl]
+    assert np.abs(b - uext.reshape(c.nmu + 8, n8)[sl]).max() > 0
+    assert np.array_equal(a, b), np.abs(a - b).max()
+
+
+# the reference's own SOR decks, run on the GPU as the reference ran them
+SOR_GOLDEN = [("h2_set01", None), ("he_set01", with_hydrogen0), ("he_set02", with_hydrogen0)]
+
+
+@pytest.mark.parametrize("name,transform", SOR_GOLDEN)
+def test_scf_sor_decks_reproduce_reference_trajectory(name, transform):
+    """Decks without the mcsor-ce card relax potentials (and, without mcsor,
+    orbitals) with list-order SOR, as the reference does; the GPU run
+    reproduces every orbital-energy line the reference printed, its
+    iteration count, its sweep count and its final energy (he/set-02: MCSOR
+    orbitals, SOR potentials)."""
+    deck = golden_deck(name)
+    if transform:
+        deck = transform(deck)
+    g = golden_json(name)
+    ctx = xg.Context(0)
+    s = xg.SCF(ctx, xg.parse_deck(deck))
+    r = s.run()
+    recs = s.records()
+    assert len(recs) == len(g["records"]), (len(recs), len(g["records"]))
+    for (it, io, ee, dee, dn), gr in zip(recs, g["records"]):
+        assert it == gr[0]
+        assert abs(ee - gr[2]) <= 1e-11 * max(1.0, abs(gr[2])), (it, ee, gr)
+    assert abs(r.total_energy - g["total_energy"]) <= 1e-12 * abs(g["total_energy"])
+    assert r.sweeps == g["sweeps"]
+    s.close()
+    ctx.close()
+
+
+def test_scf_ne_sor_reproduces_reference_trajectory():
+    """Ne (ne/set-01): 4 orbitals incl. 1pi, SOR for orbitals and potentials,
+    1432 printed orbital-energy lines and 52540 sweeps."""
+    test_scf_sor_decks_reproduce_reference_trajectory("ne_set01", None)

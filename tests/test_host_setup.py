@@ -211,3 +211,78 @@ def test_parse_deck_relaxation_schemes_follow_the_cards():
     assert schemes("\n".join(base + ["mcsor-ce", "mcsor", "stop"])) == (1, 0)
     c = xg.parse_deck("\n".join(base + ["mcsor-ce 1 7", "stop"]))
     assert c.maxsor_pot == 7
+
+
+def _sor_wavefront(oc, sched, isym, nsweeps, omega, u0, lhs, rhs, b, d):
+    """The GPU's list-order SOR schedule run as a parallel machine in numpy:
+    every update of a step is computed from the state at the start of the
+    step, then all are written (the reference's arithmetic order, no FMA)."""
+    pts, off, bpts, boff, D = sched
+    nni = oc.nni
+    n8 = nni + 8
+    dmu1, dmu2, dni1, dni2, ex, _ = oc.coeffs()
+    u = u0.copy()
+    ij_all = (pts >> 16) * n8 + (pts & 0xffff)
+    ik_all = ((pts >> 16) - 4) * nni + ((pts & 0xffff) - 4)
+    bij = (bpts >> 16) * n8 + (bpts & 0xffff)
+    bst = np.where((bpts & 0xffff) == 4, 1, np.where((bpts & 0xffff) == nni + 3, -1, n8))
+    NL, NB = len(off) - 1, len(boff) - 1
+    for t in range((nsweeps - 1) * D + max(NL, NB)):
+        writes = []
+        for s in range(nsweeps):
+            lv = t - s * D
+            if lv < 0:
+                break
+            if lv < NL:
+                ij, ik = ij_all[off[lv]:off[lv + 1]], ik_all[off[lv]:off[lv + 1]]
+
+                def f(o):
+                    return u[ij + o]
+
+                def pair(c, st, sign):
+                    a = [f(-k * st) + sign * f(k * st) for k in (4, 3, 2, 1)]
+                    return ((c[0] * a[0] + c[1] * a[1]) + c[2] * a[2]) + c[3] * a[3]
+
+                cc = ((pair(dmu2, n8, 1) + b[ik] * pair(dmu1, n8, -1)) + pair(dni2, 1, 1)) + d[ik] * pair(dni1, 1, -1)
+                writes.append((ij, (omega * (rhs[ik] - cc)) / lhs[ik] + (1.0 - omega) * u[ij]))
+            if lv < NB:
+                ij, st = bij[boff[lv]:boff[lv + 1]], bst[boff[lv]:boff[lv + 1]]
+                if isym == 1:
+                    v = (((ex[0] * u[ij + st] + ex[1] * u[ij + 2 * st]) + ex[2] * u[ij + 3 * st])
+                         + ex[3] * u[ij + 4 * st]) + ex[4] * u[ij + 5 * st]
+                else:
+                    v = np.zeros(ij.size)
+                writes.append((ij, v))
+        for ij, v in writes:
+            u[ij] = v
+    return u
+
+
+@pytest.mark.parametrize("name,iorb,kind", [("he_set01", 1, 0), ("ne_set01", 1, 0), ("ne_set01", 2, 1)])
+def test_sor_wavefront_schedule_equals_sequential_sor(name, iorb, kind):
+    """The pipelined wavefront of the GPU's list-order SOR (step = level +
+    sweep * delta, all updates of a step independent) gives bit for bit the
+    oracle's sequential SOR over the "middle" list with the axis
+    extrapolated after every sweep (sormcsor.F90:20-132), for an even and an
+    odd orbital and a potential, over 3 sweeps."""
+    oc = Case(golden_deck(name))
+    c = xg.parse_deck(golden_deck(name))
+    sched = xg.host_sor_schedule(oc.nni, oc.nmu)
+    if kind == 0:
+        f1, f2 = oc.fock(iorb)
+        lhs, rhs, b = f1 + oc.coeffs()[5], f2, oc.suppl(0)
+        isym = -1 if c.m[iorb - 1] % 2 else 1
+        u0 = oc.putin(isym, oc.orbital(iorb))
+        omega = oc.omega()[0]
+    else:
+        in1, in2, idel, isym = oc.pot_info(iorb, 1)
+        rhs = (oc.orbital(in1) * oc.orbital(in2)) * oc.suppl(9)
+        lhs = oc.suppl(7) + float(idel * idel) * oc.suppl(3)
+        b = oc.suppl(1)
+        u0 = oc.putin(isym, oc.pot(iorb, 1))
+        omega = oc.omega()[1]
+    d = oc.suppl(2)
+    ref = oc.sweep(0, isym, 3, omega, u0, lhs, rhs, b, d)
+    got = _sor_wavefront(oc, sched, isym, 3, omega, u0, lhs, rhs, b, d)
+    assert np.abs(ref - u0).max() > 0
+    assert np.array_equal(got, ref), np.abs(got - ref).max()

@@ -21,7 +21,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(HERE, "libx2dhf_gpu.so")
 
 MAXORB = 36
-FP64, MIXED = 0, 1
+FP64, MIXED, SOR = 0, 1, 2
 _ERRORS = {1: "bad argument", 2: "CUDA error", 3: "allocation failed", 4: "device barrier timeout",
            5: "NaN detected", 6: "schedule check failed", 7: "COMMON blocks not linked",
            8: "unsupported case", 9: "no CUDA device"}
@@ -75,7 +75,7 @@ EXPORTS = [
     "x2g_kernel_launches", "x2g_transfer_bytes", "mcsor_pthread_", "mcsor_tpool_", "coulExch_pthread_", "coulExch_tpool_",
     "tpoolStop4mcsor_", "tpoolStop4pots_", "x2g_host_table", "x2g_host_schedule", "x2g_profile",
     "x2g_relax_noalloc", "x2g_host_cluster_plan", "x2g_set_mixed_on_chip", "x2g_host_cluster_chunks", "x2g_host_band_schedule",
-    "x2g_convert_selftest", "x2g_set_wait_limit",
+    "x2g_convert_selftest", "x2g_set_wait_limit", "x2g_host_sor_schedule",
 ]
 
 _lib = None
@@ -129,6 +129,7 @@ def lib():
     ip = C.POINTER(C.c_int)
     L.x2g_host_schedule.argtypes = [I, I, ip, ip, ip, ip, ip, ip, ip]
     L.x2g_host_band_schedule.argtypes = [I, I, ip, ip, ip, ip, ip, ip, ip, ip]
+    L.x2g_host_sor_schedule.argtypes = [I, I, ip, ip, ip, ip, ip, ip, ip, ip]
     L.x2g_profile.argtypes = [P, I, I, dp, dp, C.POINTER(C.c_long)]
     L.x2g_host_cluster_plan.argtypes = [I, I, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_long),
                                         C.POINTER(C.c_int)]
@@ -178,6 +179,7 @@ def parse_deck(text, precision=FP64, batch_mode=0):
     grid = None
     norb = 0
     hydrogen = False
+    altsweeps = False
 
     def nums(tok):
         out = []
@@ -294,10 +296,15 @@ def parse_deck(text, precision=FP64, batch_mode=0):
             c.recalc_mm = v[0] if v and v[0] > 2.2e-16 else 1e15
             if len(v) > 1:
                 c.mpole = int(v[1])
+        elif lab == "altsweep":
+            altsweeps = True
         elif lab == "stop":
             break
     if grid is None or norb == 0 or not hydrogen:
         raise ValueError("deck needs nuclei, config, grid, orbpot hydrogen and lcao cards")
+    if altsweeps and (c.orb_scheme == 0 or c.pot_scheme == 0):
+        # reversed list order for odd orbitals (isstep=-1): not scheduled on the GPU
+        raise ValueError("altsweeps with list-order SOR is not supported")
     # lcao coefficients normalised |c1|+|c2| = 1 (read_lcao, read_stop)
     for k in range(norb):
         s = abs(c.co1[k]) + abs(c.co2[k])
@@ -348,6 +355,22 @@ def host_band_schedule(nnu, nmu):
     ip = [a.ctypes.data_as(C.POINTER(C.c_int)) for a in (pts, off, rows, r0, r1)]
     _check(L.x2g_host_band_schedule(nnu, nmu, C.byref(n), C.byref(t), C.byref(lv), *ip))
     return pts, off, rows, r0, r1, lv.value
+
+
+def host_sor_schedule(nnu, nmu):
+    """(pts, off, bpts, boff, delta) of the list-order SOR wavefront (no GPU needed)."""
+    L = lib()
+    n, nl, nb, d = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    _check(L.x2g_host_sor_schedule(nnu, nmu, C.byref(n), C.byref(nl), C.byref(nb), C.byref(d),
+                                   None, None, None, None))
+    pts, off = np.zeros(n.value, np.int32), np.zeros(nl.value + 1, np.int32)
+    boff = np.zeros(nb.value + 1, np.int32)
+    _check(L.x2g_host_sor_schedule(nnu, nmu, C.byref(n), C.byref(nl), C.byref(nb), C.byref(d),
+                                   None, None, None, boff.ctypes.data_as(C.POINTER(C.c_int))))
+    bpts = np.zeros(int(boff[-1]), np.int32)
+    ip = [a.ctypes.data_as(C.POINTER(C.c_int)) for a in (pts, off, bpts, boff)]
+    _check(L.x2g_host_sor_schedule(nnu, nmu, C.byref(n), C.byref(nl), C.byref(nb), C.byref(d), *ip))
+    return pts, off, bpts, boff, d.value
 
 
 def host_cluster_chunks(nnu, nmu):

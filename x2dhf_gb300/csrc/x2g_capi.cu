@@ -317,6 +317,13 @@ int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, doubl
   UP(h.pts_rc, pts_rc);
   UP(h.st_pts, st_pts);
   UP(h.st_off, st_off);
+  UP(h.sor_pts, sor_pts);
+  UP(h.sor_off, sor_off);
+  UP(h.sor_bpts, sor_bpts);
+  UP(h.sor_boff, sor_boff);
+  d.sor_nlev = h.sor_nlev;
+  d.sor_nblev = h.sor_nblev;
+  d.sor_delta = h.sor_delta;
   for (int k = 0; k <= HostGrid::kBandRuns; ++k) d.st_rows[k] = h.st_rows[k];
   d.cl_size = h.cl_size;
   d.cl_maxrows = h.cl_maxrows;
@@ -409,7 +416,8 @@ int x2g_grid_info(x2g_grid *gr, int *nnu, int *nmu, int *ntiles, int *nlevels, i
 
 int x2g_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, int nsweeps, int precision) {
   if (!ctx || !grid || (!jobs && njobs > 0) || njobs < 0) return set_status(X2G_ERR_ARG, "null argument");
-  if (precision != X2G_FP64 && precision != X2G_MIXED) return set_status(X2G_ERR_ARG, "unknown precision");
+  if (precision != X2G_FP64 && precision != X2G_MIXED && precision != X2G_SOR)
+    return set_status(X2G_ERR_ARG, "unknown precision");
   return launch_relax(ctx, grid, jobs, njobs, nsweeps, precision);
 }
 

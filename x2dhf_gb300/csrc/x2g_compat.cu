@@ -26,8 +26,9 @@ struct x2g_cb5d { double v[5]; };
 struct x2g_cb45 { double omegac, omega1c; };
 struct x2g_cb46 { int iorbc, isymc, nthreadsc; };
 struct x2g_cbptrd { double *p; };
-struct x2g_cbptri { int *p; };
 struct x2g_cbi4b { int i4barr[20]; };
+struct x2g_cbptri { int *p; };
+struct x2g_cbiadex { int iadex1c, iadex2c, iadex3c, iadextc, iadnorc; };
 
 extern struct x2g_cb1 c_interface_1_ __attribute__((weak));   // ins1
 extern struct x2g_cb1 c_interface_2_ __attribute__((weak));   // ins2
@@ -48,6 +49,8 @@ extern struct x2g_cbptrd c_orbptr_ __attribute__((weak));
 extern struct x2g_cbptrd c_exchptr_ __attribute__((weak));
 extern struct x2g_cbptrd c_supplptr_ __attribute__((weak));
 extern struct x2g_cbi4b c_i4b_ __attribute__((weak));
+extern struct x2g_cbptri c_sorptr_ __attribute__((weak));    // cw_sor: index lists
+extern struct x2g_cbiadex c_iadex_ __attribute__((weak));    // offsets of the lists in cw_sor
 }
 
 using namespace x2g;
@@ -112,19 +115,73 @@ void mcsor_common(int *isym, double *wk2, double *lhs, double *rhs) {
     return;
   }
   if (ensure_grid()) return;
-  x2g_mcsor_host(g_ctx, g_grid, *isym, 0, c_interface_45_.omegac, c_interface_17_.maxsor2c, wk2, lhs, rhs);
+  // maxsor2 sweeps (mcsor_single_colour_pthread.c:54-72); the Fortran
+  // caller runs the macro iterations with putin/putout around each call
+  if (x2g_mcsor_host(g_ctx, g_grid, *isym, 0, c_interface_45_.omegac, c_interface_17_.maxsor2c, wk2, lhs, rhs))
+    return;
+  set_status(X2G_OK, "");
+}
+
+// Which order the extended index list in cw_sor holds (the list sorpt_
+// sweeps, coulExch_pthread.c:42-46): 1 the colour-reordered list of a PT
+// build with the mcsor-ce card (initCBAllocArrays.F90:2221-2240: stable
+// partition of the "middle" list by position mod 5), i.e. single-thread
+// MCSOR; 0 the "middle" list itself, i.e. list-order SOR; -1 neither.
+int sor_list_order() {
+  const std::vector<int> &mid = g_grid->h.order;  // 0-based ext indices, middle order
+  const int n = int(mid.size());
+  const int *lst = c_sorptr_.p + (c_iadex_.iadextc - 1);
+  bool is_mid = true, is_col = true;
+  int j = 0;
+  for (int c = 0; c < 5; c++)
+    for (int i = c; i < n; i += 5, j++) {
+      if (lst[j] != mid[i] + 1) is_col = false;
+      if (lst[j] != mid[j] + 1) is_mid = false;
+    }
+  return is_col ? 1 : (is_mid ? 0 : -1);
+}
+
+// device and pinned host staging of coulExch_pthread_, kept across calls
+double *g_dev = nullptr, *g_pin = nullptr;
+size_t g_dev_n = 0, g_pin_n = 0;
+
+bool stage_buffers(size_t dev_n, size_t pin_n) {
+  if (g_dev_n < dev_n) {
+    if (g_dev) cudaFree(g_dev);
+    g_dev = nullptr;
+    g_dev_n = 0;
+    if (cudaMalloc(&g_dev, dev_n * sizeof(double)) != cudaSuccess) return false;
+    g_dev_n = dev_n;
+  }
+  if (g_pin_n < pin_n) {
+    if (g_pin) cudaFreeHost(g_pin);
+    g_pin = nullptr;
+    g_pin_n = 0;
+    if (cudaMallocHost(&g_pin, pin_n * sizeof(double)) != cudaSuccess) return false;
+    g_pin_n = pin_n;
+  }
+  return true;
 }
 
 // coulExch_pthread_: every potential of orbital iorbc in one launch, with
-// relax_single_pot_pthread.c:74-92's lhs/rhs and putinc/putoutc embedding
+// relax_single_pot_pthread.c:74-92's lhs/rhs and putinc/putoutc embedding,
+// staged in one host-to-device copy and read back in one copy
 void coulexch_common() {
   std::lock_guard<std::mutex> lk(g_mu);
   if (!have_common() || !&c_interface_46_ || !&c_interface_8_ || !&c_orbptr_ || !&c_exchptr_ ||
-      !&c_interface_1_ || !&c_interface_7_) {
+      !&c_interface_1_ || !&c_interface_7_ || !&c_sorptr_ || !&c_iadex_) {
     set_status(X2G_ERR_NO_COMMON, "x2dhf COMMON blocks are not linked");
     return;
   }
   if (ensure_grid()) return;
+  // sorpt_ sweeps whichever list cw_sor holds: colour-reordered = MCSOR in
+  // colour order, middle = list-order SOR
+  const int order = sor_list_order();
+  if (order < 0) {
+    set_status(X2G_ERR_UNSUPPORTED, "cw_sor holds an unrecognised list order; potentials left unchanged");
+    return;
+  }
+  const int form = (order == 1) ? X2G_FP64 : X2G_SOR;
   const int iorb = c_interface_46_.iorbc;
   const int n = c_interface_8_.nexchpotsc[iorb - 1];
   const int nni = g_nni, nmu = g_nmu, mx = nni * nmu;
@@ -136,13 +193,15 @@ void coulexch_common() {
   double *excp = c_exchptr_.p;
   const int maxsor1 = c_interface_17_.maxsor1c, maxsor2 = c_interface_17_.maxsor2c;
   const double omega = c_interface_45_.omegac;
-  double *buf = nullptr;
   const size_t per = size_t(g.next) + 3 * size_t(mx);
-  if (cudaMalloc(&buf, per * n * sizeof(double)) != cudaSuccess) {
+  if (n <= 0) {
+    set_status(X2G_OK, "");
+    return;
+  }
+  if (!stage_buffers(per * n, 3 * size_t(mx) * n)) {
     set_status(X2G_ERR_ALLOC, "coulExch buffers");
     return;
   }
-  std::vector<double> h(size_t(3) * mx);
   std::vector<x2g_job> jobs(n);
   for (int k = 0; k < n; k++) {
     const int in1 = c_interface_1_.v[k][iorb - 1], in2 = c_interface_2_.v[k][iorb - 1];
@@ -151,15 +210,14 @@ void coulexch_common() {
     const int idel = c_interface_4_.v[k][iorb - 1];
     const int isym = c_interface_6_.v[k][iorb - 1];
     const double deltam2 = double(idel * idel);
-    double *rhsh = h.data(), *lhsh = h.data() + mx, *funh = h.data() + 2 * size_t(mx);
+    double *rhsh = g_pin + 3 * size_t(mx) * k, *lhsh = rhsh + mx, *funh = rhsh + 2 * size_t(mx);
     for (int i = 0; i < mx; i++) rhsh[i] = psi[ib1 + i - 1] * psi[ib2 + i - 1] * gf[i];
     for (int i = 0; i < mx; i++) lhsh[i] = (deltam2 == 0.0) ? f3[i] : f3[i] + ef[i] * deltam2;
     std::memcpy(funh, excp + ibexc - 1, mx * sizeof(double));
-    double *base = buf + per * k;
-    cudaMemcpyAsync(base + g.next, h.data(), 3 * size_t(mx) * sizeof(double), cudaMemcpyHostToDevice, g_ctx->stream);
+    double *base = g_dev + per * k;
+    cudaMemcpyAsync(base + g.next, rhsh, 3 * size_t(mx) * sizeof(double), cudaMemcpyHostToDevice, g_ctx->stream);
     count_copy(g_ctx, 3 * size_t(mx) * sizeof(double), 0);
     launch_putin(g_ctx, g, isym, base + g.next + 2 * size_t(mx), base);
-    cudaStreamSynchronize(g_ctx->stream);
     x2g_job &j = jobs[k];
     j.u = base;
     j.rhs = base + g.next;
@@ -169,19 +227,19 @@ void coulexch_common() {
     j.idel = idel;
     j.kind = 1;
   }
-  for (int it = 0; it < maxsor1; it++) launch_relax(g_ctx, g_grid, jobs.data(), n, maxsor2, X2G_FP64);
-  std::vector<double> out(mx);
+  for (int it = 0; it < maxsor1; it++)
+    if (launch_relax(g_ctx, g_grid, jobs.data(), n, maxsor2, form)) return;
   for (int k = 0; k < n; k++) {
-    const int ibexc = c_interface_3_.v[k][iorb - 1];
-    double *base = buf + per * k;
+    double *base = g_dev + per * k;
     launch_putout(g_ctx, g, base, base + g.next + 2 * size_t(mx));
-    cudaMemcpyAsync(out.data(), base + g.next + 2 * size_t(mx), mx * sizeof(double), cudaMemcpyDeviceToHost,
-                    g_ctx->stream);
+    cudaMemcpyAsync(g_pin + 3 * size_t(mx) * k, base + g.next + 2 * size_t(mx), mx * sizeof(double),
+                    cudaMemcpyDeviceToHost, g_ctx->stream);
     count_copy(g_ctx, 0, mx * sizeof(double));
-    if (x2g_synchronize(g_ctx)) break;
-    std::memcpy(excp + ibexc - 1, out.data(), mx * sizeof(double));
   }
-  cudaFree(buf);
+  if (x2g_synchronize(g_ctx)) return;
+  for (int k = 0; k < n; k++)
+    std::memcpy(excp + c_interface_3_.v[k][iorb - 1] - 1, g_pin + 3 * size_t(mx) * k, mx * sizeof(double));
+  set_status(X2G_OK, "");
 }
 
 }  // namespace
@@ -204,6 +262,10 @@ void coulExch_tpool_(void) { coulexch_common(); }
 
 static void release() {
   std::lock_guard<std::mutex> lk(g_mu);
+  if (g_dev) cudaFree(g_dev);
+  if (g_pin) cudaFreeHost(g_pin);
+  g_dev = g_pin = nullptr;
+  g_dev_n = g_pin_n = 0;
   if (g_grid) x2g_grid_destroy(g_grid);
   if (g_ctx) x2g_destroy(g_ctx);
   g_grid = nullptr;

@@ -70,6 +70,16 @@ struct HostGrid {
   static constexpr int kBandRuns = 16;
   std::vector<int> st_pts, st_off;
   int st_rows[kBandRuns + 1] = {};
+  // list-order SOR (sor, sormcsor.F90:20-132) as a pipelined wavefront: an
+  // interior point's SOR level is 1 + the largest level of its stencil
+  // neighbours earlier in the list (their new values are read), an axis
+  // point's level 1 + the largest level of the points its extrapolation
+  // reads (the corners read the mu=1 row); sweep s of a point runs at step
+  // level + s * sor_delta.  sor_pts / sor_bpts hold the interior / axis
+  // points by level, packed (ext row << 16) | ext col, with offsets
+  // sor_off[sor_nlev + 1] / sor_boff[sor_nblev + 1]
+  int sor_nlev = 0, sor_nblev = 0, sor_delta = 0;
+  std::vector<int> sor_pts, sor_off, sor_bpts, sor_boff;
 };
 
 std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf, double z1, double z2, int mpole);
@@ -90,6 +100,8 @@ struct GridDev {
   const int *cl_tile0, *cl_row0, *cl_pts, *cl_off;
   const int *st_pts, *st_off;
   int st_rows[17];
+  const int *sor_pts, *sor_off, *sor_bpts, *sor_boff;
+  int sor_nlev, sor_nblev, sor_delta;
   // FP32 copies of the coefficient tables for the mixed form
   const float *borb_mu32, *bpot_mu32, *d_nu32;
   // separable stencil weights of the mixed form's FP64 residual: for the
@@ -174,6 +186,7 @@ struct x2g_ctx {
   int band_blocks = 0;          // co-resident blocks for that size
   int band_sm_smem = 0;         // shared memory per SM
   int f64_blocks = -1;          // co-resident blocks of the cooperative FP64 sweep on this device
+  int sor_blocks = -1;          // co-resident blocks of the cooperative list-order SOR sweep
   unsigned long long wait_limit_ns = x2g::kDefaultWaitLimitNs;  // device-side wait limit (x2g_set_wait_limit)
   // optional per-launch timing of the sweep kernels (CUDA events on stream)
   int profiling = 0;

@@ -7,6 +7,7 @@
 // FP64 arithmetic that must reproduce the reference bit for bit is written
 // with __dadd_rn/__dmul_rn/__ddiv_rn, which the compiler never contracts
 // into FMAs (the reference was built without FMA contraction).
+#include <algorithm>
 #include <cooperative_groups.h>
 #include <cstdio>
 #include <vector>
@@ -367,6 +368,81 @@ __global__ void __launch_bounds__(kThreads) k_mcsor_f64(GridDev g, const __grid_
     const int jb = item / g.ntiles, t = item - jb * g.ntiles;
     tile_boundary<double>(g, jobs.j[jb].u, t, jobs.j[jb].isym);
     __syncthreads();
+  }
+}
+
+// ----------------------------------------------------------------------
+// List-order SOR (sormcsor.F90:20-132) as a pipelined wavefront over all
+// jobs of the launch: step t updates, for every sweep s still running, the
+// interior points of SOR level t - s * delta and the axis points whose
+// extrapolation after sweep s belongs to that level (the host schedule,
+// build_sor_schedule, proves these updates independent and every read
+// value current), then all blocks meet at the grid barrier.  Reference
+// arithmetic order (relax_f64); a potential's rhs = psa psb g and lhs = f3
+// (+ idel^2 e) are formed per point with the same roundings as
+// relaxPots.F90:81-95.  Ghost cells are refreshed once before the first
+// sweep (putin) and stay fixed, as in the reference.
+// ----------------------------------------------------------------------
+__device__ __forceinline__ void sor_point(const GridDev &g, const JobDev &J, int rc) {
+  const int row = rc >> 16, col = rc & 0xffff, ij = row * g.n8 + col;
+  const int mu = row - 4, nu = col - 4, ik = mu * g.nni + nu;
+  double lhs, rhs;
+  if (J.kind == 1) {
+    lhs = (J.idel2 == 0.0) ? g.f3_mu[mu] : A(g.f3_mu[mu], M(J.idel2, g.e[ik]));
+    rhs = M(M(ldcg(J.psa + ij), ldcg(J.psb + ij)), g.g[ik]);
+  } else {
+    lhs = J.lhs[ik];
+    rhs = J.rhs[ik];
+  }
+  const double *bt = (J.kind >= 1) ? g.bpot_mu : g.borb_mu;
+  relax_f64(J.u, ij, g, bt[mu], g.d_nu[nu], lhs, rhs, J.omega, 1.0 - J.omega);
+}
+
+__device__ __forceinline__ void sor_axis(const GridDev &g, const JobDev &J, int rc) {
+  const int row = rc >> 16, col = rc & 0xffff, ij = row * g.n8 + col;
+  // the mu=1 row extrapolates along mu, the nu=1 / nu=nni columns along nu
+  const int st = (col == 4) ? 1 : (col == g.nni + 3) ? -1 : g.n8;
+  double *u = J.u;
+  double v = 0.0;
+  if (J.isym == 1)
+    v = A(A(A(A(M(g.exeven[0], ldcg(u + ij + st)), M(g.exeven[1], ldcg(u + ij + 2 * st))),
+              M(g.exeven[2], ldcg(u + ij + 3 * st))),
+            M(g.exeven[3], ldcg(u + ij + 4 * st))),
+          M(g.exeven[4], ldcg(u + ij + 5 * st)));
+  u[ij] = v;
+}
+
+__global__ void __launch_bounds__(kThreads) k_sor_f64(GridDev g, const __grid_constant__ JobTable jobs, int njobs,
+                                                      int nsweeps, BarrierDev bar, unsigned nblocks) {
+  for (int item = blockIdx.x; item < njobs * g.ntiles; item += gridDim.x) {
+    const int jb = item / g.ntiles;
+    tile_ghosts(g, jobs.j[jb].u, item - jb * g.ntiles, jobs.j[jb].isym);
+  }
+  if (!grid_barrier(bar, nblocks)) return;
+  const int D = g.sor_delta, NL = g.sor_nlev, NB = g.sor_nblev;
+  const int T = (nsweeps - 1) * D + (NL > NB ? NL : NB);
+  const int gt = int(blockIdx.x * blockDim.x + threadIdx.x), gs = int(gridDim.x * blockDim.x);
+  for (int t = 0; t < T; ++t) {
+    // the (sweep, level) pairs of this step as one index space over all jobs
+    for (int s = 0; s < nsweeps; ++s) {
+      const int l = t - s * D;
+      if (l < 0) break;
+      if (l < NL) {
+        const int b0 = g.sor_off[l], n = g.sor_off[l + 1] - b0;
+        for (int k = gt; k < n * njobs; k += gs) {
+          const int jb = k / n;
+          sor_point(g, jobs.j[jb], g.sor_pts[b0 + k - jb * n]);
+        }
+      }
+      if (l < NB) {
+        const int b0 = g.sor_boff[l], n = g.sor_boff[l + 1] - b0;
+        for (int k = gt; k < n * njobs; k += gs) {
+          const int jb = k / n;
+          sor_axis(g, jobs.j[jb], g.sor_bpts[b0 + k - jb * n]);
+        }
+      }
+    }
+    if (t + 1 < T && !grid_barrier(bar, nblocks)) return;
   }
 }
 
@@ -1846,9 +1922,48 @@ static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, 
   return X2G_OK;
 }
 
+// List-order SOR: jobs in launches of kParamJobs, each one cooperative
+// wavefront launch; the grid holds as many blocks as the widest step needs.
+static int relax_sor(x2g_ctx *ctx, const x2g_grid *grid, const x2g_job *jobs, int njobs, int nsweeps) {
+  const GridDev &g = grid->d;
+  if (ctx->sor_blocks < 0) {
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k_sor_f64, kThreads, 0);
+    if (e != cudaSuccess) return cuda_status(e, "occupancy query");
+    if (per_sm < 1) return set_status(X2G_ERR_CUDA, "cooperative SOR sweep cannot be resident");
+    ctx->sor_blocks = per_sm * ctx->num_sms;
+  }
+  int widest = 0;
+  for (int l = 0; l < g.sor_nlev; ++l) widest = std::max(widest, grid->h.sor_off[l + 1] - grid->h.sor_off[l]);
+  for (int b0 = 0; b0 < njobs; b0 += kParamJobs) {
+    const int nb = (njobs - b0 < kParamJobs) ? njobs - b0 : kParamJobs;
+    JobTable jt{};
+    for (int i = 0; i < nb; ++i)
+      if (!make_job(jobs[b0 + i], jt.j[i])) return set_status(X2G_ERR_ARG, "bad relaxation job");
+    cudaError_t err = cudaMemsetAsync(ctx->bar, 0, 2 * sizeof(unsigned), ctx->stream);
+    if (err != cudaSuccess) return cuda_status(err, "barrier reset");
+    BarrierDev bar{ctx->bar, ctx->bar + 1, reinterpret_cast<int *>(ctx->bar + 2), ctx->wait_limit_ns};
+    const int inflight = std::min(nsweeps, (std::max(g.sor_nlev, g.sor_nblev) + g.sor_delta - 1) / g.sor_delta + 1);
+    const long items = long(nb) * widest * inflight;
+    long want = (items + kThreads - 1) / kThreads;
+    want = std::max(want, long(std::min(nb * g.ntiles, ctx->sor_blocks)));  // the ghost prologue's tiles
+    unsigned nblocks = unsigned(std::min(want, long(ctx->sor_blocks)));
+    if (nblocks < 1) nblocks = 1;
+    int nj = nb, ns = nsweeps;
+    GridDev gd = g;
+    void *args[] = {&gd, &jt, &nj, &ns, &bar, &nblocks};
+    err = cudaLaunchCooperativeKernel((const void *)k_sor_f64, dim3(nblocks), dim3(kThreads), args, 0, ctx->stream);
+    if (err != cudaSuccess) return cuda_status(err, "cooperative SOR launch");
+    ctx->launches += 1;
+  }
+  return X2G_OK;
+}
+
 int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, int nsweeps, int precision) {
   if (njobs <= 0) return X2G_OK;
   if (nsweeps <= 0) return set_status(X2G_ERR_ARG, "nsweeps must be positive");
+  if (precision == X2G_SOR) return relax_sor(ctx, grid, jobs, njobs, nsweeps);
+  if (precision != X2G_FP64 && precision != X2G_MIXED) return set_status(X2G_ERR_ARG, "unknown relaxation form");
   const GridDev &g = grid->d;
   const bool mixed = (precision == X2G_MIXED);
   bool on_chip = mixed && cluster_usable(ctx, g);

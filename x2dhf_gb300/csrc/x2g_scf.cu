@@ -384,6 +384,11 @@ int fock_into(x2g_scf *s, int iorb, double *lhs, double *rhs, double *fa) {
 
 int fock(x2g_scf *s, int iorb) { return fock_into(s, iorb, s->lhs, s->rhs, s->fa); }
 
+// relaxation form of a kind of function: list-order SOR (always FP64) or
+// MCSOR in the case's precision (relaxDriver, doSCF.F90:960-1004)
+int pot_form(const x2g_scf *s) { return s->cs.pot_scheme == 0 ? X2G_SOR : s->cs.precision; }
+int orb_form(const x2g_scf *s) { return s->cs.orb_scheme == 0 ? X2G_SOR : s->cs.precision; }
+
 void potential_jobs(x2g_scf *s, int iorb, std::vector<x2g_job> &jobs) {
   for (const PotSlot &P : s->pots[iorb]) {
     x2g_job j{};
@@ -403,7 +408,7 @@ int relax_potentials(x2g_scf *s, int iorb) {
   std::vector<x2g_job> jobs;
   potential_jobs(s, iorb, jobs);
   s->nsor4pot += long(jobs.size()) * s->cs.maxsor_pot;
-  return launch_relax(s->ctx, s->grid, jobs.data(), int(jobs.size()), s->cs.maxsor_pot, s->cs.precision);
+  return launch_relax(s->ctx, s->grid, jobs.data(), int(jobs.size()), s->cs.maxsor_pot, pot_form(s));
 }
 
 // Batched mode: every orbital's batch (each Coulomb and exchange potential
@@ -413,7 +418,7 @@ int relax_all_potentials(x2g_scf *s) {
   std::vector<x2g_job> jobs;
   for (int i = 1; i <= s->norb; i++) potential_jobs(s, s->norb - i + 1, jobs);
   s->nsor4pot += long(jobs.size()) * s->cs.maxsor_pot;
-  return launch_relax(s->ctx, s->grid, jobs.data(), int(jobs.size()), s->cs.maxsor_pot, s->cs.precision);
+  return launch_relax(s->ctx, s->grid, jobs.data(), int(jobs.size()), s->cs.maxsor_pot, pot_form(s));
 }
 
 int relax_orbital(x2g_scf *s, int iorb) {
@@ -428,7 +433,7 @@ int relax_orbital(x2g_scf *s, int iorb) {
   j.isym = s->isymOrb[iorb];
   j.kind = 0;
   s->nsor4orb += s->cs.maxsor_orb;
-  int rc = launch_relax(s->ctx, s->grid, &j, 1, s->cs.maxsor_orb, s->cs.precision);
+  int rc = launch_relax(s->ctx, s->grid, &j, 1, s->cs.maxsor_orb, orb_form(s));
   if (rc) return rc;
   launch_asympt_set(s->ctx, g, s->orb[iorb], s->edecay);
   return X2G_OK;
@@ -454,7 +459,7 @@ int relax_all_orbitals(x2g_scf *s) {
     jobs.push_back(j);
   }
   s->nsor4orb += long(jobs.size()) * s->cs.maxsor_orb;
-  int rc = launch_relax(s->ctx, s->grid, jobs.data(), int(jobs.size()), s->cs.maxsor_orb, s->cs.precision);
+  int rc = launch_relax(s->ctx, s->grid, jobs.data(), int(jobs.size()), s->cs.maxsor_orb, orb_form(s));
   if (rc) return rc;
   for (int iorb = 1; iorb <= s->norb; iorb++) launch_asympt_set(s->ctx, g, s->orb[iorb], s->bedecay[iorb]);
   return X2G_OK;
@@ -895,10 +900,8 @@ int x2g_scf_create(x2g_ctx *ctx, const x2g_case *c, x2g_scf **out) {
       return set_status(X2G_ERR_UNSUPPORTED, "open-shell configurations with several orbitals are not supported");
   }
   if (c->precision != X2G_FP64 && c->precision != X2G_MIXED) return set_status(X2G_ERR_ARG, "unknown precision");
-  if (c->orb_scheme != 1 || c->pot_scheme != 1)
-    return set_status(X2G_ERR_UNSUPPORTED,
-                      "list-order SOR (a deck without the mcsor-o/mcsor and mcsor-ce cards) is not available on the "
-                      "GPU: set orb_scheme = pot_scheme = 1 (MCSOR)");
+  if (c->orb_scheme < 0 || c->orb_scheme > 1 || c->pot_scheme < 0 || c->pot_scheme > 1)
+    return set_status(X2G_ERR_ARG, "orb_scheme and pot_scheme must be 0 (SOR) or 1 (MCSOR)");
   if (c->batch_mode < 0 || c->batch_mode > 2) return set_status(X2G_ERR_ARG, "batch_mode must be 0, 1 or 2");
   if (c->maxsor_orb < 1 || c->maxsor_pot < 1) return set_status(X2G_ERR_ARG, "sweep counts must be positive");
   auto *s = new x2g_scf();

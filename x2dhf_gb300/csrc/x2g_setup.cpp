@@ -31,6 +31,116 @@ std::vector<double> newton_cotes(int n, double h) {
   return w;
 }
 
+// List-order SOR as a pipelined wavefront.  Sequential SOR over the
+// "middle" list (sormcsor.F90:41-74) followed by the axis extrapolation
+// (:94-129) after every sweep is reproduced exactly when every point update
+// and every axis extrapolation of sweep s runs at step level + s * delta and
+// the updates of one step run in any order: a point reads the new values of
+// its neighbours earlier in the list (lower levels, this sweep), the previous
+// sweep's values of those later in the list and of the axis, and delta makes
+// every such previous-sweep value final before it is read and not yet
+// overwritten.  The ghost cells and the mu >= nmu-3 rows stay fixed during a
+// relaxation call.  Every dependency is checked here; a violation refuses
+// the grid.
+std::string build_sor_schedule(HostGrid &g, const std::vector<int> &pos, const int *offs) {
+  const int npts = int(g.order.size()), n8 = g.n8, nni = g.nni, nmu = g.nmu;
+  std::vector<int> L(npts, 0);
+  int nlev = 0;
+  for (int p = 0; p < npts; ++p) {
+    const int ij = g.order[p];
+    int l = 0;
+    for (int k = 0; k < 16; ++k) {
+      const int q = ij + offs[k];
+      if (q < 0 || q >= g.next || pos[q] < 0 || pos[q] >= p) continue;
+      l = std::max(l, L[pos[q]] + 1);
+    }
+    L[p] = l;
+    nlev = std::max(nlev, l + 1);
+  }
+  // axis points (sormcsor.F90:94-129, lists of mesh:2823-2842): the mu=1
+  // row (ext row 4, cols 5..nni+2) from rows 5..9, then the nu=1 and nu=nni
+  // columns (ext rows 4..nmu-1, cols 4 and nni+3) from the 5 columns inward;
+  // their row-4 corners read the mu=1 row
+  struct Axis {
+    int ij, st;
+  };
+  std::vector<Axis> ax;
+  for (int c = 5; c <= nni + 2; ++c) ax.push_back({4 * n8 + c, n8});
+  for (int r = 4; r < nmu; ++r) {
+    ax.push_back({r * n8 + 4, 1});
+    ax.push_back({r * n8 + nni + 3, -1});
+  }
+  std::vector<int> B(g.next, -1);  // axis level by ext index
+  int nblev = 0;
+  for (const Axis &a : ax) {
+    int b = 0;
+    for (int k = 1; k <= 5; ++k) {
+      const int q = a.ij + k * a.st;
+      const int lq = (pos[q] >= 0) ? L[pos[q]] : B[q];
+      if (lq < 0) return "SOR schedule: an axis point reads neither an interior nor an axis point";
+      b = std::max(b, lq + 1);
+    }
+    B[a.ij] = b;
+    nblev = std::max(nblev, b + 1);
+  }
+  // delta: every value a step reads from the previous sweep is final and
+  // not yet overwritten by the next
+  int delta = 1;
+  for (int p = 0; p < npts; ++p) {
+    const int ij = g.order[p];
+    for (int k = 0; k < 16; ++k) {
+      const int q = ij + offs[k];
+      if (q < 0 || q >= g.next) continue;
+      if (pos[q] > p) delta = std::max(delta, L[pos[q]] - L[p] + 1);  // a later point's old value
+      if (B[q] >= 0) delta = std::max(delta, B[q] - L[p] + 1);        // an axis value
+    }
+  }
+  for (const Axis &a : ax)
+    for (int k = 1; k <= 5; ++k) {
+      const int q = a.ij + k * a.st;
+      const int lq = (pos[q] >= 0) ? L[pos[q]] : B[q];
+      delta = std::max(delta, B[a.ij] - lq + 1);  // read before the next sweep overwrites it
+    }
+  // check every dependency at sweeps s and s+1 (step = level + s * delta)
+  for (int p = 0; p < npts; ++p) {
+    const int ij = g.order[p];
+    for (int k = 0; k < 16; ++k) {
+      const int q = ij + offs[k];
+      if (q < 0 || q >= g.next) continue;
+      if (pos[q] >= 0 && pos[q] < p && !(L[pos[q]] < L[p])) return "SOR schedule: new value read too early";
+      if (pos[q] > p && !(L[pos[q]] > L[p] && L[pos[q]] < L[p] + delta))
+        return "SOR schedule: old value of a later point not preserved";
+      if (B[q] >= 0 && !(B[q] > L[p] && B[q] < L[p] + delta)) return "SOR schedule: axis value out of order";
+    }
+  }
+  for (const Axis &a : ax)
+    for (int k = 1; k <= 5; ++k) {
+      const int q = a.ij + k * a.st;
+      const int lq = (pos[q] >= 0) ? L[pos[q]] : B[q];
+      if (!(lq < B[a.ij] && B[a.ij] < lq + delta)) return "SOR schedule: extrapolation out of order";
+    }
+  g.sor_nlev = nlev;
+  g.sor_nblev = nblev;
+  g.sor_delta = delta;
+  g.sor_off.assign(nlev + 1, 0);
+  for (int p = 0; p < npts; ++p) g.sor_off[L[p] + 1]++;
+  for (int l = 0; l < nlev; ++l) g.sor_off[l + 1] += g.sor_off[l];
+  g.sor_pts.assign(npts, 0);
+  {
+    std::vector<int> fill(g.sor_off.begin(), g.sor_off.end() - 1);
+    for (int p = 0; p < npts; ++p) g.sor_pts[fill[L[p]]++] = ((g.order[p] / n8) << 16) | (g.order[p] % n8);
+  }
+  g.sor_boff.assign(nblev + 1, 0);
+  for (const Axis &a : ax) g.sor_boff[B[a.ij] + 1]++;
+  for (int l = 0; l < nblev; ++l) g.sor_boff[l + 1] += g.sor_boff[l];
+  g.sor_bpts.assign(ax.size(), 0);
+  {
+    std::vector<int> fill(g.sor_boff.begin(), g.sor_boff.end() - 1);
+    for (const Axis &a : ax) g.sor_bpts[fill[B[a.ij]]++] = ((a.ij / n8) << 16) | (a.ij % n8);
+  }
+  return "";
+}
+
 }  // namespace
 
 std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf, double z1, double z2,
@@ -434,7 +544,7 @@ std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf
     if (band_of(ra) != band_of(rb)) return "schedule check: dependency crosses a tile";
     if (!(lev[d.second] > lev[d.first])) return "schedule check: level order violated";
   }
-  return "";
+  return build_sor_schedule(g, pos, offs);
 }
 
 }  // namespace x2g
@@ -538,5 +648,26 @@ extern "C" int x2g_host_cluster_chunks(int nnu, int nmu, int *nchunks, int *noff
   if (noff) *noff = int(g.cl_off.size());
   if (chunks) std::copy(g.cl_pts.begin(), g.cl_pts.end(), chunks);
   if (off) std::copy(g.cl_off.begin(), g.cl_off.end(), off);
+  return X2G_OK;
+}
+
+// Schedule of the list-order SOR wavefront (host only): interior points by
+// SOR level, packed (ext row << 16) | ext col (pts, npoints values; off,
+// nlev + 1 offsets), axis points by the level their extrapolation follows
+// (bpts; boff, nblev + 1 offsets), and the level shift between sweeps.
+// Null arrays: counts only.
+extern "C" int x2g_host_sor_schedule(int nnu, int nmu, int *npoints, int *nlev, int *nblev, int *delta, int *pts,
+                                     int *off, int *bpts, int *boff) {
+  x2g::HostGrid g;
+  std::string msg = x2g::build_host_grid(g, nnu, nmu, 2.0, 40.0, 1.0, 1.0, 4);
+  if (!msg.empty()) return X2G_ERR_SCHEDULE;
+  if (npoints) *npoints = int(g.sor_pts.size());
+  if (nlev) *nlev = g.sor_nlev;
+  if (nblev) *nblev = g.sor_nblev;
+  if (delta) *delta = g.sor_delta;
+  if (pts) std::copy(g.sor_pts.begin(), g.sor_pts.end(), pts);
+  if (off) std::copy(g.sor_off.begin(), g.sor_off.end(), off);
+  if (bpts) std::copy(g.sor_bpts.begin(), g.sor_bpts.end(), bpts);
+  if (boff) std::copy(g.sor_boff.begin(), g.sor_boff.end(), boff);
   return X2G_OK;
 }
