@@ -7,10 +7,14 @@ Workloads (grids after the reference's n = 1 (mod 30) rounding):
   h2   H2 (Z=1,1, R=1.4), grid 169x241 -> 151x241, R_inf = 40
 One step = one full SCF solve from the hydrogenic start to the orbital-energy
 threshold.  `value` is the mixed form (FP32 sweeps + FP64 defect
-correction) with its state already resident in HBM; the plain FP64 form is
-timed beside it.  `e2e` times the public API call a user makes (host case
-description in, host orbitals out) including the host->device upload of the
-initial guess and the device->host readback of every orbital.
+correction) in its batched mode: every Coulomb and exchange potential of an
+SCF iteration relaxed in one launch, then every orbital in one launch, with
+the state already resident in HBM.  Beside it: the plain FP64 form in the
+reference's colour and relaxation order (the comparator), the mixed form in
+the reference's order, and for N2 each form's |dE| against the full FP64
+oracle solve in tests/golden.  `e2e` times the public API call a user makes
+(host case description in, host orbitals out) including the host->device
+upload of the grid tables and the device->host readback of every orbital.
 
 --impl reference times the reference on the host cores: the reference's own C
 relaxation backend (x2dhf src/c, built unmodified into oracle/_ref) under the
@@ -99,16 +103,22 @@ def kf_deck():
     return "\n".join(out) + "\n"
 
 
-WORKLOADS = {"n2": n2_deck, "h2": h2_deck, "kf": kf_deck}
+WORKLOADS = {"n2": n2_deck, "h2": h2_deck, "kf": kf_deck, "kf-solve": kf_deck}
 # workloads timed over a fixed number of SCF iterations per step (a full
 # solve of the large grid takes thousands of iterations)
 FIXED_ITERS = {"kf": 20}
+# full-solve workloads whose warm-up steps run only the first SCF iterations
+# (a warm-up full solve of the plain FP64 form would take minutes)
+WARMUP_ITERS = {"kf-solve": 20}
 WORKLOAD_TEXT = {
     "n2": "N2 closed-shell HF SCF, Z=7,7 R=2.068, 6 orbitals, 22 Poisson solves/iteration, grid 337x481 -> 331x481, "
           "R_inf=40",
     "h2": "H2 HF SCF, Z=1,1 R=1.4, grid 169x241 -> 151x241, R_inf=40",
     "kf": "KF HF SCF, Z=19,9 R=4.1035, 11 orbitals (3 pi, 8 sigma), 72 Poisson solves/iteration, grid 793x1201 -> "
           "781x1201, R_inf=60; first 20 SCF iterations from the hydrogenic start per step",
+    "kf-solve": "KF HF SCF, Z=19,9 R=4.1035, 11 orbitals (3 pi, 8 sigma), 72 Poisson solves/iteration, grid "
+                "793x1201 -> 781x1201, R_inf=60; one full SCF solve per step (warm-up steps: the first 20 "
+                "iterations)",
 }
 
 
@@ -250,6 +260,24 @@ def max_over_ranks(values, world, device):
     return t.tolist()
 
 
+# the N2 workload's full oracle solve (FP64, reference order), written by
+# tests/golden/make_oracle_solves.py: the |dE| of every form against it
+ORACLE_SOLVES = {"n2": os.path.join(ROOT, "tests", "golden", "n2_331x481_oracle.json")}
+# SCF forms timed by the GPU arm: (name, precision, batch mode); the last is
+# the headline `value` (the benchmark spec's batched mixed form)
+SCF_LEGS = (("fp64", 0, 0), ("mixed_reference_order", 1, 0), ("mixed", 1, 2))
+
+
+def oracle_reference(name):
+    try:
+        with open(ORACLE_SOLVES[name]) as f:
+            d = json.load(f)
+        return {"total_energy": d["total_energy"], "orbital_energies": d["orbital_energies"],
+                "iterations": d["iterations"]}
+    except (KeyError, OSError, ValueError):
+        return None
+
+
 def run_gpu(args):
     import torch
     import x2dhf_gb300 as xg
@@ -268,6 +296,7 @@ def run_gpu(args):
     stream = torch.cuda.ExternalStream(xg.lib().x2g_stream(ctx.h))
     deck = WORKLOADS[args.workload]()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    fixed = FIXED_ITERS.get(args.workload, 1 << 30)
 
     def barrier():
         torch.cuda.synchronize()
@@ -277,11 +306,11 @@ def run_gpu(args):
 
     copied = [0, 0, 0]  # host-to-device bytes, device-to-host bytes, timed e2e steps
 
-    def timed_solves(prec, k, warm, e2e=False):
+    def timed_solves(prec, mode, k, warm, e2e=False, cap=None):
         lat, res_last, iters = [], None, []
         for step in range(warm + k):
             if not e2e:
-                case = xg.parse_deck(deck, precision=prec)
+                case = xg.parse_deck(deck, precision=prec, batch_mode=mode)
                 scf = xg.SCF(ctx, case)  # initial guess uploaded: state resident in HBM
             flush_l2(torch, flush)
             barrier()
@@ -290,9 +319,9 @@ def run_gpu(args):
             b0 = ctx.transfer_bytes()
             ev0.record(stream)
             if e2e:
-                case = xg.parse_deck(deck, precision=prec)
+                case = xg.parse_deck(deck, precision=prec, batch_mode=mode)
                 scf = xg.SCF(ctx, case)
-            res = scf.run(FIXED_ITERS.get(args.workload, 1 << 30))
+            res = scf.run(cap if cap else (fixed if step >= warm else WARMUP_ITERS.get(args.workload, fixed)))
             if e2e:
                 for i in range(1, case.norb + 1):
                     scf.orbital(i)
@@ -312,61 +341,80 @@ def run_gpu(args):
             scf.close()
         return lat, res_last, iters
 
-    out = {}
+    legs = [lg for lg in SCF_LEGS if args.legs == "all" or lg[0] == args.legs]
+    head = legs[-1]
     sampler = ClockSampler(local)
-    run64 = args.legs in ("all", "fp64")
-    runmx = args.legs in ("all", "mixed")
-    lat64, res64, it64, ms64, pts64, n64 = [1.0], None, [], 0.0, 0.0, 0
-    latmx, resmx, itmx, msmx, ptsmx, nmx, launches_mx = [1.0], None, [], 0.0, 0.0, 0, 0
-    late2e = [1.0]
+    lat, res, its = {}, {}, {}
+    launches = 0
     ctx.profile(0, xg.FP64)  # the timed steps run without the library's per-launch events
     with sampler:
-        if run64:
-            lat64, res64, it64 = timed_solves(xg.FP64, args.steps, args.warmup)
-        if runmx:
+        for name, prec, mode in legs:
+            # the plain FP64 form is the slow comparator: a few timed solves
+            k = args.steps if name != "fp64" or len(legs) == 1 else min(args.steps, args.fp64_steps)
             l0 = ctx.launches
-            # launches of the timed mixed solves (the warm-up ones counted out)
-            latmx, resmx, itmx = timed_solves(xg.MIXED, args.steps, args.warmup)
-            launches_mx = int((ctx.launches - l0) * args.steps / (args.steps + args.warmup))
-            late2e, rese2e, _ = timed_solves(xg.MIXED, max(1, args.steps // 2), 1, e2e=True)
+            lat[name], res[name], its[name] = timed_solves(prec, mode, k, args.warmup)
+            if name == head[0]:
+                # launches of the timed headline solves (the warm-up ones counted out)
+                launches = int((ctx.launches - l0) * k / (k + args.warmup))
+        late2e, rese2e, _ = timed_solves(head[1], head[2], max(1, args.steps // 2), 1, e2e=True)
     # roofline figures: one more step of each form with the library's
-    # per-launch CUDA events on (recorded on its own stream), not timed
-    if runmx:
-        ctx.profile(2, xg.MIXED)
-        timed_solves(xg.MIXED, 1, 0)
-        msmx, ptsmx, nmx = ctx.profile(-1, xg.MIXED)
-    if run64:
-        ctx.profile(2, xg.FP64)
-        timed_solves(xg.FP64, 1, 0)
-        ms64, pts64, n64 = ctx.profile(-1, xg.FP64)
+    # per-launch CUDA events on (recorded on its own stream), not timed; a
+    # long full-solve workload profiles its first iterations only
+    prof = {}
+    for name, prec, mode in legs:
+        if name == "mixed_reference_order":
+            continue
+        ctx.profile(2, prec)
+        timed_solves(prec, mode, 1, 0, cap=WARMUP_ITERS.get(args.workload))
+        prof[name] = ctx.profile(-1, prec)
     ctx.profile(0, xg.FP64)
     # max over ranks: the slowest replica sets the pace
-    tot64, totmx, tote2e = max_over_ranks([sum(lat64), sum(latmx), sum(late2e)], world, f"cuda:{local}")
+    names = list(lat)
+    tot = max_over_ranks([sum(lat[n]) for n in names] + [sum(late2e)], world, f"cuda:{local}")
+    tot, tote2e = dict(zip(names, tot[:-1])), tot[-1]
     if rank != 0:
         return None
     hbm, peak_kind = peaks()
-    grid_pts = None
     c = xg.parse_deck(deck)
-    # per-launch figures of the dominant kernel of the headline (mixed) run
-    sweep_gbs_mx = ptsmx * BYTES_PER_PT[1] / (msmx / 1e3) / 1e9 if msmx > 0 else None
-    sweep_gbs_64 = pts64 * BYTES_PER_PT[0] / (ms64 / 1e3) / 1e9 if ms64 > 0 else None
     per_step = FIXED_ITERS.get(args.workload, 1)  # solves, or iterations for a fixed-iteration workload
     unit = "SCF iterations/s" if args.workload in FIXED_ITERS else UNIT
     metric = (f"SCF iterations/s over the first {per_step} iterations: mixed vs FP64 MCSOR, 1 GB300"
               if args.workload in FIXED_ITERS else METRIC)
-    value = world * args.steps * per_step / totmx
-    fp64_value = world * args.steps * per_step / tot64
+    rate = {n: world * len(lat[n]) * per_step / tot[n] for n in names}
+    value = rate[head[0]]
     e2e_value = world * len(late2e) * per_step / tote2e
     on_chip = xg.host_cluster_plan(c.nnu, c.nmu)[0] > 0
-    mx_sorted = sorted(latmx)
-    p99 = mx_sorted[min(len(mx_sorted) - 1, int(round(0.99 * (len(mx_sorted) - 1))))]
+    hs = sorted(lat[head[0]])
+    p99 = hs[min(len(hs) - 1, int(round(0.99 * (len(hs) - 1))))]
     # bytes the library copied per timed e2e step (grid tables up; per-iteration
     # scalars and the orbitals down), from its own transfer counters
     h2d = copied[0] // max(1, copied[2])
     d2h = copied[1] // max(1, copied[2])
+    msmx, ptsmx, nmx = prof.get(head[0], (0.0, 0.0, 0)) if head[1] == 1 else (0.0, 0.0, 0)
+    ms64, pts64, n64 = prof.get("fp64", (0.0, 0.0, 0))
+    sweep_gbs_mx = ptsmx * BYTES_PER_PT[1] / (msmx / 1e3) / 1e9 if msmx > 0 else None
+    sweep_gbs_64 = pts64 * BYTES_PER_PT[0] / (ms64 / 1e3) / 1e9 if ms64 > 0 else None
     pts_per_launch = ptsmx / nmx if nmx else None
     traffic = ((CLUSTER_DRAM_BYTES_PER_PT if on_chip else BAND_DRAM_BYTES_PER_PT) * pts_per_launch
                if pts_per_launch else None)
+    oref = oracle_reference(args.workload)
+    fp64_e = res["fp64"].total_energy if "fp64" in res else None
+
+    def form(n):
+        r = res[n]
+        d = {"value": rate[n], "unit": unit, "iterations": its[n], "total_energy": r.total_energy,
+             "orbital_energies": [r.ee[i] for i in range(c.norb)], "sweeps": r.sweeps,
+             "latency_p50_s": statistics.median(lat[n]),
+             "batch_mode": dict((x[0], x[2]) for x in SCF_LEGS)[n]}
+        if fp64_e is not None and n != "fp64":
+            d["dE_vs_fp64"] = abs(r.total_energy - fp64_e)
+            d["max_dee_vs_fp64"] = max(abs(r.ee[i] - res["fp64"].ee[i]) for i in range(c.norb))
+            d["speedup_vs_fp64"] = rate[n] / rate["fp64"]
+        if oref and args.workload not in FIXED_ITERS:
+            d["dE_vs_fp64_oracle"] = abs(r.total_energy - oref["total_energy"])
+            d["max_dee_vs_fp64_oracle"] = max(abs(r.ee[i] - oref["orbital_energies"][i]) for i in range(c.norb))
+        return d
+
     out = {
         "metric": metric,
         "value": value,
@@ -374,23 +422,20 @@ def run_gpu(args):
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": 1e3 * totmx / args.steps,
+        "ms_per_step": 1e3 * tot[head[0]] / len(lat[head[0]]),
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32 sweeps + f64 defect correction (value); f64 (fp64 leg)",
         "data": "synthetic: hydrogenic LCAO start of the reference's own input deck, no dataset",
         "config": workload_config(args.workload),
-        "latency_s": {"p50": statistics.median(latmx), "p99": p99,
-                      "fp64_p50": statistics.median(lat64) if run64 else None},
-        "fp64": {"value": fp64_value if run64 else None, "unit": unit, "iterations": it64,
-                 "total_energy": res64.total_energy if res64 else None, "sweeps": res64.sweeps if res64 else None},
-        "mixed": {"iterations": itmx, "total_energy": resmx.total_energy if resmx else None,
-                  "sweeps": resmx.sweeps if resmx else None,
-                  "dE_vs_fp64": abs(resmx.total_energy - res64.total_energy) if (resmx and res64) else None,
-                  "speedup_vs_fp64": value / fp64_value if run64 else None},
+        "form": {"value": f"{head[0]}: FP32 MCSOR sweeps + FP64 defect correction, "
+                          + ("every potential of an SCF iteration in one launch, then every orbital in one "
+                             "launch (batch mode 2)" if head[2] == 2 else "the reference's relaxation order"),
+                 "fp64": "plain form: FP64 MCSOR in the reference's colour order and relaxation order"},
+        "latency_s": {"p50": statistics.median(lat[head[0]]), "p99": p99},
         "e2e": {"value": e2e_value, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": launches_mx,
+        "gpu_launches": launches,
         "roofline": {
             "bound": "hbm",
             "kernel": ("k_mixed_cluster (mixed-form FP32 correction sweeps, one 16-CTA cluster per relaxation job, "
@@ -406,11 +451,8 @@ def run_gpu(args):
                      "memory during the sweeps, so DRAM traffic is far below it and the launch is bound by the "
                      "colour-phase latency (cluster barrier + shared-memory pipe), not by HBM" if on_chip else
                      "achieved = 16 algorithmic B per point-update / launch time; the correction stays in shared "
-                     "memory for the whole launch (each colour phase reloads only the 4-row halos from L2 and "
-                     "writes back only the points within 4 rows of a shared band edge) and the (residual, "
-                     "omega/lhs) pairs stream once per sweep, so DRAM traffic stays far below the algorithmic "
-                     "bytes and the launch is bound by phase latency (neighbour wait, halo round trip, level chain), "
-                     "not by HBM"),
+                     "memory for the whole launch, so DRAM traffic stays far below the algorithmic bytes and the "
+                     "launch is bound by phase latency (neighbour wait, halo round trip, level chain), not by HBM"),
             "sweep_ms_total": msmx, "sweep_launches": nmx, "point_updates": ptsmx,
             "point_updates_per_launch": pts_per_launch,
             "fp64_kernel": {"kernel": "k_mcsor_f64", "achieved_gbs": sweep_gbs_64,
@@ -421,6 +463,10 @@ def run_gpu(args):
         },
         "clocks": sampler.summary(),
     }
+    for n in names:
+        out[n] = form(n)
+    if oref:
+        out["fp64_oracle"] = dict(oref, source="tests/golden/n2_331x481_oracle.json (FP64 oracle, reference order)")
     if not args.no_cpu_baseline:
         nthreads = min(16, os.cpu_count() or 1)
         out["cpu_baseline"] = cpu_baseline(args.workload, deck,
@@ -429,10 +475,19 @@ def run_gpu(args):
     return out
 
 
+POISSON_BATCHES = (16, 64, 256)
+
+
 def run_poisson(args):
-    """Batched Poisson relaxation (R=2.0, 337x481 -> 331x481, R_inf=40): B
-    independent potentials psi_a psi_b g, one relaxation call of 10 MCSOR
-    sweeps each, all B in one persistent launch.  Reports point-updates/s."""
+    """Batched Poisson relaxation (survey config 2: R=2.0, 337x481 ->
+    331x481, R_inf=40): B independent potentials with sources psi_a psi_b g
+    from seeded Slater functions, one relaxation call of 10 MCSOR sweeps
+    each, every B in {16, 64, 256} in the plain FP64 form and in the mixed
+    form (FP32 sweeps + FP64 defect correction).  A step is one relaxation
+    call over the whole batch; reports point-updates/s per (B, form), the
+    sweep kernels' algorithmic GB/s from a separate profiled step, and the
+    mixed form's largest deviation from the FP64 result relative to the
+    change the call made."""
     import numpy as np
     import torch
     import x2dhf_gb300 as xg
@@ -444,52 +499,90 @@ def run_poisson(args):
     grid = xg.Grid(ctx, nnu, nmu, r, rinf, 1.0, 1.0)
     dev = torch.device("cuda:0")
     n8, m8 = nnu + 8, nmu + 8
-    src = slater_sources(rinf, nnu, nmu, r, args.batch)
     omega_orb, omega_pot = C_double_pair(xg, nnu, nmu)
-    jobs, keep = [], []
-    for pa, pb in src:
-        ua = torch.zeros(m8, n8, dtype=torch.float64, device=dev)
-        ub = torch.zeros_like(ua)
-        ua[4:nmu + 4, 4:nnu + 4] = torch.from_numpy(pa[0])
-        ub[4:nmu + 4, 4:nnu + 4] = torch.from_numpy(pb[0])
-        u = torch.zeros_like(ua)
-        idel = abs(pa[1] - pb[1])
-        keep += [ua, ub, u]
-        jobs.append(xg.Job(u=u.data_ptr(), psa=ua.data_ptr(), psb=ub.data_ptr(), omega=omega_pot,
-                           isym=1 if idel % 2 == 0 else -1, idel=idel, kind=1))
-    torch.cuda.synchronize()
     stream = torch.cuda.ExternalStream(xg.lib().x2g_stream(ctx.h))
-    prec = xg.MIXED if args.precision == "mixed" else xg.FP64
-    for _ in range(args.warmup):
-        xg.relax(ctx, grid, jobs, 10, prec)
-    ctx.synchronize()
-    ctx.profile(2, prec)
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    for _ in range(args.steps):
-        xg.relax(ctx, grid, jobs, 10, prec)
-    ev1.record(stream)
-    ctx.synchronize()
-    ms = ev0.elapsed_time(ev1)
-    kms, pts, nl = ctx.profile(-1, prec)
-    pts_step = len(jobs) * (nnu - 2) * (nmu - 5) * 10
+    batches = [args.batch] if args.batch else list(POISSON_BATCHES)
+    forms = [args.precision] if args.precision else ["fp64", "mixed"]
     hbm, peak_kind = peaks()
-    bpp = BYTES_PER_PT[1 if prec == xg.MIXED else 0]
-    gbs = pts * bpp / (kms / 1e3) / 1e9
-    return {"metric": "point-updates/s (batched Poisson MCSOR)", "value": pts_step * args.steps / (ms / 1e3),
+    runs = []
+    sampler = ClockSampler(0)
+    with sampler:
+        for B in batches:
+            src = slater_sources(rinf, nnu, nmu, r, B)
+            keep, start = [], []
+            for pa, pb in src:
+                ua = torch.zeros(m8, n8, dtype=torch.float64, device=dev)
+                ub = torch.zeros_like(ua)
+                ua[4:nmu + 4, 4:nnu + 4] = torch.from_numpy(pa[0])
+                ub[4:nmu + 4, 4:nnu + 4] = torch.from_numpy(pb[0])
+                keep += [ua, ub]
+                start.append((ua, ub, abs(pa[1] - pb[1])))
+            results = {}
+            for form in forms:
+                prec = xg.MIXED if form == "mixed" else xg.FP64
+                us = [torch.zeros(m8, n8, dtype=torch.float64, device=dev) for _ in start]
+                jobs = [xg.Job(u=u.data_ptr(), psa=ua.data_ptr(), psb=ub.data_ptr(), omega=omega_pot,
+                               isym=1 if idel % 2 == 0 else -1, idel=idel, kind=1)
+                        for u, (ua, ub, idel) in zip(us, start)]
+                torch.cuda.synchronize()
+                # the first call from zero is the result compared between the forms
+                xg.relax(ctx, grid, jobs, 10, prec)
+                ctx.synchronize()
+                results[form] = [u.clone() for u in us]
+                for _ in range(args.warmup):
+                    xg.relax(ctx, grid, jobs, 10, prec)
+                ctx.synchronize()
+                ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                ev0.record(stream)
+                for _ in range(args.steps):
+                    xg.relax(ctx, grid, jobs, 10, prec)
+                ev1.record(stream)
+                ctx.synchronize()
+                ms = ev0.elapsed_time(ev1) / args.steps
+                ctx.profile(2, prec)
+                xg.relax(ctx, grid, jobs, 10, prec)
+                ctx.synchronize()
+                kms, pts, nl = ctx.profile(-1, prec)
+                ctx.profile(0, prec)
+                pts_step = B * (nnu - 2) * (nmu - 5) * 10
+                bpp = BYTES_PER_PT[1 if prec == xg.MIXED else 0]
+                gbs = pts * bpp / (kms / 1e3) / 1e9
+                runs.append({"batch": B, "form": form, "point_updates_per_s": pts_step / (ms / 1e3), "ms_per_call": ms,
+                             "sweep_kernel_gbs": gbs, "frac": gbs / hbm, "sweep_kernel_ms": kms,
+                             "sweep_launches": nl,
+                             "fp64_tflops": (pts * FLOPS_PER_PT / (kms / 1e3) / 1e12) if prec == xg.FP64 else None})
+            if "fp64" in results and "mixed" in results:
+                worst = 0.0
+                for a, b in zip(results["fp64"], results["mixed"]):
+                    worst = max(worst, float((a - b).abs().max() / a.abs().max()))
+                for run in runs:
+                    if run["batch"] == B and run["form"] == "mixed":
+                        run["max_rel_dev_vs_fp64"] = worst
+            del keep
+    head = [x for x in runs if x["form"] == forms[-1]][-1]
+    return {"metric": "point-updates/s (batched Poisson MCSOR)", "value": head["point_updates_per_s"],
             "unit": "point-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms / args.steps, "higher_is_better": True, "dtype": args.precision,
-            "config": {"workload": f"poisson: B={args.batch} Slater-product sources, 331x481, R=2.0, "
-                                   "R_inf=40, 10 MCSOR sweeps per solve"},
-            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
-                         "peak_kind": peak_kind, "kernel_ms": kms, "launches": nl, "traffic": None}}
+            "ms_per_step": head["ms_per_call"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 sweeps + f64 defect correction (mixed); f64 (fp64)", "data": "synthetic: seeded Slater sources",
+            "config": {"workload": f"poisson: B={batches} Slater-product sources (exponents U[0.5,8], l<=3, m<=2), "
+                                   "331x481, R=2.0, R_inf=40, 10 MCSOR sweeps per solve, FP64 and mixed",
+                       "l2": "not flushed: the B=16 batch (~64 MB) fits in L2, B=64 and B=256 (~0.26 and ~1 GB) "
+                             "exceed it"},
+            "runs": runs,
+            "roofline": {"bound": "hbm", "achieved": head["sweep_kernel_gbs"], "peak": hbm, "unit": "GB/s",
+                         "frac": head["frac"], "peak_kind": peak_kind, "traffic": None,
+                         "kernel": f"{head['form']} sweep kernel at B={head['batch']}"},
+            "clocks": sampler.summary()}
 
 
 def run_serve(args):
     """Serving loop (survey config 5): seeded Poisson arrivals of closed-shell
-    diatomic HF solves (H2, LiH, FH, CO, N2 decks of the reference, bond
-    length +-10 %, grids 151..241 x 241..361, R_inf=40), `--slots` concurrent
-    solves on one GPU, mixed form and FP64 form on the same request stream."""
+    diatomic HF solves (H2, LiH, FH, CO, N2 decks of the reference; bond
+    length U[1.5, 5.0] bohr within [0.8, 1.5] x the deck's; grids 169..505 x
+    241..721 before rounding, R_inf=40), `--slots` concurrent solves on one
+    GPU, each in the batched mode; the mixed form and the FP64 form on the
+    same request stream, and the mixed form again under an HBM budget of 1.2
+    times the largest request, which admits one large solve at a time."""
     import x2dhf_gb300 as xg
     from x2dhf_gb300 import build, serve
 
@@ -501,27 +594,32 @@ def run_serve(args):
     reqs = serve.make_requests(templates, args.requests, rate=args.rate, seed=42)
     # warm-up: one request per template, not timed
     warm = [q for i, q in enumerate(reqs) if q.template not in {r.template for r in reqs[:i]}]
+    tight = int(1.2 * max(q.bytes for q in reqs))
     out = {}
     sampler = ClockSampler(0)
     with sampler:
-        for name, prec in (("mixed", xg.MIXED), ("fp64", xg.FP64)):
-            srv = serve.Server(slots=args.slots, precision=prec)
+        for name, prec, budget in (("mixed", xg.MIXED, 64 << 30), ("fp64", xg.FP64, 64 << 30),
+                                   ("mixed_tight_budget", xg.MIXED, tight)):
+            srv = serve.Server(slots=args.slots, precision=prec, hbm_budget=budget)
             srv.run(warm, realtime=False)
             done, wall = srv.run(reqs)
-            out[name] = dict(serve.summary(done, wall), peak_footprint_bytes=srv.peak_bytes)
+            out[name] = dict(serve.summary(done, wall), peak_footprint_bytes=srv.peak_bytes, hbm_budget_bytes=budget,
+                             budget_waits=srv.budget_waits)
             out[name + "_energies"] = [c.total_energy for c in done]
     de = max(abs(a - b) for a, b in zip(out["mixed_energies"], out["fp64_energies"]))
+    same = out["mixed_energies"] == out["mixed_tight_budget_energies"]
     mx, f64 = out["mixed"], out["fp64"]
     return {"metric": "served SCF solves/s and p99 latency (Poisson arrivals), mixed vs FP64", "value":
             mx["solves_per_s"], "unit": "SCF solves/s", "n_gpus": 1, "steps": 1, "warmup": 1,
             "ms_per_step": 1e3 * mx["wall_s"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 sweeps + f64 defect correction", "data": "synthetic: seeded request stream",
             "config": {"workload": f"serve: {args.requests} requests, rate {args.rate}/s, {args.slots} slots, "
-                                   "H2/LiH/FH/CO/N2, R +-10 %, grids 151..241 x 241..361, R_inf=40"},
+                                   "H2/LiH/FH/CO/N2, R in U[1.5,5.0] within [0.8,1.5] x R_eq, grids 169..505 x "
+                                   "241..721 -> 151..481 x 241..721, R_inf=40, batched SCF mode"},
             "latency_s": {"p50": mx["latency_p50_s"], "p99": mx["latency_p99_s"],
                           "fp64_p50": f64["latency_p50_s"], "fp64_p99": f64["latency_p99_s"]},
-            "mixed": {k: v for k, v in mx.items()}, "fp64": {k: v for k, v in f64.items()},
-            "max_dE_mixed_vs_fp64": de, "clocks": sampler.summary()}
+            "mixed": mx, "fp64": f64, "mixed_tight_budget": out["mixed_tight_budget"],
+            "max_dE_mixed_vs_fp64": de, "tight_budget_energies_identical": same, "clocks": sampler.summary()}
 
 
 def C_double_pair(xg, nnu, nmu):
@@ -540,8 +638,13 @@ REF_FULL_SOLVE = {"h2"}
 
 
 def ref_solve_record(name):
-    with open(REF_SOLVES) as f:
-        return json.load(f)[name]
+    """The full reference solve of a workload (None when there is none: a
+    solve of the largest grid on the host cores would take hours)."""
+    try:
+        with open(REF_SOLVES) as f:
+            return json.load(f).get(name)
+    except (OSError, ValueError):
+        return None
 
 
 def _ref_backend(deck, nthreads):
@@ -645,7 +748,7 @@ def cpu_baseline(name, deck, sample_iters, nthreads, kernels=True):
     """The reference's C relaxation kernels (one thread per potential,
     mcsor_pthread_ on `nthreads` threads) under the oracle's SCF driver on a
     bounded sample of the same workload, plus the per-kernel sweep rates."""
-    if name in FIXED_ITERS:
+    if name in FIXED_ITERS or (name not in REF_FULL_SOLVE and ref_solve_record(name) is None):
         setup, per_iter, kind = cpu_sample(deck, sample_iters, nthreads)
         out = {"value": 1.0 / per_iter, "unit": "SCF iterations/s", "cores": nthreads, "kind": kind,
                "sample": f"setup + prepSCF + 1 iteration ({setup:.2f} s), then {sample_iters} timed SCF "
@@ -680,6 +783,9 @@ def run_reference(args):
     if rank != 0:
         return None
     name = args.workload
+    if name not in FIXED_ITERS and name not in REF_FULL_SOLVE and ref_solve_record(name) is None:
+        return {"impl": "reference", "unavailable": "no full reference solve of this workload is on record (hours on "
+                                                    "the host cores); the kf workload times its SCF iterations"}
     deck = WORKLOADS[name]()
     nthreads = min(16, os.cpu_count() or 1)
     walls, vals, kind, note = [], [], "port", ""
@@ -697,6 +803,7 @@ def run_reference(args):
         else:
             rec = ref_solve_record(name)
             setup, per_iter, kind = cpu_sample(deck, args.cpu_iters, nthreads)
+            assert rec is not None
             v = 1.0 / (setup + per_iter * (rec["iterations"] - 1))
             note = (f"per step: setup + prepSCF + {1 + args.cpu_iters} SCF iterations on {nthreads} threads; the "
                     f"solve rate scales the timed iterations to the {rec['iterations']} iterations of a full "
@@ -736,10 +843,14 @@ def main():
     ap.add_argument("--slots", type=int, default=4, help="serve workload: concurrent solves")
     ap.add_argument("--cpu-iters", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--legs", default="all", choices=["all", "mixed", "fp64"],
-                    help="SCF workloads: time both forms (default) or one (for profiling runs)")
-    ap.add_argument("--batch", type=int, default=64, help="poisson workload: independent solves per launch")
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"], help="poisson workload")
+    ap.add_argument("--legs", default="all", choices=["all"] + [lg[0] for lg in SCF_LEGS],
+                    help="SCF workloads: time every form (default) or one (for profiling runs)")
+    ap.add_argument("--fp64-steps", type=int, default=3,
+                    help="SCF workloads: timed solves of the slow plain FP64 comparator")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="poisson workload: one batch size (default: every size of the configuration)")
+    ap.add_argument("--precision", default="", choices=["", "mixed", "fp64"],
+                    help="poisson workload: one form (default: both)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

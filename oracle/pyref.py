@@ -93,9 +93,9 @@ class ReferenceSCF:
         O.x2o_set_hooks.argtypes = [C.c_void_p, POT_HOOK, ORB_HOOK, C.c_void_p]
         h = self.case.h
         norb, mx = self.case.norb, self.case.mxsize
-        L.x2r_set_functions.argtypes = [C.c_void_p, np.ctypeslib.ndpointer(np.int32), C.c_int, C.c_void_p]
+        set_functions = C.CFUNCTYPE(None, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p)(("x2r_set_functions", L))
         self.i1b = np.array([1 + i * mx for i in range(norb)], np.int32)
-        L.x2r_set_functions(O.x2o_orbital_block(h), self.i1b, norb, O.x2o_potential_block(h))
+        set_functions(O.x2o_orbital_block(h), self.i1b.ctypes.data, norb, O.x2o_potential_block(h))
         self.batches = []
         for iorb in range(1, norb + 1):
             n = self.case.npots(iorb)
@@ -105,7 +105,9 @@ class ReferenceSCF:
             L.x2r_set_batch(iorb, n, arr[0], arr[1], ib, arr[2], arr[3])
             self.batches.append(arr + [ib])
         oo, op = self.case.omega()
-        L.x2r_mcsor.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        # the orbital hook passes raw pointers: a separately typed handle of
+        # x2r_mcsor, leaving RefKernels' array-typed one untouched
+        mcsor_vp = C.CFUNCTYPE(None, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p)(("x2r_mcsor", L))
 
         def pot(ud, iorb):
             L.x2r_use_colour_lists(1)
@@ -114,7 +116,7 @@ class ReferenceSCF:
 
         def orb(ud, iorb, isym, wk2, lhs, rhs):
             L.x2r_set_omega(oo)
-            L.x2r_mcsor(isym, nthreads, wk2, lhs, rhs)
+            mcsor_vp(isym, nthreads, wk2, lhs, rhs)
 
         self._pot, self._orb = POT_HOOK(pot), ORB_HOOK(orb)
         O.x2o_set_hooks(h, self._pot, self._orb, None)

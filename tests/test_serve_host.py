@@ -24,7 +24,9 @@ def test_requests_are_reproducible_and_valid():
         c = xg.parse_deck(q.deck)
         assert (c.nnu, c.nmu) == (q.nnu, q.nmu)
         assert (q.nnu - 1) % 30 == 0 and (q.nmu - 1) % 30 == 0
-        assert 151 <= q.nnu <= 241 and 241 <= q.nmu <= 361
+        assert 151 <= q.nnu <= 481 and 241 <= q.nmu <= 721
+        r0 = {"h2": 1.4, "lih": 3.015, "fh": 1.7328, "co": 2.132, "n2": 2.068}[q.template]
+        assert max(1.5, 0.8 * r0) <= q.r <= min(5.0, 1.5 * r0)
         assert round(c.z1 + c.z2) == electrons[q.template] and max(c.z1, c.z2) <= 9
         assert sum(c.occ[i] for i in range(c.norb)) == electrons[q.template]
         assert q.bytes > 0
@@ -61,6 +63,7 @@ def test_admission_fifo_and_budget(slots, budget_factor):
     assert [c.rid for c in done] == [q.rid for q in reqs]
     assert be.order == sorted(be.order)  # first in, first out
     assert srv.peak_bytes <= budget
+    assert (srv.budget_waits > 0) == (slots > 1 and budget_factor < 10)
     assert all(c.iterations == 10 + c.rid and c.total_energy == -float(c.rid) for c in done)
     s = serve.summary(done, wall)
     assert s["requests"] == 30 and s["latency_p99_s"] >= s["latency_p50_s"] > 0

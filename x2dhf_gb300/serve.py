@@ -17,9 +17,13 @@ the GPU.
 The request mix follows the serving configuration of the survey: seeded
 Poisson arrivals; closed-shell diatomics with 2, 4, 10 and 14 electrons and
 nuclear charges up to 9, each from one of the reference's own input decks
-(its hydrogenic LCAO start), with the bond length drawn within +-10 % of the
-deck's and the grid drawn from N_nu in [169, 265] and N_mu in [241, 361]
-before the reference's n = 1 (mod 30) rounding, R_inf = 40.
+(its hydrogenic LCAO start), with the grid drawn from N_nu in [169, 505] and
+N_mu in [241, 721] before the reference's n = 1 (mod 30) rounding, R_inf =
+40, and the bond length drawn from U[1.5, 5.0] bohr restricted to [0.8, 1.5]
+times the deck's bond length (further out the restricted closed-shell start
+dissociates and no longer converges).  Every solve relaxes all potentials
+of an SCF iteration in one launch and then all orbitals in one launch
+(x2g_case.batch_mode 2).
 """
 import dataclasses
 import statistics
@@ -109,9 +113,10 @@ def make_requests(templates, n, rate, seed=42):
         name = names[int(rng.integers(0, len(names)))]
         base = templates[name]
         r0 = next(float(ln.split()[3]) for ln in base.splitlines() if ln.strip().lower().startswith("nuclei"))
-        r = r0 * float(rng.uniform(0.9, 1.1))
-        nnu = round_grid(int(rng.integers(169, 266)))
-        nmu = round_grid(int(rng.integers(241, 362)))
+        lo, hi = max(1.5, 0.8 * r0), min(5.0, 1.5 * r0)
+        r = float(rng.uniform(lo, hi))
+        nnu = round_grid(int(rng.integers(169, 506)))
+        nmu = round_grid(int(rng.integers(241, 722)))
         deck = request_deck(base, r, nnu, nmu)
         case = parse_deck(deck)
         out.append(Request(i, name, t, r, case.nnu, case.nmu, deck, case.norb, footprint_bytes(case)))
@@ -121,15 +126,16 @@ def make_requests(templates, n, rate, seed=42):
 class GpuBackend:
     """Solves on the GPU: one library context (own stream) per slot."""
 
-    def __init__(self, device=0, precision=MIXED):
+    def __init__(self, device=0, precision=MIXED, batch_mode=2):
         self.device = device
         self.precision = precision
+        self.batch_mode = batch_mode
 
     def open(self):
         return Context(self.device)
 
     def solve(self, ctx, q):
-        s = SCF(ctx, parse_deck(q.deck, precision=self.precision))
+        s = SCF(ctx, parse_deck(q.deck, precision=self.precision, batch_mode=self.batch_mode))
         try:
             res = s.run()
             return res.iterations, res.converged, res.total_energy, tuple(float(res.ee[i]) for i in range(q.norb))
@@ -144,11 +150,12 @@ class Server:
     """`slots` concurrent SCF solves under an HBM budget; `backend` opens a
     per-slot handle and solves one request on it (default: the GPU)."""
 
-    def __init__(self, device=0, slots=4, precision=MIXED, hbm_budget=64 << 30, backend=None):
+    def __init__(self, device=0, slots=4, precision=MIXED, hbm_budget=64 << 30, backend=None, batch_mode=2):
         self.slots = slots
         self.budget = hbm_budget
-        self.backend = backend or GpuBackend(device, precision)
+        self.backend = backend or GpuBackend(device, precision, batch_mode)
         self.peak_bytes = 0  # largest footprint in flight during the last run
+        self.budget_waits = 0  # admissions the HBM budget delayed during the last run
 
     def run(self, requests, realtime=True):
         """Serve the requests (sorted by arrival); with realtime=False every
@@ -156,6 +163,8 @@ class Server:
         in request order and the run's wall time."""
         reqs = sorted(requests, key=lambda q: (q.arrival, q.rid))
         self.peak_bytes = 0
+        self.budget_waits = 0
+        waited = set()
         done = {}
         errors = []
         lock = threading.Condition()
@@ -176,6 +185,9 @@ class Server:
                         lock.wait(wait)
                         continue
                     if state["inflight"] > 0 and state["bytes"] + q.bytes > self.budget:
+                        if q.rid not in waited:
+                            waited.add(q.rid)
+                            self.budget_waits += 1
                         lock.wait()
                         continue
                     state["next"] += 1
@@ -237,4 +249,8 @@ def summary(completed, wall):
 
     return {"requests": len(completed), "solves_per_s": len(completed) / wall, "wall_s": wall,
             "latency_p50_s": pct(0.50), "latency_p99_s": pct(0.99), "service_mean_s": statistics.mean(svc),
-            "converged": sum(1 for c in completed if c.converged)}
+            "converged": sum(1 for c in completed if c.converged),
+            "converged_energy": sum(1 for c in completed if c.converged == 1),
+            "converged_norm": sum(1 for c in completed if c.converged == 2),
+            "unconverged": sum(1 for c in completed if not c.converged),
+            "converged_solves_per_s": sum(1 for c in completed if c.converged) / wall}
