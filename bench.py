@@ -830,6 +830,32 @@ def run_reference(args):
     return out
 
 
+def run_window(args):
+    """Profiling window of an SCF workload's headline form: `warm` SCF
+    iterations, then `n` more inside a CUDA profiler range (for
+    ncu --profile-from-start off); prints the library's launches per
+    iteration in the window.  Not a bench line."""
+    import torch
+    import x2dhf_gb300 as xg
+    from x2dhf_gb300 import build
+
+    warm, n = (int(x) for x in args.window.split(","))
+    name, prec, mode = [lg for lg in SCF_LEGS if args.legs == "all" or lg[0] == args.legs][-1]
+    build.build()
+    ctx = xg.Context(0)
+    s = xg.SCF(ctx, xg.parse_deck(WORKLOADS[args.workload](), precision=prec, batch_mode=mode))
+    s.run(warm)
+    ctx.synchronize()
+    l0 = ctx.launches
+    torch.cuda.profiler.start()
+    s.run(n)
+    ctx.synchronize()
+    torch.cuda.profiler.stop()
+    print(json.dumps({"window": f"{args.workload} {name}: iterations {warm + 1}..{warm + n}",
+                      "launches_per_iteration": (ctx.launches - l0) / n}))
+    return None
+
+
 def main():
     faulthandler.enable()  # a fatal signal prints the Python stack to stderr
     ap = argparse.ArgumentParser()
@@ -851,10 +877,14 @@ def main():
                     help="poisson workload: one batch size (default: every size of the configuration)")
     ap.add_argument("--precision", default="", choices=["", "mixed", "fp64"],
                     help="poisson workload: one form (default: both)")
+    ap.add_argument("--window", default="", help="WARM,N: profile SCF iterations WARM+1..WARM+N of the headline form "
+                                                 "inside a CUDA profiler range (no bench line)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.workload == "poisson":
+    if args.window:
+        out = run_window(args)
+    elif args.workload == "poisson":
         out = run_poisson(args)
     elif args.workload == "serve":
         out = run_serve(args) if args.impl != "reference" else {

@@ -1145,41 +1145,58 @@ __device__ __forceinline__ double madd(double a, double b, double c) {  // a*b +
 }
 
 template <bool exact>
+__device__ __forceinline__ void fock_point(const GridDev &g, const FockArgs &a, double ee, int k) {
+  const int mu = k / g.nni, nu = k - mu * g.nni;
+  const int ij = (mu + 4) * g.n8 + nu + 4;
+  double fock1 = g.f0[k];
+  fock1 = madd<exact>(ee, g.f1[k], fock1);
+  if (a.m != 0) fock1 = madd<exact>(double(a.m * a.m), g.e[k], fock1);
+  double fock2 = 0.0;
+  if (!a.nel1) {
+    double wk1 = 0.0;
+    for (int q = 0; q < a.nterms; ++q) {
+      const FockTerm &T = a.t[q];
+      wk1 = madd<exact>(T.coo, T.coul[ij], wk1);
+      if (T.mode == 0) {
+        double wk2 = M(T.gec, T.ex[ij]);
+        if (T.ex2) wk2 = madd<exact>(T.gec2, T.ex2[ij], wk2);
+        fock2 = madd<exact>(wk2, T.psi[ij], fock2);
+      } else if (T.mode == 1) {
+        const double wk2 = M(T.ex[ij], T.psi[ij]);
+        fock2 = madd<exact>(T.gec, wk2, fock2);
+      }
+    }
+    a.coulp[k] = wk1;
+    a.exchp[k] = fock2;
+    fock2 = M(fock2, g.f2[k]);
+    fock1 = madd<exact>(wk1, g.f2[k], fock1);
+  }
+  a.lhs[k] = A(fock1, g.diag);
+  a.rhs[k] = fock2;
+  if (mu >= g.nmu - 5) {
+    const double f1 = g.f1[k];
+    a.fa[(mu - (g.nmu - 5)) * g.nni + nu] = (fabs(f1) <= kPrecis) ? 0.0 : D(fock1, f1);
+  }
+}
+
+template <bool exact>
 __global__ void k_fock(GridDev g, FockArgs a) {
   const double ee = *a.ee;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
-    const int mu = k / g.nni, nu = k - mu * g.nni;
-    const int ij = (mu + 4) * g.n8 + nu + 4;
-    double fock1 = g.f0[k];
-    fock1 = madd<exact>(ee, g.f1[k], fock1);
-    if (a.m != 0) fock1 = madd<exact>(double(a.m * a.m), g.e[k], fock1);
-    double fock2 = 0.0;
-    if (!a.nel1) {
-      double wk1 = 0.0;
-      for (int q = 0; q < a.nterms; ++q) {
-        const FockTerm &T = a.t[q];
-        wk1 = madd<exact>(T.coo, T.coul[ij], wk1);
-        if (T.mode == 0) {
-          double wk2 = M(T.gec, T.ex[ij]);
-          if (T.ex2) wk2 = madd<exact>(T.gec2, T.ex2[ij], wk2);
-          fock2 = madd<exact>(wk2, T.psi[ij], fock2);
-        } else if (T.mode == 1) {
-          const double wk2 = M(T.ex[ij], T.psi[ij]);
-          fock2 = madd<exact>(T.gec, wk2, fock2);
-        }
-      }
-      a.coulp[k] = wk1;
-      a.exchp[k] = fock2;
-      fock2 = M(fock2, g.f2[k]);
-      fock1 = madd<exact>(wk1, g.f2[k], fock1);
-    }
-    a.lhs[k] = A(fock1, g.diag);
-    a.rhs[k] = fock2;
-    if (mu >= g.nmu - 5) {
-      const double f1 = g.f1[k];
-      a.fa[(mu - (g.nmu - 5)) * g.nni + nu] = (fabs(f1) <= kPrecis) ? 0.0 : D(fock1, f1);
-    }
-  }
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x)
+    fock_point<exact>(g, a, ee, k);
+}
+
+// the Fock builds of several orbitals from the same state, orbital blockIdx.y
+constexpr int kFockBatch = 8;
+struct FockBatch {
+  FockArgs a[kFockBatch];
+};
+template <bool exact>
+__global__ void k_fock_batch(GridDev g, const __grid_constant__ FockBatch B) {
+  const FockArgs &a = B.a[blockIdx.y];
+  const double ee = *a.ee;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x)
+    fock_point<exact>(g, a, ee, k);
 }
 
 // orbAsymptGet (relaxOrbs.F90:415-437): edecay for mu = nmu-4..nmu-1 (0-based)
@@ -1205,6 +1222,26 @@ __global__ void k_asympt_set(GridDev g, double *psi, const double *edecay) {
       psi[ij] = M(psi[ij - g.n8], edecay[jj * g.nni + i]);
     }
   }
+}
+
+// orbAsymptGet / orbAsymptSet of several orbitals, orbital blockIdx.y
+__global__ void k_asympt_get_batch(GridDev g, const __grid_constant__ OrbDecayList L) {
+  const int n = 4 * g.nni, o = blockIdx.y;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int jj = k / g.nni, i = k - jj * g.nni;
+    const double dr = g.asy[size_t(50) * n + k];
+    const double fj = L.fa[o][(jj + 1) * g.nni + i], fjm = L.fa[o][jj * g.nni + i];
+    L.edecay[o][k] = sqrt(sqrt(fabs(fj / fjm))) * exp(sqrt(fabs(fjm)) * dr);
+  }
+}
+__global__ void k_asympt_set_batch(GridDev g, const __grid_constant__ OrbDecayList L) {
+  const int o = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < g.nni; i += gridDim.x * blockDim.x)
+    for (int jj = 0; jj < 4; ++jj) {
+      const int j = g.nmu - 4 + jj;
+      const int ij = (j + 4) * g.n8 + i + 4;
+      L.psi[o][ij] = M(L.psi[o][ij - g.n8], L.edecay[o][jj * g.nni + i]);
+    }
 }
 
 // setCiOrb (scfUtils.F90:380-434)
@@ -1508,10 +1545,11 @@ __global__ void k_overlaps(GridDev g, const double *psi, PtrList o, int n, doubl
 // and lagrangeMultipliers.F90:67-72.  psi's ghost cells are read as the
 // mirrored interior values (identical to a putin ghost refresh); exact keeps
 // the reference's unfused order, otherwise products are fused (mixed form).
+// EaHF of one orbital (lagrangeMultipliers.F90:21-107 with the kinetic
+// term of integrals.F90:406-480): the per-thread partial sums of one block
 template <bool exact>
-__global__ void k_eahf(GridDev g, const double *psi, int isym, int m, const double *coulp, const double *exchp,
-                       double *partials, double *sums, double *ee_out, double *parts, unsigned *ticket) {
-  double v[5] = {0, 0, 0, 0, 0};
+__device__ __forceinline__ void eahf_partials(const GridDev &g, const double *psi, int isym, int m,
+                                              const double *coulp, const double *exchp, double (&v)[5]) {
   const int n8 = g.n8;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
     const int mu = k / g.nni, nu = k - mu * g.nni;
@@ -1551,18 +1589,43 @@ __global__ void k_eahf(GridDev g, const double *psi, int isym, int m, const doub
     }
   }
   if (!exact) v[0] = v[1] + v[2];  // oneel = kinetic + nuclear, summed per block
-  if (block_sum_finish<5>(v, partials, sums, 5, ticket) && threadIdx.x == 0) {
-    // EaHF and its parts (lagrangeMultipliers.F90:67-72)
-    const double woneel = sums[0], wc = sums[3], wx = -sums[4];
-    *ee_out = woneel + (wc + wx);
-    if (parts) {
-      parts[0] = sums[1];
-      parts[1] = sums[2];
-      parts[2] = woneel;
-      parts[3] = wc;
-      parts[4] = wx;
-    }
+}
+
+// EaHF and its parts from the summed quadratures (lagrangeMultipliers.F90:67-72)
+__device__ __forceinline__ void eahf_store(const double *sums, double *ee_out, double *parts) {
+  const double woneel = sums[0], wc = sums[3], wx = -sums[4];
+  *ee_out = woneel + (wc + wx);
+  if (parts) {
+    parts[0] = sums[1];
+    parts[1] = sums[2];
+    parts[2] = woneel;
+    parts[3] = wc;
+    parts[4] = wx;
   }
+}
+
+template <bool exact>
+__global__ void k_eahf(GridDev g, const double *psi, int isym, int m, const double *coulp, const double *exchp,
+                       double *partials, double *sums, double *ee_out, double *parts, unsigned *ticket) {
+  double v[5] = {0, 0, 0, 0, 0};
+  eahf_partials<exact>(g, psi, isym, m, coulp, exchp, v);
+  if (block_sum_finish<5>(v, partials, sums, 5, ticket) && threadIdx.x == 0) eahf_store(sums, ee_out, parts);
+}
+
+// EaHF of several orbitals in one launch: orbital blockIdx.y with its own
+// partials, sums and ticket, reduced in the same block order as k_eahf
+constexpr int kEahfItems = 36;
+struct EahfList {
+  EahfItem it[kEahfItems];
+};
+template <bool exact>
+__global__ void k_eahf_batch(GridDev g, const __grid_constant__ EahfList L, double *partials, unsigned *tickets) {
+  const EahfItem &I = L.it[blockIdx.y];
+  double v[5] = {0, 0, 0, 0, 0};
+  eahf_partials<exact>(g, I.psi, I.isym, I.m, I.coulp, I.exchp, v);
+  double *part = partials + size_t(blockIdx.y) * (gridDim.x * 5 + 5);
+  if (block_sum_finish<5>(v, part, part + size_t(gridDim.x) * 5, 5, tickets + blockIdx.y) && threadIdx.x == 0)
+    eahf_store(part + size_t(gridDim.x) * 5, I.ee_out, I.parts);
 }
 
 struct TripleList {
@@ -2098,6 +2161,32 @@ void launch_fock(x2g_ctx *ctx, const GridDev &g, const FockArgs &a) {
   ctx->launches++;
 }
 
+void launch_fock_batch(x2g_ctx *ctx, const GridDev &g, const FockArgs *a, int n) {
+  for (int b = 0; b < n; b += kFockBatch) {
+    const int m = (n - b < kFockBatch) ? n - b : kFockBatch;
+    FockBatch B{};
+    for (int q = 0; q < m; ++q) B.a[q] = a[b + q];
+    const dim3 gg(grid_blocks(g.mxsize), m);
+    if (a[0].exact)
+      k_fock_batch<true><<<gg, kThreads, 0, ctx->stream>>>(g, B);
+    else
+      k_fock_batch<false><<<gg, kThreads, 0, ctx->stream>>>(g, B);
+    ctx->launches++;
+  }
+}
+
+void launch_asympt_get_batch(x2g_ctx *ctx, const GridDev &g, const OrbDecayList &L, int n) {
+  if (n <= 0) return;
+  k_asympt_get_batch<<<dim3(grid_blocks(4 * g.nni), n), kThreads, 0, ctx->stream>>>(g, L);
+  ctx->launches++;
+}
+
+void launch_asympt_set_batch(x2g_ctx *ctx, const GridDev &g, const OrbDecayList &L, int n) {
+  if (n <= 0) return;
+  k_asympt_set_batch<<<dim3(grid_blocks(g.nni), n), kThreads, 0, ctx->stream>>>(g, L);
+  ctx->launches++;
+}
+
 void launch_asympt_get(x2g_ctx *ctx, const GridDev &g, const double *fa, double *edecay) {
   k_asympt_get<<<grid_blocks(4 * g.nni), kThreads, 0, ctx->stream>>>(g, fa, edecay);
   ctx->launches++;
@@ -2195,6 +2284,21 @@ void launch_eahf(x2g_ctx *ctx, const GridDev &g, const double *psi, int isym, in
     k_eahf<false><<<nb, kThreads, 0, ctx->stream>>>(g, psi, isym, m, coulp, exchp, part, sums, ee_out, parts,
                                                     ctx->bar + 3);
   ctx->launches += 1;
+}
+
+void launch_eahf_batch(x2g_ctx *ctx, const GridDev &g, const EahfItem *items, int n, bool exact) {
+  const int nb = red_blocks(g);
+  for (int b = 0; b < n; b += kEahfItems) {
+    const int m = (n - b < kEahfItems) ? n - b : kEahfItems;
+    EahfList L{};
+    for (int q = 0; q < m; ++q) L.it[q] = items[b + q];
+    double *part = reduction_partials(ctx, 5 * kEahfItems + 5 * kEahfItems / 4);
+    if (exact)
+      k_eahf_batch<true><<<dim3(nb, m), kThreads, 0, ctx->stream>>>(g, L, part, ctx->bar + kMomentTickets);
+    else
+      k_eahf_batch<false><<<dim3(nb, m), kThreads, 0, ctx->stream>>>(g, L, part, ctx->bar + kMomentTickets);
+    ctx->launches += 1;
+  }
 }
 
 void launch_triples(x2g_ctx *ctx, const GridDev &g, const TripleItem *items, int n, double *out) {

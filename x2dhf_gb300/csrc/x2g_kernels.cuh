@@ -63,6 +63,16 @@ void launch_ghost_fill(x2g_ctx *ctx, const GridDev &g, double *u, int isym);    
 void launch_putin(x2g_ctx *ctx, const GridDev &g, int isym, const double *plain, double *ext);
 void launch_putout(x2g_ctx *ctx, const GridDev &g, const double *ext, double *plain);
 void launch_fock(x2g_ctx *ctx, const GridDev &g, const FockArgs &a);
+// Fock builds of n orbitals from the same state (a[0].exact for all)
+void launch_fock_batch(x2g_ctx *ctx, const GridDev &g, const FockArgs *a, int n);
+// per-orbital asymptotic decay of several orbitals (fa, edecay, psi by orbital)
+struct OrbDecayList {
+  const double *fa[kMaxTerms];
+  double *edecay[kMaxTerms];
+  double *psi[kMaxTerms];
+};
+void launch_asympt_get_batch(x2g_ctx *ctx, const GridDev &g, const OrbDecayList &L, int n);
+void launch_asympt_set_batch(x2g_ctx *ctx, const GridDev &g, const OrbDecayList &L, int n);
 void launch_asympt_get(x2g_ctx *ctx, const GridDev &g, const double *fa, double *edecay);
 void launch_asympt_set(x2g_ctx *ctx, const GridDev &g, double *psi, const double *edecay);
 void launch_setci(x2g_ctx *ctx, const GridDev &g, double *psi, int ihomo);
@@ -90,6 +100,13 @@ void launch_overlaps(x2g_ctx *ctx, const GridDev &g, const double *psi, const do
 // needed); exact: the reference's unfused FP64 order, else FMAs (mixed form)
 void launch_eahf(x2g_ctx *ctx, const GridDev &g, const double *psi, int isym, int m, const double *coulp,
                  const double *exchp, double *ee_out, double *parts, bool exact = true);
+// EaHF of several orbitals in one launch (same sums, same order as launch_eahf)
+struct EahfItem {
+  const double *psi, *coulp, *exchp;
+  double *ee_out, *parts;
+  int isym, m;
+};
+void launch_eahf_batch(x2g_ctx *ctx, const GridDev &g, const EahfItem *items, int n, bool exact);
 // generic weighted triple products: out[k] = sum w * a_k * b_k * c_k (c may be null), w = wgt2
 struct TripleItem {
   const double *a, *b, *c;  // a,b ext arrays; c ext or null

@@ -342,8 +342,7 @@ void exchange_weights(x2g_scf *s) {
 // ---------------------------------------------------------------------
 // fockHF of orbital iorb into lhs (fock1 + diag), rhs (fock2) and fa
 // (fock1/f1 on the last 5 mu rows)
-int fock_into(x2g_scf *s, int iorb, double *lhs, double *rhs, double *fa) {
-  const GridDev &g = s->grid->d;
+FockArgs fock_args(x2g_scf *s, int iorb, double *lhs, double *rhs, double *fa) {
   FockArgs a{};
   a.m = s->m[iorb];
   a.nel1 = (s->nel == 1);
@@ -378,11 +377,13 @@ int fock_into(x2g_scf *s, int iorb, double *lhs, double *rhs, double *fa) {
     }
   }
   a.nterms = n;
-  launch_fock(s->ctx, g, a);
-  return X2G_OK;
+  return a;
 }
 
-int fock(x2g_scf *s, int iorb) { return fock_into(s, iorb, s->lhs, s->rhs, s->fa); }
+int fock(x2g_scf *s, int iorb) {
+  launch_fock(s->ctx, s->grid->d, fock_args(s, iorb, s->lhs, s->rhs, s->fa));
+  return X2G_OK;
+}
 
 // relaxation form of a kind of function: list-order SOR (always FP64) or
 // MCSOR in the case's precision (relaxDriver, doSCF.F90:960-1004)
@@ -445,10 +446,14 @@ int relax_orbital(x2g_scf *s, int iorb) {
 int relax_all_orbitals(x2g_scf *s) {
   const GridDev &g = s->grid->d;
   std::vector<x2g_job> jobs;
+  std::vector<FockArgs> fa;
+  OrbDecayList dl{};
   for (int i = 1; i <= s->norb; i++) {
     const int iorb = s->norb - i + 1;
-    fock_into(s, iorb, s->blhs[iorb], s->brhs[iorb], s->bfa[iorb]);
-    launch_asympt_get(s->ctx, g, s->bfa[iorb], s->bedecay[iorb]);
+    fa.push_back(fock_args(s, iorb, s->blhs[iorb], s->brhs[iorb], s->bfa[iorb]));
+    dl.fa[i - 1] = s->bfa[iorb];
+    dl.edecay[i - 1] = s->bedecay[iorb];
+    dl.psi[i - 1] = s->orb[iorb];
     x2g_job j{};
     j.u = s->orb[iorb];
     j.lhs = s->blhs[iorb];
@@ -458,10 +463,12 @@ int relax_all_orbitals(x2g_scf *s) {
     j.kind = 0;
     jobs.push_back(j);
   }
+  launch_fock_batch(s->ctx, g, fa.data(), int(fa.size()));
+  launch_asympt_get_batch(s->ctx, g, dl, s->norb);
   s->nsor4orb += long(jobs.size()) * s->cs.maxsor_orb;
   int rc = launch_relax(s->ctx, s->grid, jobs.data(), int(jobs.size()), s->cs.maxsor_orb, orb_form(s));
   if (rc) return rc;
-  for (int iorb = 1; iorb <= s->norb; iorb++) launch_asympt_set(s->ctx, g, s->orb[iorb], s->bedecay[iorb]);
+  launch_asympt_set_batch(s->ctx, g, dl, s->norb);
   return X2G_OK;
 }
 
@@ -500,6 +507,24 @@ void eahf(x2g_scf *s, int iorb, double *ee_out, double *parts) {
               parts, s->cs.precision == X2G_FP64);
 }
 
+// EaHF of the listed orbitals in one launch: the same sums in the same
+// order as one launch per orbital.  parts: 5 values per orbital (index
+// iorb) or null.
+void eahf_batch(x2g_scf *s, const std::vector<int> &orbs, double *ee_base, double *parts) {
+  std::vector<EahfItem> items;
+  for (int iorb : orbs)
+    items.push_back(EahfItem{s->orb[iorb], s->coulp[iorb], s->exchp[iorb], ee_base + iorb,
+                             parts ? parts + 5 * iorb : nullptr, s->isymOrb[iorb], s->m[iorb]});
+  if (!items.empty())
+    launch_eahf_batch(s->ctx, s->grid->d, items.data(), int(items.size()), s->cs.precision == X2G_FP64);
+}
+
+std::vector<int> orbitals_descending(const x2g_scf *s) {
+  std::vector<int> v;
+  for (int i = s->norb; i >= 1; i--) v.push_back(i);
+  return v;
+}
+
 void mpole_moments(x2g_scf *s) {
   if (s->nel == 1) return;
   const GridDev &g = s->grid->d;
@@ -514,6 +539,42 @@ void mpole_moments(x2g_scf *s) {
     items.push_back(MomentItem{s->orb[s->mm_i1[q]], s->orb[s->mm_i2[q]], s->sc + x2g_scf::O_EX + 8 * s->mm_ipc[q],
                                s->mm_idel[q], 0});
   if (!items.empty()) launch_moments(s->ctx, g, items.data(), int(items.size()), homo);
+}
+
+// the boundary rows of orbital iorb1's potentials (potAsympt) as items
+void pot_asympt_items(x2g_scf *s, int iorb1, std::vector<AsymptItem> &items) {
+  if (s->itouch[iorb1] == 1) items.push_back(AsymptItem{s->coul[iorb1], 0, iorb1 - 1, 0, 0});
+  for (int iorb2 = 1; iorb2 <= s->norb; iorb2++) {
+    if (!s->itouch[iorb1] && !s->itouch[iorb2]) continue;
+    int k = s->k2[iorb1][iorb2];
+    if (k == 0 || s->ilc[k] == 0) continue;
+    int idel = std::abs(s->m[iorb1] - s->m[iorb2]);
+    if (iorb1 == iorb2) idel = 2 * s->m[iorb1];
+    items.push_back(AsymptItem{s->exch[2 * k], 1, k, idel, 0});
+    if (s->ilc[k] == 2)
+      items.push_back(AsymptItem{s->exch[2 * k + 1], 1, k + s->norb * (s->norb + 1) / 2, s->m[iorb2] + s->m[iorb1], 0});
+  }
+}
+
+// potAsympt items in launches of kMaxAsympt; an item repeated for the same
+// potential (the same values) is written once
+void launch_asympt_items(x2g_scf *s, const std::vector<AsymptItem> &all) {
+  std::vector<AsymptItem> items;
+  for (const AsymptItem &it : all) {
+    bool dup = false;
+    for (const AsymptItem &x : items) dup = dup || (x.pot == it.pot);
+    if (!dup) items.push_back(it);
+  }
+  for (size_t b = 0; b < items.size(); b += kMaxAsympt) {
+    AsymptArgs a{};
+    a.norb = s->norb;
+    a.cmulti = s->sc + x2g_scf::O_CM;
+    a.excm = s->sc + x2g_scf::O_EX;
+    a.nslots = s->nslots;
+    a.n = int(std::min(items.size() - b, size_t(kMaxAsympt)));
+    for (int q = 0; q < a.n; q++) a.it[q] = items[b + q];
+    launch_asympt(s->ctx, s->grid->d, a);
+  }
 }
 
 void pot_asympt(x2g_scf *s, int iorb1) {
@@ -544,8 +605,8 @@ int etotal(x2g_scf *s) {
   const GridDev &g = s->grid->d;
   const int norb = s->norb;
   double *parts = s->sc + x2g_scf::O_OVL + 64 * 40;  // scratch region after the overlaps
-  double *eedummy = parts + 5 * (MAXO + 1);
-  for (int i = 1; i <= norb; i++) eahf(s, i, eedummy, parts + 5 * i);
+  double *eedummy = parts + 5 * (MAXO + 1);           // MAXO + 1 discarded orbital energies
+  eahf_batch(s, orbitals_descending(s), eedummy, parts);
   std::vector<TripleItem> items;
   std::vector<int> kind;  // 0 coulij(i,i) 1 coulij(i2,i1) 2 exch self 3 exch type0 4 exch type1
   std::vector<std::pair<int, int>> who;
@@ -673,7 +734,7 @@ int prep_scf(x2g_scf *s) {
   }
   for (int i = 1; i <= s->norb; i++) s->itouch[i] = 1;
   mpole_moments(s);
-  for (int i = s->norb; i >= 1; i--) eahf(s, i, s->sc + x2g_scf::O_EE + i, nullptr);
+  eahf_batch(s, orbitals_descending(s), s->sc + x2g_scf::O_EE, nullptr);
   int rc = read_scalars(s);
   if (rc) return rc;
   for (int i = 1; i <= s->norb; i++) s->eeOld[i] = s->ee[i];
@@ -687,18 +748,22 @@ int scf_iteration(x2g_scf *s, int *rc) {
   int iasympt = norb;
   *rc = X2G_OK;
   const bool batched = (s->cs.batch_mode >= 1);
+  bool frozen = false;
+  for (int i = 1; i <= norb; i++) frozen = frozen || (s->ifixorb[i] != 0);
   if (batched) {
     // the boundary values of every potential first (they depend only on the
     // multipole moments, which change only between iterations), then all
     // potentials of the iteration in one relaxation launch
+    for (int i = 1; i <= norb; i++) s->itouch[norb - i + 1] = 1;
+    std::vector<AsymptItem> items;
     for (int i = 1; i <= norb; i++) {
       const int iorb = norb - i + 1;
-      s->itouch[iorb] = 1;
       if (iasympt != 0 && s->ifixorb[iorb] == 0) {
-        pot_asympt(s, iorb);
+        pot_asympt_items(s, iorb, items);
         iasympt--;
       }
     }
+    launch_asympt_items(s, items);
     if ((*rc = relax_all_potentials(s))) return 1;
     if (s->cs.batch_mode == 2 && !s->lfixorb)
       if ((*rc = relax_all_orbitals(s))) return 1;
@@ -727,8 +792,12 @@ int scf_iteration(x2g_scf *s, int *rc) {
     }
     if (norb > 1 && s->ifixorb[iorb] == 0) ortho(s, iorb);
     if (s->ifixorb[iorb] != 0) fock(s, iorb);
-    eahf(s, iorb, s->sc + x2g_scf::O_EE + iorb, nullptr);
+    // EaHF of iorb reads only iorb and its own Fock sums, which nothing
+    // later in the iteration changes: deferred and batched unless an
+    // orbital is frozen (its Fock build above reads the current potentials)
+    if (frozen) eahf(s, iorb, s->sc + x2g_scf::O_EE + iorb, nullptr);
   }
+  if (!frozen) eahf_batch(s, orbitals_descending(s), s->sc + x2g_scf::O_EE, nullptr);
   if ((*rc = read_scalars(s))) return 1;
   for (int i = 1; i <= norb; i++) {
     const int iorb = norb - i + 1;
@@ -845,7 +914,7 @@ int scf_finish(x2g_scf *s) {
       ortho(s, j);
     }
   }
-  for (int i = s->norb; i >= 1; i--) eahf(s, i, s->sc + x2g_scf::O_EE + i, nullptr);
+  eahf_batch(s, orbitals_descending(s), s->sc + x2g_scf::O_EE, nullptr);
   mpole_moments(s);
   int rc = read_scalars(s);
   if (rc) return rc;
