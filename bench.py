@@ -265,7 +265,7 @@ def max_over_ranks(values, world, device):
 ORACLE_SOLVES = {"n2": os.path.join(ROOT, "tests", "golden", "n2_331x481_oracle.json")}
 # SCF forms timed by the GPU arm: (name, precision, batch mode); the last is
 # the headline `value` (the benchmark spec's batched mixed form)
-SCF_LEGS = (("fp64", 0, 0), ("mixed_reference_order", 1, 0), ("mixed", 1, 2))
+SCF_LEGS = (("fp64", 0, 0), ("fp64_batched", 0, 2), ("mixed_reference_order", 1, 0), ("mixed", 1, 2))
 
 
 def oracle_reference(name):
@@ -293,6 +293,7 @@ def run_gpu(args):
     build.build()
     torch.cuda.set_device(local)
     ctx = xg.Context(local)
+    _configure(ctx, args)
     stream = torch.cuda.ExternalStream(xg.lib().x2g_stream(ctx.h))
     deck = WORKLOADS[args.workload]()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
@@ -306,7 +307,7 @@ def run_gpu(args):
 
     copied = [0, 0, 0]  # host-to-device bytes, device-to-host bytes, timed e2e steps
 
-    def timed_solves(prec, mode, k, warm, e2e=False, cap=None):
+    def timed_solves(prec, mode, k, warm, e2e=False, cap=None, warm_cap=None):
         lat, res_last, iters = [], None, []
         for step in range(warm + k):
             if not e2e:
@@ -321,7 +322,8 @@ def run_gpu(args):
             if e2e:
                 case = xg.parse_deck(deck, precision=prec, batch_mode=mode)
                 scf = xg.SCF(ctx, case)
-            res = scf.run(cap if cap else (fixed if step >= warm else WARMUP_ITERS.get(args.workload, fixed)))
+            res = scf.run(cap if cap else (fixed if step >= warm else
+                                           warm_cap or WARMUP_ITERS.get(args.workload, fixed)))
             if e2e:
                 for i in range(1, case.norb + 1):
                     scf.orbital(i)
@@ -350,9 +352,12 @@ def run_gpu(args):
     with sampler:
         for name, prec, mode in legs:
             # the plain FP64 form is the slow comparator: a few timed solves
-            k = args.steps if name != "fp64" or len(legs) == 1 else min(args.steps, args.fp64_steps)
+            k = args.steps if not name.startswith("fp64") or len(legs) == 1 else min(args.steps, args.fp64_steps)
             l0 = ctx.launches
-            lat[name], res[name], its[name] = timed_solves(prec, mode, k, args.warmup)
+            # the comparator's warm-up solves stop after 50 iterations (a full
+            # plain-FP64 solve takes seconds and warms nothing more)
+            lat[name], res[name], its[name] = timed_solves(prec, mode, k, args.warmup,
+                                                           warm_cap=50 if name.startswith("fp64") else None)
             if name == head[0]:
                 # launches of the timed headline solves (the warm-up ones counted out)
                 launches = int((ctx.launches - l0) * k / (k + args.warmup))
@@ -384,6 +389,11 @@ def run_gpu(args):
     value = rate[head[0]]
     e2e_value = world * len(late2e) * per_step / tote2e
     on_chip = xg.host_cluster_plan(c.nnu, c.nmu)[0] > 0
+    occ = (0, 0)
+    if on_chip:
+        g = xg.Grid(ctx, c.nnu, c.nmu, c.r, c.rinf, c.z1, c.z2)
+        occ = g.cluster_occupancy()
+        g.close()
     hs = sorted(lat[head[0]])
     p99 = hs[min(len(hs) - 1, int(round(0.99 * (len(hs) - 1))))]
     # bytes the library copied per timed e2e step (grid tables up; per-iteration
@@ -392,6 +402,7 @@ def run_gpu(args):
     d2h = copied[1] // max(1, copied[2])
     msmx, ptsmx, nmx = prof.get(head[0], (0.0, 0.0, 0)) if head[1] == 1 else (0.0, 0.0, 0)
     ms64, pts64, n64 = prof.get("fp64", (0.0, 0.0, 0))
+    msb64, ptsb64, nb64 = prof.get("fp64_batched", (0.0, 0.0, 0))
     sweep_gbs_mx = ptsmx * BYTES_PER_PT[1] / (msmx / 1e3) / 1e9 if msmx > 0 else None
     sweep_gbs_64 = pts64 * BYTES_PER_PT[0] / (ms64 / 1e3) / 1e9 if ms64 > 0 else None
     pts_per_launch = ptsmx / nmx if nmx else None
@@ -410,6 +421,8 @@ def run_gpu(args):
             d["dE_vs_fp64"] = abs(r.total_energy - fp64_e)
             d["max_dee_vs_fp64"] = max(abs(r.ee[i] - res["fp64"].ee[i]) for i in range(c.norb))
             d["speedup_vs_fp64"] = rate[n] / rate["fp64"]
+        if "fp64_batched" in res and n.startswith("mixed"):
+            d["speedup_vs_fp64_batched"] = rate[n] / rate["fp64_batched"]
         if oref and args.workload not in FIXED_ITERS:
             d["dE_vs_fp64_oracle"] = abs(r.total_energy - oref["total_energy"])
             d["max_dee_vs_fp64_oracle"] = max(abs(r.ee[i] - oref["orbital_energies"][i]) for i in range(c.norb))
@@ -432,7 +445,9 @@ def run_gpu(args):
         "form": {"value": f"{head[0]}: FP32 MCSOR sweeps + FP64 defect correction, "
                           + ("every potential of an SCF iteration in one launch, then every orbital in one "
                              "launch (batch mode 2)" if head[2] == 2 else "the reference's relaxation order"),
-                 "fp64": "plain form: FP64 MCSOR in the reference's colour order and relaxation order"},
+                 "fp64": "plain form: FP64 MCSOR in the reference's colour order and relaxation order",
+                 "fp64_batched": "plain form, FP64 MCSOR in the reference's colour order, batched like the "
+                                 "headline (batch mode 2): the comparator with the same launch shape"},
         "latency_s": {"p50": statistics.median(lat[head[0]]), "p99": p99},
         "e2e": {"value": e2e_value, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
@@ -455,11 +470,17 @@ def run_gpu(args):
                      "launch is bound by phase latency (neighbour wait, halo round trip, level chain), not by HBM"),
             "sweep_ms_total": msmx, "sweep_launches": nmx, "point_updates": ptsmx,
             "point_updates_per_launch": pts_per_launch,
+            "clusters_co_resident": {"plain": occ[0], "potentials_variant": occ[1],
+                                     "potentials_variant_mode": args.potential_clusters},
             "fp64_kernel": {"kernel": "k_mcsor_f64", "achieved_gbs": sweep_gbs_64,
                             "frac_hbm": (sweep_gbs_64 / hbm) if sweep_gbs_64 else None,
                             "achieved_tflops": pts64 * FLOPS_PER_PT / (ms64 / 1e3) / 1e12 if ms64 > 0 else None,
                             "bound": "fp64 ALU (1.19 TFLOP/s measured on this GB300)",
-                            "sweep_ms_total": ms64, "sweep_launches": n64},
+                            "sweep_ms_total": ms64, "sweep_launches": n64,
+                            "batched": {"achieved_tflops": (ptsb64 * FLOPS_PER_PT / (msb64 / 1e3) / 1e12
+                                                            if msb64 > 0 else None),
+                                        "sweep_ms_total": msb64, "sweep_launches": nb64,
+                                        "point_updates_per_launch": ptsb64 / nb64 if nb64 else None}},
         },
         "clocks": sampler.summary(),
     }
@@ -495,6 +516,7 @@ def run_poisson(args):
 
     build.build()
     ctx = xg.Context(0)
+    _configure(ctx, args)
     nnu, nmu, r, rinf = 331, 481, 2.0, 40.0
     grid = xg.Grid(ctx, nnu, nmu, r, rinf, 1.0, 1.0)
     dev = torch.device("cuda:0")
@@ -606,6 +628,11 @@ def run_serve(args):
             out[name] = dict(serve.summary(done, wall), peak_footprint_bytes=srv.peak_bytes, hbm_budget_bytes=budget,
                              budget_waits=srv.budget_waits)
             out[name + "_energies"] = [c.total_energy for c in done]
+            if name == "mixed":
+                # every request: template, grid, bond length, SCF iterations, exit (0: the iteration cap
+                # or stagnation, 1: energy threshold, 2: norm threshold)
+                out[name]["per_request"] = [[q.template, q.nnu, q.nmu, round(q.r, 4), c.iterations, c.converged]
+                                            for q, c in zip(reqs, done)]
     de = max(abs(a - b) for a, b in zip(out["mixed_energies"], out["fp64_energies"]))
     same = out["mixed_energies"] == out["mixed_tight_budget_energies"]
     mx, f64 = out["mixed"], out["fp64"]
@@ -843,6 +870,7 @@ def run_window(args):
     name, prec, mode = [lg for lg in SCF_LEGS if args.legs == "all" or lg[0] == args.legs][-1]
     build.build()
     ctx = xg.Context(0)
+    _configure(ctx, args)
     s = xg.SCF(ctx, xg.parse_deck(WORKLOADS[args.workload](), precision=prec, batch_mode=mode))
     s.run(warm)
     ctx.synchronize()
@@ -854,6 +882,12 @@ def run_window(args):
     print(json.dumps({"window": f"{args.workload} {name}: iterations {warm + 1}..{warm + n}",
                       "launches_per_iteration": (ctx.launches - l0) / n}))
     return None
+
+
+def _configure(ctx, args):
+    """Context options the command line sets."""
+    mode = getattr(args, "potential_clusters", "auto")
+    ctx.set_potential_clusters("auto" if mode == "auto" else mode == "on")
 
 
 def main():
@@ -871,12 +905,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--legs", default="all", choices=["all"] + [lg[0] for lg in SCF_LEGS],
                     help="SCF workloads: time every form (default) or one (for profiling runs)")
-    ap.add_argument("--fp64-steps", type=int, default=3,
+    ap.add_argument("--fp64-steps", type=int, default=2,
                     help="SCF workloads: timed solves of the slow plain FP64 comparator")
     ap.add_argument("--batch", type=int, default=0,
                     help="poisson workload: one batch size (default: every size of the configuration)")
     ap.add_argument("--precision", default="", choices=["", "mixed", "fp64"],
                     help="poisson workload: one form (default: both)")
+    ap.add_argument("--potential-clusters", default="auto", choices=["auto", "on", "off"],
+                    help="mixed form: cluster sweep of potential batches at two CTAs per SM "
+                         "(default: for batches above the plain kernel's co-resident clusters)")
     ap.add_argument("--window", default="", help="WARM,N: profile SCF iterations WARM+1..WARM+N of the headline form "
                                                  "inside a CUDA profiler range (no bench line)")
     args = ap.parse_args()

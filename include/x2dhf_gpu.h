@@ -154,6 +154,17 @@ int x2g_host_sor_schedule(int nnu, int nmu, int *npoints, int *nlev, int *nblev,
  * fit its co-resident clusters and the persistent-band kernel for larger
  * batches that it holds in one launch. */
 int x2g_set_mixed_on_chip(x2g_ctx *ctx, int on);
+/* Mixed form, cluster kernel, batches of potentials built from orbitals
+ * (lhs = f3 + idel^2 e, separable in mu and nu): a variant that keeps only
+ * the residual on chip and forms omega / lhs from a row and a column term,
+ * so that two CTAs fit each SM and twice the clusters are co-resident.
+ * mode 0 never, 1 always, 2 (default) for batches larger than the clusters
+ * of the plain kernel co-resident on the device.  No reference counterpart. */
+int x2g_set_potential_clusters(x2g_ctx *ctx, int mode);
+/* Co-resident clusters of the mixed form's cluster sweep (plain) and of its
+ * potentials' variant (pot) for this grid on the context's device; 0 where
+ * that kernel cannot run the grid.  No reference counterpart. */
+int x2g_cluster_occupancy(x2g_ctx *ctx, x2g_grid *grid, int *plain, int *pot);
 /* Self-check of the mixed form's integer-pipe FP64<->FP32 conversions
  * against the hardware conversions on n values (edge cases, then hashed bit
  * patterns from seed); mismatches outside the documented flush-to-zero

@@ -151,6 +151,61 @@ def test_mixed_on_chip_matches_persistent_band_path(ctx, name):
     assert np.abs(out[0] - out[1]).max() <= 1e-5 * change
 
 
+@pytest.mark.parametrize("name", ["ne_set01", "h2_set01"])
+def test_potential_cluster_variant_tracks_fp64(ctx, name):
+    """Every potential of the case in one mixed-form launch, through the
+    cluster kernel and through its potentials' variant (two CTAs per SM,
+    residual only on chip, omega/lhs from the row term f3 + idel^2 e_mu and
+    the column term idel^2 e_nu): both stay within FP32 rounding of the FP64
+    sweep's change, Coulomb (idel 0) and exchange (idel > 0) potentials
+    alike.  The start is one FP64 sweep from the deck's initial potentials,
+    so that the axis values are the extrapolation of the interior, as after
+    any relaxation: the mixed form extrapolates the correction on the axis,
+    which equals extrapolating u only for such a start."""
+    torch = pytest.importorskip("torch")
+    deck = golden_deck(name)
+    oc = Case(deck)
+    c, g = _grid(ctx, deck)
+    dev = torch.device("cuda:0")
+    orbs = {i: torch.tensor(oc.putin(1 if c.m[i - 1] % 2 == 0 else -1, oc.orbital(i)), device=dev)
+            for i in range(1, oc.norb + 1)}
+    omega = oc.omega()[1]
+    specs = []
+    for iorb in range(1, oc.norb + 1):
+        for k in range(1, oc.npots(iorb) + 1):
+            in1, in2, idel, isym = oc.pot_info(iorb, k)
+            specs.append((in1, in2, idel, isym, oc.putin(isym, oc.pot(iorb, k))))
+    assert len({s[2] for s in specs}) >= (2 if name == "ne_set01" else 1)
+
+    def run(precision, variant, start=None, nsweeps=10):
+        bufs = [torch.tensor(s[4], device=dev) for s in specs] if start is None else \
+            [torch.tensor(x, device=dev) for x in start]
+        jobs = [xg.Job(u=u.data_ptr(), psa=orbs[a].data_ptr(), psb=orbs[b].data_ptr(), omega=omega, isym=sy,
+                       idel=d, kind=1) for u, (a, b, d, sy, _) in zip(bufs, specs)]
+        ctx.set_potential_clusters(variant)
+        torch.cuda.synchronize()
+        xg.relax(ctx, g, jobs, nsweeps, precision)
+        ctx.synchronize()
+        return [u.cpu().numpy() for u in bufs]
+
+    def grid_part(x):
+        # the nu x mu points the caller reads back (putout): the ghost cells
+        # are refreshed from the interior at the start of an FP64 call, and
+        # only read as mirrored interior values by the mixed form
+        return x.reshape(c.nmu + 8, c.nnu + 8)[4:c.nmu + 4, 4:c.nnu + 4]
+
+    start = run(xg.FP64, False, nsweeps=1)
+    exact = [grid_part(x) for x in run(xg.FP64, False, start)]
+    plain = [grid_part(x) for x in run(xg.MIXED, False, start)]
+    pair = [grid_part(x) for x in run(xg.MIXED, True, start)]
+    ctx.set_potential_clusters("auto")
+    for k, (e, a, b, u0, s) in enumerate(zip(exact, plain, pair, [grid_part(x) for x in start], specs)):
+        change = np.abs(e - u0).max()
+        assert change > 0
+        assert np.abs(a - e).max() <= 1e-5 * change + 1e-14, (k, s[2], np.abs(a - e).max() / change)
+        assert np.abs(b - e).max() <= 1e-5 * change + 1e-14, (k, s[2], np.abs(b - e).max() / change)
+
+
 def _scf_records_match(name, niter, transform=None, tol=1e-11, batch_mode=0):
     deck = golden_deck(name)
     if transform:

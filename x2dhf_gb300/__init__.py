@@ -74,7 +74,8 @@ EXPORTS = [
     "x2g_scf_set_function", "x2g_scf_get_function", "x2g_scf_set_start_values", "x2g_scf_get_start_values",
     "x2g_kernel_launches", "x2g_transfer_bytes", "mcsor_pthread_", "mcsor_tpool_", "coulExch_pthread_", "coulExch_tpool_",
     "tpoolStop4mcsor_", "tpoolStop4pots_", "x2g_host_table", "x2g_host_schedule", "x2g_profile",
-    "x2g_relax_noalloc", "x2g_host_cluster_plan", "x2g_set_mixed_on_chip", "x2g_host_cluster_chunks", "x2g_host_band_schedule",
+    "x2g_relax_noalloc", "x2g_host_cluster_plan", "x2g_set_mixed_on_chip", "x2g_set_potential_clusters", "x2g_cluster_occupancy",
+    "x2g_host_cluster_chunks", "x2g_host_band_schedule",
     "x2g_convert_selftest", "x2g_set_wait_limit", "x2g_host_sor_schedule",
 ]
 
@@ -134,6 +135,8 @@ def lib():
     L.x2g_host_cluster_plan.argtypes = [I, I, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_long),
                                         C.POINTER(C.c_int)]
     L.x2g_set_mixed_on_chip.argtypes = [P, I]
+    L.x2g_set_potential_clusters.argtypes = [P, I]
+    L.x2g_cluster_occupancy.argtypes = [P, P, C.POINTER(I), C.POINTER(I)]
     L.x2g_set_wait_limit.argtypes = [P, D]
     L.x2g_kernel_launches.restype = C.c_long
     L.x2g_kernel_launches.argtypes = [P]
@@ -429,6 +432,13 @@ class Context:
         kernel, "auto" cluster kernel up to its co-resident clusters."""
         _check(self.L.x2g_set_mixed_on_chip(self.h, 2 if on == "auto" else (1 if on else 0)))
 
+    def set_potential_clusters(self, mode):
+        """Cluster sweep of potential batches: True the two-CTAs-per-SM
+        variant (residual only on chip, omega/lhs from row and column terms),
+        False the plain kernel, "auto" the variant for batches above the
+        plain kernel's co-resident clusters."""
+        _check(self.L.x2g_set_potential_clusters(self.h, 2 if mode == "auto" else (1 if mode else 0)))
+
     def convert_selftest(self, n, seed=1):
         """Mismatches of the integer-pipe FP64<->FP32 conversions against the hardware ones."""
         bad = C.c_ulonglong()
@@ -463,6 +473,13 @@ class Grid:
         v = [C.c_int() for _ in range(5)]
         _check(self.L.x2g_grid_info(self.h, *[C.byref(x) for x in v]))
         return dict(zip(("nnu", "nmu", "ntiles", "nlevels", "npoints"), [x.value for x in v]))
+
+    def cluster_occupancy(self):
+        """(plain, potentials' variant) co-resident clusters of the mixed
+        form's cluster sweep for this grid on the context's device."""
+        a, b = C.c_int(), C.c_int()
+        _check(self.L.x2g_cluster_occupancy(self.ctx.h, self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def table(self, which):
         out = np.zeros(self.nnu * self.nmu)

@@ -188,6 +188,12 @@ int x2g_set_mixed_on_chip(x2g_ctx *c, int on) {
   return X2G_OK;
 }
 
+int x2g_set_potential_clusters(x2g_ctx *c, int mode) {
+  if (!c || mode < 0 || mode > 2) return set_status(X2G_ERR_ARG, "mode must be 0, 1 or 2");
+  c->pot_clusters = mode;
+  return X2G_OK;
+}
+
 int x2g_round_grid(int n) {
   // nnucalc/nmucalc (inputInterface.F90:2961-3095): n = 1 (mod 6) and
   // n - 6 = 0 (mod 5) enforced alternately, always rounding down.
@@ -294,6 +300,8 @@ int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, doubl
   UP(h.borb_mu, borb_mu);
   UP(h.bpot_mu, bpot_mu);
   UP(h.f3_mu, f3_mu);
+  UP(h.e_mu, e_mu);
+  UP(h.e_nu, e_nu);
   UP(h.d_nu, d_nu);
   UP(h.e, e);
   UP(h.f0, f0);
@@ -331,6 +339,9 @@ int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, doubl
   d.cl_wa = h.cl_wa;
   d.cl_wb = h.cl_wb;
   d.cl_ws = h.cl_ws;
+  d.cl_pa = h.cl_pa;
+  d.cl_pb = h.cl_pb;
+  d.cl_ps = h.cl_ps;
   if (h.cl_size > 0) {
     UP(h.cl_tile0, cl_tile0);
     UP(h.cl_row0, cl_row0);
@@ -412,6 +423,11 @@ int x2g_grid_info(x2g_grid *gr, int *nnu, int *nmu, int *ntiles, int *nlevels, i
   if (nlevels) *nlevels = gr->h.nlev;
   if (npoints) *npoints = int(gr->h.order.size());
   return X2G_OK;
+}
+
+int x2g_cluster_occupancy(x2g_ctx *ctx, x2g_grid *grid, int *plain, int *pot) {
+  if (!ctx || !grid) return set_status(X2G_ERR_ARG, "null argument");
+  return cluster_occupancy(ctx, grid, plain, pot);
 }
 
 int x2g_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, int nsweeps, int precision) {

@@ -36,6 +36,9 @@ struct HostGrid {
   double dmu1[4], dmu2[4], dni1[4], dni2[4], exeven[5];
   std::vector<double> dmu9, dni9;              // 9-point derivative weights (diffmu/diffnu)
   std::vector<double> borb_mu, bpot_mu, f3_mu;  // mu-only coefficient tables
+  // the two axis terms of e = e_mu(mu) - e_nu(nu) (e_mu = -1/(xi^2-1),
+  // e_nu = 1/(1-eta^2), 0 on the nu axis points, where e is 0)
+  std::vector<double> e_mu, e_nu;
   std::vector<double> d_nu;                     // nu-only
   std::vector<double> e, f0, f1, f2, f4, g, wgt1, wgt2;  // plain 2-D tables
   std::vector<double> leg;                      // mpole tables P_k(cos th) r^k, plain
@@ -50,6 +53,8 @@ struct HostGrid {
   // cluster plan of the on-chip FP32 sweep: cl_size CTAs per job, CTA k
   // owns tiles [cl_tile0[k], cl_tile0[k+1]) = ext rows [cl_row0[k], cl_row0[k+1])
   int cl_size = 0, cl_maxrows = 0, cl_maxchunks = 0, cl_wa = 1, cl_wb = 1, cl_ws = 1;
+  // warps per role of the potentials' variant (two CTAs per SM, 16 warps)
+  int cl_pa = 1, cl_pb = 1, cl_ps = 1;
   size_t cl_smem = 0;
   std::vector<int> cl_tile0, cl_row0;
   // the CTAs' points regrouped [cta][colour][segment] as chunks of up to 4
@@ -96,7 +101,7 @@ struct GridDev {
   const double *dmu9, *dni9;
   const double *vxi, *vxisq, *veta, *vetasq;
   const int *tile_row0, *tile_row1, *pts, *off, *pts_rc;
-  int cl_size, cl_maxrows, cl_maxchunks, cl_wa, cl_wb, cl_ws;
+  int cl_size, cl_maxrows, cl_maxchunks, cl_wa, cl_wb, cl_ws, cl_pa, cl_pb, cl_ps;
   const int *cl_tile0, *cl_row0, *cl_pts, *cl_off;
   const int *st_pts, *st_off;
   int st_rows[17];
@@ -104,6 +109,7 @@ struct GridDev {
   int sor_nlev, sor_nblev, sor_delta;
   // FP32 copies of the coefficient tables for the mixed form
   const float *borb_mu32, *bpot_mu32, *d_nu32;
+  const double *e_mu, *e_nu;
   // separable stencil weights of the mixed form's FP64 residual: for the
   // neighbours at distance 4,3,2,1 before and after the point, cmu_*[mu * 8 +
   // q] = dmu2 + b dmu1 (q < 4, before) and dmu2 - b dmu1 (q >= 4, after) with
@@ -177,10 +183,12 @@ struct x2g_ctx {
   size_t cluster_smem_set = 0;  // dynamic shared memory granted to the cluster kernel
   int no_cluster = 0;           // 1: mixed form uses the persistent-band FP32 kernel
   int auto_band = 0;            // 1: batches beyond the co-resident clusters take the persistent-band kernel
-  int cluster_active = 0;       // clusters of the cluster kernel co-resident on the device (last shape checked)
-  int cluster_nonportable = 0;  // cluster kernel allowed more than 8 CTAs
-  long cluster_checked_key = -1;  // (shared bytes, cluster size) last checked
-  int cluster_ok = 0;             // that cluster shape is schedulable here
+  int pot_clusters = 2;         // potentials' cluster variant: 0 never, 1 always, 2 batches above cluster_active[0]
+  // [0] the cluster kernel, [1] its potentials' variant:
+  int cluster_active[2] = {0, 0};       // clusters co-resident on the device (last shape checked)
+  long cluster_checked_key[2] = {-1, -1};  // (shared bytes, cluster size, warps) last checked
+  int cluster_ok[2] = {0, 0};             // that cluster shape is schedulable here
+  int cluster_nonportable = 0;  // cluster kernels allowed more than 8 CTAs
   int band_attr = 0;            // shared memory cap granted to the persistent-band sweep
   long band_key = -1;           // shared bytes of its last occupancy query
   int band_blocks = 0;          // co-resident blocks for that size

@@ -446,6 +446,24 @@ __global__ void __launch_bounds__(kThreads) k_sor_f64(GridDev g, const __grid_co
   }
 }
 
+// double -> float with round to nearest even, on the integer pipes (GB300
+// issues conversion instructions on its narrow FP64 pipe); values beyond the
+// float range become infinities, values below its normal range signed zero
+__device__ __forceinline__ float narrow_f64(double x) {
+  const unsigned hi = unsigned(__double2hiint(x)), lo = unsigned(__double2loint(x));
+  const unsigned sign = hi & 0x80000000u;
+  const int dex = int((hi >> 20) & 0x7ffu);
+  if (dex == 0x7ff) return __uint_as_float(sign | 0x7f800000u | ((hi & 0xfffffu) ? 0x400000u : 0u));
+  const int fex = dex - 896;
+  if (fex >= 255) return __uint_as_float(sign | 0x7f800000u);
+  if (fex <= 0) return __uint_as_float(sign);
+  // 23 mantissa bits: 20 from hi, 3 from lo; the remaining 29 bits round
+  unsigned bits = (unsigned(fex) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const unsigned rest = lo & 0x1fffffffu;
+  if (rest > 0x10000000u || (rest == 0x10000000u && (bits & 1u))) ++bits;  // may carry into the exponent
+  return __uint_as_float(sign | bits);
+}
+
 // float -> double by bit manipulation on the integer pipes (GB300 issues
 // conversion instructions on its narrow FP64 pipe); exact for normal floats,
 // infinities and NaNs; float subnormals (|e| < 1.2e-38, far below any
@@ -708,12 +726,17 @@ __device__ void smem_boundary(const GridDev &g, float *E, int R0, int R1, int ra
 
 // dynamic shared memory of k_mixed_cluster: (residual, omega/lhs) pairs of
 // the band's points, correction band with 4-row halos, b(mu) of the band's
-// rows, d(nu) by ext column, the CTA's segment offsets, then its chunk list
-size_t cluster_smem_bytes(const GridDev &g) {
-  return 2 * size_t(g.cl_maxrows) * g.n8 * sizeof(float) + size_t(g.cl_maxrows + 8) * g.n8 * sizeof(float) +
-         size_t(g.cl_maxrows + g.n8) * sizeof(float) + size_t(5 * (g.nlev + 2) + 1) * sizeof(int) +
+// rows, d(nu) by ext column, the CTA's segment offsets, then its chunk list.
+// k_mixed_cluster_pot (potentials, lhs = f3(mu) + idel^2 (e_mu(mu) -
+// e_nu(nu))) keeps the residual alone and the lhs as a row term of the
+// band's rows and a column term by ext column, after d(nu).
+size_t cluster_smem_bytes(const GridDev &g, bool sep) {
+  const size_t band = size_t(g.cl_maxrows) * g.n8 * sizeof(float);
+  return (sep ? band : 2 * band) + size_t(g.cl_maxrows + 8) * g.n8 * sizeof(float) +
+         size_t(g.cl_maxrows + g.n8) * sizeof(float) * (sep ? 2 : 1) + size_t(5 * (g.nlev + 2) + 1) * sizeof(int) +
          size_t(g.cl_maxchunks) * sizeof(int);
 }
+constexpr int kClusterPotThreads = 512;  // potentials' variant: 16 warps, two CTAs per SM
 
 // split cluster barrier: arrive releases this thread's earlier shared and
 // distributed-shared writes, wait acquires every CTA's released writes
@@ -745,11 +768,13 @@ struct BandWalk {
 struct ClusterBand {
   float *E;               // correction rows [R0-4, R1+4) of the band
   const float2 *RW;       // (residual, omega/lhs) by band row * n8 + col
+  const float *R;         // potentials' variant: residual by band row * n8 + col
   const float *BT, *DN;   // b(mu) by band row, d(nu) by ext column
+  const float *LP, *LQ;   // potentials' variant: lhs = LP[band row] - LQ[ext column]
   const unsigned *PL;     // chunks (band row << 19) | (col << 2) | (count-1)
   float *up, *dn;         // neighbours' halos addressed like E, or null
   int n8, hdn;            // band rows >= hdn feed the lower neighbour
-  float omega1;
+  float omega, omega1;
   CoefF cf;
 };
 
@@ -758,9 +783,12 @@ struct ClusterBand {
 // point's left neighbours are the previous point's right ones); every read
 // precedes every write.  Positions past the chunk's count are computed but
 // not stored: their reads stay inside the CTA's shared allocation (at most
-// 10 elements past the correction band, the pairs or d(nu), each followed
-// by a larger array).
-template <bool halo>
+// 10 elements past the correction band, the pairs, the residual, d(nu) or
+// the lhs column term, each followed by a larger array).  kSep: omega / lhs
+// from the row and column terms (fast reciprocal: the correction sweep is
+// the inner solver of the FP64 defect correction, whose fixed point does
+// not depend on it).
+template <bool halo, bool kSep>
 __device__ __forceinline__ void cluster_chunk(const ClusterBand &B, unsigned q) {
   const int n8 = B.n8;
   const int lr = int(q >> 19), col = int((q >> 2) & 0x1ffffu), n = int(q & 3u) + 1;
@@ -779,7 +807,11 @@ __device__ __forceinline__ void cluster_chunk(const ClusterBand &B, unsigned q) 
     const float m2 = pj[-2 * n8], p2 = pj[2 * n8], m1 = pj[-n8], p1 = pj[n8];
     const float l4 = rv[5 * j], l3 = rv[5 * j + 1], l2 = rv[5 * j + 2], l1 = rv[5 * j + 3], ec = rv[5 * j + 4];
     const float r1 = rv[5 * j + 5], r2 = rv[5 * j + 6], r3 = rv[5 * j + 7], r4 = rv[5 * j + 8];
-    const float2 rw = B.RW[ls + 5 * j];
+    float2 rw;
+    if (kSep)
+      rw = make_float2(B.R[ls + 5 * j], __fdividef(B.omega, B.LP[lr] - B.LQ[col + 5 * j]));
+    else
+      rw = B.RW[ls + 5 * j];
     const float d = B.DN[col + 5 * j];
     float dm2 = cf.dmu2[0] * (m4 + p4);
     dm2 = __fmaf_rn(cf.dmu2[1], m3 + p3, dm2);
@@ -819,9 +851,9 @@ __device__ __forceinline__ void cluster_chunk(const ClusterBand &B, unsigned q) 
 
 // update chunks [b0, b1) of the CTA's list (their points are independent),
 // thread t of the n threads of a warp role taking chunks t, t+n, ...
-template <bool halo>
+template <bool halo, bool kSep>
 __device__ __forceinline__ void cluster_chunks(const ClusterBand &B, int b0, int b1, int t, int n) {
-  for (int k = b0 + t; k < b1; k += n) cluster_chunk<halo>(B, B.PL[k]);
+  for (int k = b0 + t; k < b1; k += n) cluster_chunk<halo, kSep>(B, B.PL[k]);
 }
 
 // barrier among the seam warps only (named barrier 1)
@@ -829,8 +861,8 @@ __device__ __forceinline__ void seam_barrier(int nthreads) {
   asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
 }
 
-__global__ void __launch_bounds__(kClusterMaxThreads, 1) k_mixed_cluster(GridDev g, const __grid_constant__ JobTable jobs,
-                                                                        int nsweeps) {
+template <bool kSep>
+__device__ __forceinline__ void mixed_cluster_body(const GridDev &g, const JobTable &jobs, int nsweeps) {
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
   const int C = int(cl.num_blocks()), rank = int(cl.block_rank());
@@ -843,10 +875,13 @@ __global__ void __launch_bounds__(kClusterMaxThreads, 1) k_mixed_cluster(GridDev
   const int R0 = g.cl_row0[rank], R1 = g.cl_row0[rank + 1];
   const int nloc = (g.cl_maxrows + 8) * n8;
   float2 *const RW = smem2;
-  float *const E = reinterpret_cast<float *>(RW + g.cl_maxrows * n8);
+  float *const RR = reinterpret_cast<float *>(smem2);
+  float *const E = kSep ? RR + g.cl_maxrows * n8 : reinterpret_cast<float *>(RW + g.cl_maxrows * n8);
   float *const BT = E + nloc;
   float *const DN = BT + g.cl_maxrows;
-  int *const SO = reinterpret_cast<int *>(DN + n8);  // segment offsets into PL
+  float *const LP = DN + n8;                   // kSep only
+  float *const LQ = LP + g.cl_maxrows;         // kSep only
+  int *const SO = reinterpret_cast<int *>(kSep ? LQ + n8 : DN + n8);  // segment offsets into PL
   unsigned *const PL = reinterpret_cast<unsigned *>(SO + 5 * S + 1);
   const int *const coff = g.cl_off + size_t(rank) * 5 * S;
   const int pbase = coff[0], npl = coff[5 * S] - pbase;
@@ -854,6 +889,16 @@ __global__ void __launch_bounds__(kClusterMaxThreads, 1) k_mixed_cluster(GridDev
   for (int k = threadIdx.x; k < nloc; k += blockDim.x) E[k] = 0.0f;
   for (int k = threadIdx.x; k < R1 - R0; k += blockDim.x) BT[k] = bt[R0 + k - 4];
   for (int k = threadIdx.x; k < n8; k += blockDim.x) DN[k] = (k >= 4 && k < nni + 4) ? g.d_nu32[k - 4] : 0.0f;
+  if (kSep) {
+    // lhs = f3 + idel^2 e with e = e_mu - e_nu: the row term in FP64, then
+    // both terms in FP32 (the nu axis columns, never updated, get 0)
+    for (int k = threadIdx.x; k < R1 - R0; k += blockDim.x) {
+      const int mu = R0 + k - 4;
+      LP[k] = narrow_f64(fma(J.idel2, g.e_mu[mu], g.f3_mu[mu]));
+    }
+    for (int k = threadIdx.x; k < n8; k += blockDim.x)
+      LQ[k] = (k >= 4 && k < nni + 4) ? narrow_f64(J.idel2 * g.e_nu[k - 4]) : 0.0f;
+  }
   for (int k = threadIdx.x; k < npl; k += blockDim.x) PL[k] = unsigned(g.cl_pts[pbase + k]);
   const int ra = (R0 < 5) ? 5 : R0, ncols = nni - 2, nband = (R1 - ra) * ncols;
   {
@@ -869,23 +914,32 @@ __global__ void __launch_bounds__(kClusterMaxThreads, 1) k_mixed_cluster(GridDev
           const int ik = (w.row - 4) * nni + (w.col - 4);
           ls[j] = (w.row - R0) * n8 + w.col;
           rv[j] = r32[ik];
-          wv[j] = w32[ik];
+          if (!kSep) wv[j] = w32[ik];
         }
         w.next();
       }
 #pragma unroll
       for (int j = 0; j < 4; ++j)
-        if (ls[j] >= 0) RW[ls[j]] = make_float2(rv[j], wv[j]);
+        if (ls[j] >= 0) {
+          if (kSep)
+            RR[ls[j]] = rv[j];
+          else
+            RW[ls[j]] = make_float2(rv[j], wv[j]);
+        }
     }
   }
   ClusterBand B;
   B.E = E;
   B.RW = RW;
+  B.R = RR;
   B.BT = BT;
   B.DN = DN;
+  B.LP = LP;
+  B.LQ = LQ;
   B.PL = PL;
   B.n8 = n8;
   B.hdn = R1 - R0 - 4;
+  B.omega = J.omegaf;
   B.omega1 = J.omega1f;
   for (int k = 0; k < 4; ++k) {
     B.cf.dmu1[k] = g.dmu1f[k];
@@ -899,11 +953,12 @@ __global__ void __launch_bounds__(kClusterMaxThreads, 1) k_mixed_cluster(GridDev
   B.up = (rank > 0) ? cl.map_shared_rank(E, rank - 1) + (R0 - g.cl_row0[rank - 1]) * n8 : nullptr;
   B.dn = (rank < C - 1) ? cl.map_shared_rank(E, rank + 1) + (R0 - R1) * n8 : nullptr;
   // warp roles: interior, edge, seam
+  const int wa = kSep ? g.cl_pa : g.cl_wa, wb = kSep ? g.cl_pb : g.cl_wb, ws = kSep ? g.cl_ps : g.cl_ws;
   const int warp = threadIdx.x >> 5;
-  const int role = (warp < g.cl_wa) ? 0 : (warp < g.cl_wa + g.cl_wb) ? 1 : 2;
-  const int rbase = (role == 0) ? 0 : (role == 1) ? g.cl_wa : g.cl_wa + g.cl_wb;
+  const int role = (warp < wa) ? 0 : (warp < wa + wb) ? 1 : 2;
+  const int rbase = (role == 0) ? 0 : (role == 1) ? wa : wa + wb;
   const int rt = threadIdx.x - 32 * rbase;
-  const int rn = 32 * ((role == 0) ? g.cl_wa : (role == 1) ? g.cl_wb : g.cl_ws);
+  const int rn = 32 * ((role == 0) ? wa : (role == 1) ? wb : ws);
   __syncthreads();
   cluster_arrive();  // this band is zeroed: neighbours may push into its halos
   for (int s = 0; s < nsweeps; ++s) {
@@ -918,18 +973,18 @@ __global__ void __launch_bounds__(kClusterMaxThreads, 1) k_mixed_cluster(GridDev
       // overwrites.  Interior points need only this CTA's values; seam points
       // go level by level among the seam warps.
       if (role == 0) {
-        cluster_chunks<false>(B, o[0], o[1], rt, rn);
+        cluster_chunks<false, kSep>(B, o[0], o[1], rt, rn);
         cluster_wait();
       } else if (role == 1) {
         cluster_wait();
-        cluster_chunks<true>(B, o[1], o[2], rt, rn);
+        cluster_chunks<true, kSep>(B, o[1], o[2], rt, rn);
       } else {
         cluster_wait();
-        cluster_chunks<true>(B, o[2], o[3], rt, rn);
+        cluster_chunks<true, kSep>(B, o[2], o[3], rt, rn);
         for (int l = 1; l < nlev; ++l) {
           if (o[2 + l] == o[3 + l]) continue;
           seam_barrier(rn);
-          cluster_chunks<true>(B, o[2 + l], o[3 + l], rt, rn);
+          cluster_chunks<true, kSep>(B, o[2 + l], o[3 + l], rt, rn);
         }
       }
       __syncthreads();
@@ -980,6 +1035,19 @@ __global__ void __launch_bounds__(kClusterMaxThreads, 1) k_mixed_cluster(GridDev
   }
 }
 
+__global__ void __launch_bounds__(kClusterMaxThreads, 1) k_mixed_cluster(GridDev g, const __grid_constant__ JobTable jobs,
+                                                                        int nsweeps) {
+  mixed_cluster_body<false>(g, jobs, nsweeps);
+}
+
+// Potentials only (job kind 1): two CTAs per SM, so that twice the clusters
+// are co-resident for the batches of an SCF iteration's potentials
+__global__ void __launch_bounds__(kClusterPotThreads, 2) k_mixed_cluster_pot(GridDev g,
+                                                                            const __grid_constant__ JobTable jobs,
+                                                                            int nsweeps) {
+  mixed_cluster_body<true>(g, jobs, nsweeps);
+}
+
 // ----------------------------------------------------------------------
 // Mixed form: ghost refresh, FP64 residual, FP32 correction, FP64 update.
 // ----------------------------------------------------------------------
@@ -1004,24 +1072,6 @@ __device__ __forceinline__ void ghost_point(const GridDev &g, double *u, int k, 
     const double v = u[(4 + i) * g.n8 + col];
     u[(4 - i) * g.n8 + col] = neg ? -v : v;
   }
-}
-
-// double -> float with round to nearest even, on the integer pipes (GB300
-// issues conversion instructions on its narrow FP64 pipe); values beyond the
-// float range become infinities, values below its normal range signed zero
-__device__ __forceinline__ float narrow_f64(double x) {
-  const unsigned hi = unsigned(__double2hiint(x)), lo = unsigned(__double2loint(x));
-  const unsigned sign = hi & 0x80000000u;
-  const int dex = int((hi >> 20) & 0x7ffu);
-  if (dex == 0x7ff) return __uint_as_float(sign | 0x7f800000u | ((hi & 0xfffffu) ? 0x400000u : 0u));
-  const int fex = dex - 896;
-  if (fex >= 255) return __uint_as_float(sign | 0x7f800000u);
-  if (fex <= 0) return __uint_as_float(sign);
-  // 23 mantissa bits: 20 from hi, 3 from lo; the remaining 29 bits round
-  unsigned bits = (unsigned(fex) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
-  const unsigned rest = lo & 0x1fffffffu;
-  if (rest > 0x10000000u || (rest == 0x10000000u && (bits & 1u))) ++bits;  // may carry into the exponent
-  return __uint_as_float(sign | bits);
 }
 
 // u at ext (row, col) with the putin ghost cells (inout.F90:47-80) read as
@@ -1051,9 +1101,11 @@ __device__ __forceinline__ double ghost_read(const GridDev &g, const double *u, 
 // so u needs no ghost refresh first.  kPacked: the points are taken in
 // st_pts order and stored as (r, w) pairs in that order (persistent-band
 // sweep);
-// otherwise r32 / w32 are plain nni x nmu arrays (cluster sweep).
+// otherwise r32 / w32 are plain nni x nmu arrays (cluster sweep; need_w 0:
+// the potentials' cluster sweep forms omega / lhs itself, only r32 is
+// stored).
 template <bool kPacked>
-__global__ void k_residual(GridDev g, const __grid_constant__ JobTable jobs, int zero_e) {
+__global__ void k_residual(GridDev g, const __grid_constant__ JobTable jobs, int zero_e, int need_w) {
   const JobDev &J = jobs.j[blockIdx.y];
   const int nint = (g.nni - 2) * (g.nmu - 5);
   const int n8 = g.n8;
@@ -1108,7 +1160,7 @@ __global__ void k_residual(GridDev g, const __grid_constant__ JobTable jobs, int
       J.rw[k] = make_float2(narrow_f64(rhs - cc), J.omegaf / narrow_f64(lhs));
     } else {
       J.r32[ik] = narrow_f64(rhs - cc);
-      J.w32[ik] = J.omegaf / narrow_f64(lhs);
+      if (need_w) J.w32[ik] = J.omegaf / narrow_f64(lhs);
     }
   }
 }
@@ -1541,6 +1593,89 @@ __global__ void k_overlaps(GridDev g, const double *psi, PtrList o, int n, doubl
   block_sum_finish<kMaxK>(v, partials, out, n, ticket);
 }
 
+// One round of the orthonormalisation of several orbitals (normOrtho.F90:
+// 14-59, 103-207, scfUtils.F90:380-434): orbital blockIdx.y of the round's
+// list.  Each orbital's sums run over the same blocks in the same order as
+// k_norm / k_overlaps, so the results equal the one-orbital launches.
+constexpr int kRoundItems = 12;
+struct OrthoItem {
+  double *psi;
+  const double *o[kMaxK];  // orthogonalisation partners (normalised earlier)
+  int n;                   // number of partners
+  int ihomo;               // 0: scale only; +-1: scale and setCiOrb
+  double *norm_out;        // sum wgt2 psi psi f4
+  double *ovl_out;         // overlaps with the partners
+};
+struct OrthoRound {
+  OrthoItem it[kRoundItems];
+};
+
+__global__ void k_norm_round(GridDev g, const __grid_constant__ OrthoRound R, double *partials, unsigned *tickets) {
+  const OrthoItem &I = R.it[blockIdx.y];
+  double v[1] = {0.0};
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+    const int mu = k / g.nni, nu = k - mu * g.nni;
+    const double p = I.psi[(mu + 4) * g.n8 + nu + 4];
+    v[0] += g.wgt2[k] * M(M(p, p), g.f4[k]);
+  }
+  block_sum_finish<1>(v, partials + size_t(blockIdx.y) * gridDim.x, I.norm_out, 1, tickets + blockIdx.y);
+}
+
+__global__ void k_scale_round(GridDev g, const __grid_constant__ OrthoRound R) {
+  const OrthoItem &I = R.it[blockIdx.y];
+  const double zarea = D(1.0, sqrt(*I.norm_out));
+  if (I.ihomo == 0) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+      const int mu = k / g.nni, nu = k - mu * g.nni;
+      const int ij = (mu + 4) * g.n8 + nu + 4;
+      I.psi[ij] = M(zarea, I.psi[ij]);
+    }
+    return;
+  }
+  const int n2 = g.nni / 2 + 1;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n2 * g.nmu; k += gridDim.x * blockDim.x) {
+    const int mu = k / n2, ni = k - mu * n2;
+    const int row = (mu + 4) * g.n8 + 4;
+    if (ni < n2 - 1) {
+      const double v = M(zarea, I.psi[row + ni]);
+      I.psi[row + ni] = v;
+      I.psi[row + (g.nni - 1 - ni)] = (I.ihomo == 1) ? v : -v;
+    } else {
+      I.psi[row + ni] = (I.ihomo == 1) ? M(zarea, I.psi[row + ni]) : 0.0;
+    }
+  }
+}
+
+__global__ void k_overlaps_round(GridDev g, const __grid_constant__ OrthoRound R, double *partials,
+                                 unsigned *tickets) {
+  const OrthoItem &I = R.it[blockIdx.y];
+  double v[kMaxK];
+  for (int q = 0; q < kMaxK; ++q) v[q] = 0.0;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+    const int mu = k / g.nni, nu = k - mu * g.nni;
+    const int ij = (mu + 4) * g.n8 + nu + 4;
+    const double p = I.psi[ij], w = g.wgt2[k], f4 = g.f4[k];
+    for (int q = 0; q < I.n; ++q) v[q] += w * M(M(p, I.o[q][ij]), f4);
+  }
+  block_sum_finish<kMaxK>(v, partials + size_t(blockIdx.y) * gridDim.x * kMaxK, I.ovl_out, I.n,
+                          tickets + blockIdx.y);
+}
+
+__global__ void k_ortho_round(GridDev g, const __grid_constant__ OrthoRound R) {
+  const OrthoItem &I = R.it[blockIdx.y];
+  const double *ovl = I.ovl_out;
+  double ano = 0.0;
+  for (int q = 0; q < I.n; ++q) ano = A(ano, M(ovl[q], ovl[q]));
+  ano = D(sqrt(A(1.0, ano)), S(1.0, M(ano, ano)));
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+    const int mu = k / g.nni, nu = k - mu * g.nni;
+    const int ij = (mu + 4) * g.n8 + nu + 4;
+    double v = I.psi[ij];
+    for (int q = 0; q < I.n; ++q) v = A(M(-ovl[q], I.o[q][ij]), v);
+    I.psi[ij] = M(ano, v);
+  }
+}
+
 // EaHF = oneelij(i,i) + (J + K): per point terms of integrals.F90:406-480
 // and lagrangeMultipliers.F90:67-72.  psi's ghost cells are read as the
 // mirrored interior values (identical to a putin ghost refresh); exact keeps
@@ -1788,6 +1923,10 @@ static bool cluster_attributes(x2g_ctx *ctx) {
       cudaFuncSetAttribute((const void *)k_mixed_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) !=
           cudaSuccess ||
       cudaFuncSetAttribute((const void *)k_mixed_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute((const void *)k_mixed_cluster_pot, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute((const void *)k_mixed_cluster_pot, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
           cudaSuccess) {
     (void)cudaGetLastError();
     return false;
@@ -1797,20 +1936,27 @@ static bool cluster_attributes(x2g_ctx *ctx) {
   return true;
 }
 
-// whether the on-chip cluster sweep can run this grid here (asked once per
-// shape: shared memory per CTA, cluster size, block size)
-static bool cluster_usable(x2g_ctx *ctx, const GridDev &g) {
+// block size of the cluster sweep (pot: the potentials' variant)
+static int cluster_threads(const GridDev &g, bool pot) {
+  return 32 * (pot ? g.cl_pa + g.cl_pb + g.cl_ps : g.cl_wa + g.cl_wb + g.cl_ws);
+}
+
+// whether the on-chip cluster sweep (pot: its potentials' variant) can run
+// this grid here, and how many of its clusters are co-resident (asked once
+// per shape: shared memory per CTA, cluster size, block size)
+static bool cluster_usable(x2g_ctx *ctx, const GridDev &g, bool pot = false) {
   if (g.cl_size < 2 || ctx->no_cluster) return false;
-  const size_t smem = cluster_smem_bytes(g);
-  const long key = (long(smem) * 64 + g.cl_size) * 32 + (g.cl_wa + g.cl_wb + g.cl_ws);
-  if (ctx->cluster_checked_key != key) {
-    ctx->cluster_checked_key = key;
-    ctx->cluster_ok = 0;
+  const size_t smem = cluster_smem_bytes(g, pot);
+  const long key = (long(smem) * 64 + g.cl_size) * 32 + cluster_threads(g, pot) / 32;
+  const int v = pot ? 1 : 0;
+  if (ctx->cluster_checked_key[v] != key) {
+    ctx->cluster_checked_key[v] = key;
+    ctx->cluster_ok[v] = 0;
     const bool attr_ok = cluster_attributes(ctx) && smem <= ctx->cluster_smem_set;
     if (attr_ok) {
       cudaLaunchConfig_t q = {};
       q.gridDim = dim3(unsigned(g.cl_size));
-      q.blockDim = dim3(unsigned(32 * (g.cl_wa + g.cl_wb + g.cl_ws)));
+      q.blockDim = dim3(unsigned(cluster_threads(g, pot)));
       q.dynamicSmemBytes = smem;
       cudaLaunchAttribute qa[1];
       qa[0].id = cudaLaunchAttributeClusterDimension;
@@ -1820,15 +1966,15 @@ static bool cluster_usable(x2g_ctx *ctx, const GridDev &g) {
       q.attrs = qa;
       q.numAttrs = 1;
       int nclusters = 0;
-      if (cudaOccupancyMaxActiveClusters(&nclusters, (const void *)k_mixed_cluster, &q) == cudaSuccess &&
-          nclusters > 0) {
-        ctx->cluster_ok = 1;
-        ctx->cluster_active = nclusters;
+      const void *fn = pot ? (const void *)k_mixed_cluster_pot : (const void *)k_mixed_cluster;
+      if (cudaOccupancyMaxActiveClusters(&nclusters, fn, &q) == cudaSuccess && nclusters > 0) {
+        ctx->cluster_ok[v] = 1;
+        ctx->cluster_active[v] = nclusters;
       }
     }
     (void)cudaGetLastError();
   }
-  return ctx->cluster_ok != 0;
+  return ctx->cluster_ok[v] != 0;
 }
 
 // Launch shape of the persistent-band sweep: the most jobs per launch (at
@@ -1899,16 +2045,16 @@ static int f64_block_limit(x2g_ctx *ctx) {
 
 // One launch batch (at most kParamJobs jobs) of launch_relax.
 static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, int nsweeps, bool mixed,
-                       bool on_chip, int G, size_t smem) {
+                       bool on_chip, bool pot, int G, size_t smem) {
   cudaError_t err;
   x2g_ctx::Pending pe{};
   const double points = double(njobs) * double(g.nni - 2) * double(g.nmu - 5) * double(nsweeps);
   if (mixed) {
     dim3 gr(grid_blocks((g.nni - 2) * (g.nmu - 5)), njobs);
     if (on_chip)
-      k_residual<false><<<gr, kThreads, 0, ctx->stream>>>(g, jt, 0);
+      k_residual<false><<<gr, kThreads, 0, ctx->stream>>>(g, jt, 0, pot ? 0 : 1);
     else
-      k_residual<true><<<gr, kThreads, 0, ctx->stream>>>(g, jt, 1);
+      k_residual<true><<<gr, kThreads, 0, ctx->stream>>>(g, jt, 1, 1);
     ctx->launches += 1;
   }
   if (ctx->profiling) {
@@ -1919,12 +2065,12 @@ static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, 
     cudaEventRecord(pe.a, ctx->stream);
   }
   if (on_chip) {
-    const size_t smem = cluster_smem_bytes(g);
+    const size_t smem = cluster_smem_bytes(g, pot);
     if (!cluster_attributes(ctx) || smem > ctx->cluster_smem_set)
       return set_status(X2G_ERR_CUDA, "cluster kernel attributes could not be set");
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(unsigned(njobs * g.cl_size));
-    cfg.blockDim = dim3(unsigned(32 * (g.cl_wa + g.cl_wb + g.cl_ws)));
+    cfg.blockDim = dim3(unsigned(cluster_threads(g, pot)));
     cfg.dynamicSmemBytes = smem;
     cfg.stream = ctx->stream;
     cudaLaunchAttribute attr[1];
@@ -1935,7 +2081,8 @@ static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, 
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     GridDev gd = g;
-    err = cudaLaunchKernelEx(&cfg, k_mixed_cluster, gd, jt, nsweeps);
+    err = pot ? cudaLaunchKernelEx(&cfg, k_mixed_cluster_pot, gd, jt, nsweeps)
+              : cudaLaunchKernelEx(&cfg, k_mixed_cluster, gd, jt, nsweeps);
     if (err != cudaSuccess) return cuda_status(err, "cluster MCSOR launch");
     ctx->launches += 1;
     if (ctx->profiling) {
@@ -2022,6 +2169,17 @@ static int relax_sor(x2g_ctx *ctx, const x2g_grid *grid, const x2g_job *jobs, in
   return X2G_OK;
 }
 
+// co-resident clusters of the cluster sweep and of its potentials' variant
+// for this grid on the context's device (0: that kernel cannot run it)
+int cluster_occupancy(x2g_ctx *ctx, x2g_grid *grid, int *plain, int *pot) {
+  const GridDev &g = grid->d;
+  const int a = cluster_usable(ctx, g, false) ? ctx->cluster_active[0] : 0;
+  const int b = cluster_usable(ctx, g, true) ? ctx->cluster_active[1] : 0;
+  if (plain) *plain = a;
+  if (pot) *pot = b;
+  return set_status(X2G_OK, "");
+}
+
 int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, int nsweeps, int precision) {
   if (njobs <= 0) return X2G_OK;
   if (nsweeps <= 0) return set_status(X2G_ERR_ARG, "nsweeps must be positive");
@@ -2030,7 +2188,16 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
   const GridDev &g = grid->d;
   const bool mixed = (precision == X2G_MIXED);
   bool on_chip = mixed && cluster_usable(ctx, g);
-  if (on_chip && ctx->auto_band && njobs > ctx->cluster_active) {
+  // potentials built from orbitals (separable lhs): the variant at two CTAs
+  // per SM when the batch is larger than the clusters co-resident at one
+  bool pot = false;
+  if (on_chip && ctx->pot_clusters != 0) {
+    pot = true;
+    for (int i = 0; i < njobs && pot; ++i) pot = (jobs[i].kind == 1 && !(jobs[i].lhs && jobs[i].rhs));
+    if (pot && ctx->pot_clusters == 2) pot = njobs > ctx->cluster_active[0];
+    pot = pot && cluster_usable(ctx, g, true);
+  }
+  if (on_chip && !pot && ctx->auto_band && njobs > ctx->cluster_active[0]) {
     // more jobs than co-resident clusters: the cluster kernel would run in
     // waves, while the persistent-band kernel may hold the whole batch
     int nj = 0, G1 = 0;
@@ -2070,7 +2237,7 @@ int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, i
         d.rhs_buf = reinterpret_cast<double *>(p);
       }
     }
-    int rc = relax_batch(ctx, g, jt, nb, nsweeps, mixed, on_chip, G, smem);
+    int rc = relax_batch(ctx, g, jt, nb, nsweeps, mixed, on_chip, pot, G, smem);
     if (rc) return rc;
   }
   // barrier error word: checked by the caller at its next synchronisation
@@ -2269,6 +2436,37 @@ void launch_overlaps(x2g_ctx *ctx, const GridDev &g, const double *psi, const do
     for (int q = 0; q < m; ++q) L.p[q] = others[b + q];
     k_overlaps<<<red_blocks(g), kThreads, 0, ctx->stream>>>(g, psi, L, m, part, out + b, ctx->bar + 3);
     ctx->launches += 1;
+  }
+}
+
+// one orthonormalisation round: norms, scaling (and setCiOrb), overlaps
+// with the partners, Gram-Schmidt, each over all orbitals of the round
+void launch_ortho_round(x2g_ctx *ctx, const GridDev &g, const OrthoOrbital *orbs, int n) {
+  const int nb = red_blocks(g);
+  for (int b = 0; b < n; b += kRoundItems) {
+    const int m = (n - b < kRoundItems) ? n - b : kRoundItems;
+    OrthoRound R{};
+    bool any_partner = false;
+    for (int q = 0; q < m; ++q) {
+      const OrthoOrbital &x = orbs[b + q];
+      OrthoItem &I = R.it[q];
+      I.psi = x.psi;
+      I.n = x.n;
+      for (int k = 0; k < x.n; ++k) I.o[k] = x.partners[k];
+      I.ihomo = x.ihomo;
+      I.norm_out = x.norm_out;
+      I.ovl_out = x.ovl_out;
+      any_partner = any_partner || x.n > 0;
+    }
+    double *part = reduction_partials(ctx, kMaxK * kRoundItems);
+    k_norm_round<<<dim3(nb, m), kThreads, 0, ctx->stream>>>(g, R, part, ctx->bar + kMomentTickets);
+    k_scale_round<<<dim3(grid_blocks(g.mxsize), m), kThreads, 0, ctx->stream>>>(g, R);
+    ctx->launches += 2;
+    if (any_partner) {
+      k_overlaps_round<<<dim3(nb, m), kThreads, 0, ctx->stream>>>(g, R, part, ctx->bar + kMomentTickets);
+      k_ortho_round<<<dim3(grid_blocks(g.mxsize), m), kThreads, 0, ctx->stream>>>(g, R);
+      ctx->launches += 2;
+    }
   }
 }
 

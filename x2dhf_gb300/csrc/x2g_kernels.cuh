@@ -51,6 +51,7 @@ struct AsymptArgs {
 };
 
 // ---- sweeps ----
+int cluster_occupancy(x2g_ctx *ctx, x2g_grid *grid, int *plain, int *pot);
 int launch_relax(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jobs, int njobs, int nsweeps, int precision);
 // FP64 sweep whose job table, right-hand-side buffers and barrier words live
 // in caller-provided device scratch (no allocation on this path).
@@ -100,6 +101,18 @@ void launch_overlaps(x2g_ctx *ctx, const GridDev &g, const double *psi, const do
 // needed); exact: the reference's unfused FP64 order, else FMAs (mixed form)
 void launch_eahf(x2g_ctx *ctx, const GridDev &g, const double *psi, int isym, int m, const double *coulp,
                  const double *exchp, double *ee_out, double *parts, bool exact = true);
+// One orthonormalisation round over orbitals whose partners were finished
+// in earlier rounds: norm (out norm_out), scaling by 1/sqrt(norm) (and
+// setCiOrb with ihomo = +-1; 0 scales only), overlaps with the partners (out
+// ovl_out) and the Gram-Schmidt step; the same sums and operations as
+// launch_norm / launch_scale(_setci) / launch_overlaps / launch_ortho_apply.
+struct OrthoOrbital {
+  double *psi;
+  const double *partners[16];
+  int n, ihomo;
+  double *norm_out, *ovl_out;
+};
+void launch_ortho_round(x2g_ctx *ctx, const GridDev &g, const OrthoOrbital *orbs, int n);
 // EaHF of several orbitals in one launch (same sums, same order as launch_eahf)
 struct EahfItem {
   const double *psi, *coulp, *exchp;

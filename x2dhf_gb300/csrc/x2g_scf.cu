@@ -491,6 +491,42 @@ std::vector<int> ortho_partners(x2g_scf *s, int iorb1) {
   return v;
 }
 
+// Batch mode 2, no orbital frozen: the norms and Gram-Schmidt steps of the
+// iteration in rounds.  Orbital i is orthogonalised only against the higher
+// orbitals of its own symmetry, which the reference's loop has finished by
+// then, so an orbital's round is 1 + the latest round of its partners; the
+// orbitals of one round are independent and each goes through the same
+// operations as in the loop.  N2: 3 rounds instead of 6 orbitals.  false:
+// an orbital has more partners than one round item holds.
+bool orthonormalise_in_rounds(x2g_scf *s) {
+  const int norb = s->norb;
+  std::vector<int> depth(norb + 1, 0);
+  std::vector<std::vector<int>> partners(norb + 1);
+  int maxd = 0;
+  for (int iorb = norb; iorb >= 1; iorb--) {
+    partners[iorb] = ortho_partners(s, iorb);
+    if (partners[iorb].size() > 16) return false;
+    for (int q : partners[iorb]) depth[iorb] = std::max(depth[iorb], depth[q] + 1);
+    maxd = std::max(maxd, depth[iorb]);
+  }
+  for (int r = 0; r <= maxd; r++) {
+    std::vector<OrthoOrbital> v;
+    for (int iorb = norb; iorb >= 1; iorb--) {
+      if (depth[iorb] != r) continue;
+      OrthoOrbital x{};
+      x.psi = s->orb[iorb];
+      x.n = int(partners[iorb].size());
+      for (int k = 0; k < x.n; k++) x.partners[k] = s->orb[partners[iorb][k]];
+      x.ihomo = s->cs.homonuclear ? s->ihomo[iorb] : 0;
+      x.norm_out = s->sc + x2g_scf::O_NORM + iorb;
+      x.ovl_out = s->sc + x2g_scf::O_OVL + 64 * iorb;
+      v.push_back(x);
+    }
+    launch_ortho_round(s->ctx, s->grid->d, v.data(), int(v.size()));
+  }
+  return true;
+}
+
 void ortho(x2g_scf *s, int iorb) {
   if (s->ifixorb[iorb] != 0) return;  // normOrtho.F90:143
   std::vector<int> p = ortho_partners(s, iorb);
@@ -768,6 +804,7 @@ int scf_iteration(x2g_scf *s, int *rc) {
     if (s->cs.batch_mode == 2 && !s->lfixorb)
       if ((*rc = relax_all_orbitals(s))) return 1;
   }
+  const bool rounds = s->cs.batch_mode == 2 && !frozen && !s->lfixorb && norb > 1 && orthonormalise_in_rounds(s);
   for (int i = 1; i <= norb; i++) {
     const int iorb = norb - i + 1;
     if (!batched) {
@@ -781,7 +818,9 @@ int scf_iteration(x2g_scf *s, int *rc) {
     }
     if (!s->lfixorb && s->cs.batch_mode != 2)
       if ((*rc = relax_orbital(s, iorb))) return 1;
-    if (s->ifixorb[iorb] == 0 && s->cs.homonuclear) {
+    if (rounds) {
+      // normalised and orthogonalised above
+    } else if (s->ifixorb[iorb] == 0 && s->cs.homonuclear) {
       // norm scaling and setCiOrb in one pass
       double *out = s->sc + x2g_scf::O_NORM + iorb;
       launch_norm(s->ctx, s->grid->d, s->orb[iorb], out);
@@ -790,7 +829,7 @@ int scf_iteration(x2g_scf *s, int *rc) {
       if (s->ifixorb[iorb] == 0) norm(s, iorb);
       if (s->cs.homonuclear) launch_setci(s->ctx, s->grid->d, s->orb[iorb], s->ihomo[iorb]);
     }
-    if (norb > 1 && s->ifixorb[iorb] == 0) ortho(s, iorb);
+    if (!rounds && norb > 1 && s->ifixorb[iorb] == 0) ortho(s, iorb);
     if (s->ifixorb[iorb] != 0) fock(s, iorb);
     // EaHF of iorb reads only iorb and its own Fock sums, which nothing
     // later in the iteration changes: deferred and batched unless an

@@ -202,6 +202,8 @@ std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf
   g.borb_mu.assign(nmu, 0);
   g.bpot_mu.assign(nmu, 0);
   g.f3_mu.assign(nmu, 0);
+  g.e_mu.assign(nmu, 0);
+  g.e_nu.assign(nni, 0);
   g.d_nu = g.veta2;
   g.diag = -14350.0 / (5040.0) * (1.0 / (g.hmu * g.hmu) + 1.0 / (g.hni * g.hni));
   std::vector<double> wjac1(mx), wjac2(mx);
@@ -217,10 +219,12 @@ std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf
     g.borb_mu[i] = w4;
     g.bpot_mu[i] = w5;
     g.f3_mu[i] = -2.0 / w2 + g.diag;
+    g.e_mu[i] = -w6;
     for (int j = 0; j < nni; j++) {
       int ij = i * nni + j;
       double w10 = g.veta1[j];
       g.e[ij] = (w10 < kPrecis) ? 0.0 : (-w6 - 1.0 / (w10 * w10));
+      if (i == 0) g.e_nu[j] = (w10 < kPrecis) ? 0.0 : 1.0 / (w10 * w10);
       double w7 = w2 - g.veta[j] * g.veta[j];
       g.f1[ij] = r * r * w7 / 2.0;
       g.f0[ij] = r * (g.vxi[i] * (z1 + z2) + g.veta[j] * (z2 - z1));
@@ -524,11 +528,18 @@ std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf
         g.cl_wa = std::max(1, (maxa + 31) / 32);
         g.cl_wb = std::max(1, (maxb + 31) / 32);
         g.cl_ws = std::max(1, (maxs + 31) / 32);
-        while (g.cl_wa + g.cl_wb + g.cl_ws > 24) {
-          if (g.cl_wa >= g.cl_wb && g.cl_wa >= g.cl_ws) --g.cl_wa;
-          else if (g.cl_wb >= g.cl_ws) --g.cl_wb;
-          else --g.cl_ws;
-        }
+        auto fit = [](int &a, int &b, int &c, int most) {
+          while (a + b + c > most) {
+            if (a >= b && a >= c) --a;
+            else if (b >= c) --b;
+            else --c;
+          }
+        };
+        g.cl_pa = g.cl_wa;
+        g.cl_pb = g.cl_wb;
+        g.cl_ps = g.cl_ws;
+        fit(g.cl_wa, g.cl_wb, g.cl_ws, 24);
+        fit(g.cl_pa, g.cl_pb, g.cl_ps, 16);
         g.cl_smem = smem;
         g.cl_tile0 = t0;
         g.cl_row0 = r0;

@@ -70,7 +70,9 @@ class Completed:
 
 def request_deck(template_deck, r, nnu, nmu, maxscf=3000):
     """The template's cards with bond length r, grid nnu x nmu (R_inf = 40),
-    MCSOR for orbitals and potentials and an energy threshold of 1e-12."""
+    MCSOR for orbitals and potentials, orbital-energy threshold 1e-11 and
+    norm threshold 1e-13 (at 1e-12 the heteronuclear FH and CO requests
+    hover at the threshold and leave by the reference's stagnation exit)."""
     out = []
     for ln in template_deck.splitlines():
         key = ln.strip().lower()
@@ -81,7 +83,7 @@ def request_deck(template_deck, r, nnu, nmu, maxscf=3000):
             ln = f"nuclei {f[1]} {f[2]} {r:.6f}"
         out.append(ln)
     out = ["title served"] + out
-    out += [f"grid {nnu} {nmu} 40.0", f"scf {maxscf} 0 12 14 1", "mcsor", "mcsor-ce", "stop"]
+    out += [f"grid {nnu} {nmu} 40.0", f"scf {maxscf} 0 11 13 1", "mcsor", "mcsor-ce", "stop"]
     return "\n".join(out) + "\n"
 
 
