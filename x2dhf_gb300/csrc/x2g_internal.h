@@ -195,6 +195,7 @@ struct x2g_ctx {
   int band_sm_smem = 0;         // shared memory per SM
   int f64_blocks = -1;          // co-resident blocks of the cooperative FP64 sweep on this device
   int sor_blocks = -1;          // co-resident blocks of the cooperative list-order SOR sweep
+  int ortho_blocks = -1;        // co-resident blocks of the one-launch orthonormalisation
   unsigned long long wait_limit_ns = x2g::kDefaultWaitLimitNs;  // device-side wait limit (x2g_set_wait_limit)
   // optional per-launch timing of the sweep kernels (CUDA events on stream)
   int profiling = 0;

@@ -1542,10 +1542,31 @@ __device__ void block_sum_store(double (&v)[K], double *partials) {
 // block order -- the same order on every run -- and
 // writes out[0..nout).  Returns true in that block.  No block waits for
 // another.
+// Sum of partial q of nblocks blocks' stores (K per block), in block order:
+// thread t adds blocks t, t + blockDim, ..., then a warp tree, then the warp
+// totals in warp order.  Every thread of the block gets the total.
+__device__ double sum_partials(const double *partials, int K, int q, int nblocks) {
+  __shared__ double sh[kThreads / 32];
+  __shared__ double tot;
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += __ldcg(partials + size_t(b) * K + q);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < kThreads / 32; ++i) t += sh[i];
+    tot = t;
+  }
+  __syncthreads();
+  const double r = tot;
+  __syncthreads();
+  return r;
+}
+
 template <int K>
 __device__ bool block_sum_finish(double (&v)[K], double *partials, double *out, int nout, unsigned *ticket) {
   __shared__ bool s_last;
-  __shared__ double sh[kThreads / 32];
   block_sum_store<K>(v, partials);
   __threadfence();
   __syncthreads();
@@ -1554,17 +1575,8 @@ __device__ bool block_sum_finish(double (&v)[K], double *partials, double *out, 
   if (!s_last) return false;
   __threadfence();
   for (int q = 0; q < nout; ++q) {
-    double s = 0.0;
-    for (int b = threadIdx.x; b < int(gridDim.x); b += blockDim.x) s += __ldcg(partials + size_t(b) * K + q);
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double t = 0.0;
-      for (int i = 0; i < kThreads / 32; ++i) t += sh[i];
-      out[q] = t;
-    }
-    __syncthreads();
+    const double t = sum_partials(partials, K, q, int(gridDim.x));
+    if (threadIdx.x == 0) out[q] = t;
   }
   if (threadIdx.x == 0) *ticket = 0u;
   return true;
@@ -1673,6 +1685,122 @@ __global__ void k_ortho_round(GridDev g, const __grid_constant__ OrthoRound R) {
     double v = I.psi[ij];
     for (int q = 0; q < I.n; ++q) v = A(M(-ovl[q], I.o[q][ij]), v);
     I.psi[ij] = M(ano, v);
+  }
+}
+
+// Every round of an iteration's orthonormalisation in one cooperative
+// launch: per round the norms, the scaling (and setCiOrb), the overlaps
+// with the partners and the Gram-Schmidt step of each of its orbitals,
+// separated by grid barriers.  Each block stores the same per-block partial
+// sums as k_norm_round / k_overlaps_round (same blocks, same points, same
+// order) and every block adds them up in the order of block_sum_finish, so
+// the results equal the per-round launches bit for bit.
+constexpr int kOrthoItems = 32, kOrthoRounds = 16;
+struct OrthoPlan {
+  OrthoItem it[kOrthoItems];
+  int round_off[kOrthoRounds + 1];
+  int nrounds;
+};
+
+__device__ void scale_item(const GridDev &g, const OrthoItem &I, double norm) {
+  const double zarea = D(1.0, sqrt(norm));
+  const int stride = gridDim.x * blockDim.x;
+  if (I.ihomo == 0) {
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += stride) {
+      const int mu = k / g.nni, nu = k - mu * g.nni;
+      const int ij = (mu + 4) * g.n8 + nu + 4;
+      I.psi[ij] = M(zarea, I.psi[ij]);
+    }
+    return;
+  }
+  const int n2 = g.nni / 2 + 1;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n2 * g.nmu; k += stride) {
+    const int mu = k / n2, ni = k - mu * n2;
+    const int row = (mu + 4) * g.n8 + 4;
+    if (ni < n2 - 1) {
+      const double v = M(zarea, I.psi[row + ni]);
+      I.psi[row + ni] = v;
+      I.psi[row + (g.nni - 1 - ni)] = (I.ihomo == 1) ? v : -v;
+    } else {
+      I.psi[row + ni] = (I.ihomo == 1) ? M(zarea, I.psi[row + ni]) : 0.0;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_orthonormalise(GridDev g, const __grid_constant__ OrthoPlan P,
+                                                             double *partials, BarrierDev bar) {
+  __shared__ double s_ovl[kMaxK];
+  const int nb = int(gridDim.x);
+  for (int r = 0; r < P.nrounds; ++r) {
+    const int i0 = P.round_off[r], i1 = P.round_off[r + 1];
+    bool partners = false;
+    for (int i = i0; i < i1; ++i) {
+      const OrthoItem &I = P.it[i];
+      partners = partners || I.n > 0;
+      double v[1] = {0.0};
+      for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+        const int mu = k / g.nni, nu = k - mu * g.nni;
+        const double p = I.psi[(mu + 4) * g.n8 + nu + 4];
+        v[0] += g.wgt2[k] * M(M(p, p), g.f4[k]);
+      }
+      block_sum_store<1>(v, partials + size_t(i - i0) * nb);
+      __syncthreads();
+    }
+    __threadfence();
+    if (!grid_barrier(bar, unsigned(nb))) return;
+    for (int i = i0; i < i1; ++i) {
+      const OrthoItem &I = P.it[i];
+      const double norm = sum_partials(partials + size_t(i - i0) * nb, 1, 0, nb);
+      if (blockIdx.x == 0 && threadIdx.x == 0) *I.norm_out = norm;
+      scale_item(g, I, norm);
+    }
+    if (!partners) {
+      __threadfence();
+      if (r + 1 < P.nrounds && !grid_barrier(bar, unsigned(nb))) return;
+      continue;
+    }
+    __threadfence();
+    if (!grid_barrier(bar, unsigned(nb))) return;
+    for (int i = i0; i < i1; ++i) {
+      const OrthoItem &I = P.it[i];
+      if (I.n == 0) continue;
+      double v[kMaxK];
+      for (int q = 0; q < kMaxK; ++q) v[q] = 0.0;
+      for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+        const int mu = k / g.nni, nu = k - mu * g.nni;
+        const int ij = (mu + 4) * g.n8 + nu + 4;
+        // values other blocks wrote in this launch: read through L2
+        const double p = __ldcg(I.psi + ij), w = g.wgt2[k], f4 = g.f4[k];
+        for (int q = 0; q < I.n; ++q) v[q] += w * M(M(p, __ldcg(I.o[q] + ij)), f4);
+      }
+      block_sum_store<kMaxK>(v, partials + size_t(i - i0) * nb * kMaxK);
+      __syncthreads();
+    }
+    __threadfence();
+    if (!grid_barrier(bar, unsigned(nb))) return;
+    for (int i = i0; i < i1; ++i) {
+      const OrthoItem &I = P.it[i];
+      if (I.n == 0) continue;
+      for (int q = 0; q < I.n; ++q) {
+        const double t = sum_partials(partials + size_t(i - i0) * nb * kMaxK, kMaxK, q, nb);
+        if (threadIdx.x == 0) s_ovl[q] = t;
+      }
+      __syncthreads();
+      if (blockIdx.x == 0 && threadIdx.x < I.n) I.ovl_out[threadIdx.x] = s_ovl[threadIdx.x];
+      double ano = 0.0;
+      for (int q = 0; q < I.n; ++q) ano = A(ano, M(s_ovl[q], s_ovl[q]));
+      ano = D(sqrt(A(1.0, ano)), S(1.0, M(ano, ano)));
+      for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+        const int mu = k / g.nni, nu = k - mu * g.nni;
+        const int ij = (mu + 4) * g.n8 + nu + 4;
+        double v = __ldcg(I.psi + ij);
+        for (int q = 0; q < I.n; ++q) v = A(M(-s_ovl[q], __ldcg(I.o[q] + ij)), v);
+        I.psi[ij] = M(ano, v);
+      }
+      __syncthreads();
+    }
+    __threadfence();
+    if (r + 1 < P.nrounds && !grid_barrier(bar, unsigned(nb))) return;
   }
 }
 
@@ -2468,6 +2596,53 @@ void launch_ortho_round(x2g_ctx *ctx, const GridDev &g, const OrthoOrbital *orbs
       ctx->launches += 2;
     }
   }
+}
+
+// every round in one cooperative launch; false: the plan does not fit it
+// (more orbitals or rounds than its table holds, or too few co-resident
+// blocks), the caller then launches round by round
+bool launch_orthonormalise(x2g_ctx *ctx, const GridDev &g, const OrthoOrbital *orbs, const int *round_off,
+                           int nrounds) {
+  const int n = round_off[nrounds];
+  if (n > kOrthoItems || nrounds > kOrthoRounds || nrounds < 1) return false;
+  const int nb = red_blocks(g);
+  if (ctx->ortho_blocks < 0) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k_orthonormalise, kThreads, 0) !=
+        cudaSuccess)
+      per_sm = 0;
+    (void)cudaGetLastError();
+    ctx->ortho_blocks = per_sm * ctx->num_sms;
+  }
+  if (nb > ctx->ortho_blocks) return false;
+  OrthoPlan P{};
+  for (int q = 0; q < n; ++q) {
+    const OrthoOrbital &x = orbs[q];
+    OrthoItem &I = P.it[q];
+    I.psi = x.psi;
+    I.n = x.n;
+    for (int k = 0; k < x.n; ++k) I.o[k] = x.partners[k];
+    I.ihomo = x.ihomo;
+    I.norm_out = x.norm_out;
+    I.ovl_out = x.ovl_out;
+  }
+  int most = 0;
+  for (int r = 0; r <= nrounds; ++r) P.round_off[r] = round_off[r];
+  for (int r = 0; r < nrounds; ++r) most = std::max(most, round_off[r + 1] - round_off[r]);
+  P.nrounds = nrounds;
+  double *part = reduction_partials(ctx, kMaxK * most);
+  if (!part) return false;
+  if (cudaMemsetAsync(ctx->bar, 0, 2 * sizeof(unsigned), ctx->stream) != cudaSuccess) return false;
+  BarrierDev bar{ctx->bar, ctx->bar + 1, reinterpret_cast<int *>(ctx->bar + 2), ctx->wait_limit_ns};
+  GridDev gd = g;
+  void *args[] = {&gd, &P, &part, &bar};
+  if (cudaLaunchCooperativeKernel((const void *)k_orthonormalise, dim3(nb), dim3(kThreads), args, 0, ctx->stream) !=
+      cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  ctx->launches += 1;
+  return true;
 }
 
 void launch_eahf(x2g_ctx *ctx, const GridDev &g, const double *psi, int isym, int m, const double *coulp,

@@ -113,6 +113,10 @@ struct OrthoOrbital {
   double *norm_out, *ovl_out;
 };
 void launch_ortho_round(x2g_ctx *ctx, const GridDev &g, const OrthoOrbital *orbs, int n);
+// all rounds in one cooperative launch (round r: orbs[round_off[r] ..
+// round_off[r+1])); false: not launched, take launch_ortho_round per round
+bool launch_orthonormalise(x2g_ctx *ctx, const GridDev &g, const OrthoOrbital *orbs, const int *round_off,
+                           int nrounds);
 // EaHF of several orbitals in one launch (same sums, same order as launch_eahf)
 struct EahfItem {
   const double *psi, *coulp, *exchp;

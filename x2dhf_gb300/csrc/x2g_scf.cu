@@ -496,8 +496,9 @@ std::vector<int> ortho_partners(x2g_scf *s, int iorb1) {
 // orbitals of its own symmetry, which the reference's loop has finished by
 // then, so an orbital's round is 1 + the latest round of its partners; the
 // orbitals of one round are independent and each goes through the same
-// operations as in the loop.  N2: 3 rounds instead of 6 orbitals.  false:
-// an orbital has more partners than one round item holds.
+// operations as in the loop.  N2: 3 rounds instead of 6 orbitals, all in
+// one cooperative launch.  false: an orbital has more partners than one
+// round item holds.
 bool orthonormalise_in_rounds(x2g_scf *s) {
   const int norb = s->norb;
   std::vector<int> depth(norb + 1, 0);
@@ -509,8 +510,9 @@ bool orthonormalise_in_rounds(x2g_scf *s) {
     for (int q : partners[iorb]) depth[iorb] = std::max(depth[iorb], depth[q] + 1);
     maxd = std::max(maxd, depth[iorb]);
   }
+  std::vector<OrthoOrbital> v;
+  std::vector<int> off(1, 0);
   for (int r = 0; r <= maxd; r++) {
-    std::vector<OrthoOrbital> v;
     for (int iorb = norb; iorb >= 1; iorb--) {
       if (depth[iorb] != r) continue;
       OrthoOrbital x{};
@@ -522,8 +524,11 @@ bool orthonormalise_in_rounds(x2g_scf *s) {
       x.ovl_out = s->sc + x2g_scf::O_OVL + 64 * iorb;
       v.push_back(x);
     }
-    launch_ortho_round(s->ctx, s->grid->d, v.data(), int(v.size()));
+    off.push_back(int(v.size()));
   }
+  // every round in one launch where the plan fits it, else round by round
+  if (!launch_orthonormalise(s->ctx, s->grid->d, v.data(), off.data(), maxd + 1))
+    for (int r = 0; r <= maxd; r++) launch_ortho_round(s->ctx, s->grid->d, v.data() + off[r], off[r + 1] - off[r]);
   return true;
 }
 
@@ -947,9 +952,8 @@ int scf_finish(x2g_scf *s) {
     for (int i = 1; i <= s->norb; i++) {
       int j = s->norb + 1 - i;
       double *keep = s->sc + x2g_scf::O_OVL + 64 * 50 + j;  // norm kept for the report
-      (void)keep;
-      launch_norm(s->ctx, s->grid->d, s->orb[j], s->sc + x2g_scf::O_OVL + 64 * 50 + j);
-      launch_scale(s->ctx, s->grid->d, s->orb[j], s->sc + x2g_scf::O_OVL + 64 * 50 + j);
+      launch_norm(s->ctx, s->grid->d, s->orb[j], keep);
+      launch_scale(s->ctx, s->grid->d, s->orb[j], keep);
       ortho(s, j);
     }
   }
