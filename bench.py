@@ -265,7 +265,22 @@ def max_over_ranks(values, world, device):
 ORACLE_SOLVES = {"n2": os.path.join(ROOT, "tests", "golden", "n2_331x481_oracle.json")}
 # SCF forms timed by the GPU arm: (name, precision, batch mode); the last is
 # the headline `value` (the benchmark spec's batched mixed form)
-SCF_LEGS = (("fp64", 0, 0), ("fp64_batched", 0, 2), ("mixed_reference_order", 1, 0), ("mixed", 1, 2))
+# (name, precision 0 FP64 / 1 mixed, batch mode, MCSOR sweeps per relaxation:
+# 0 the deck's own, else the mcsor card's maxsor for orbitals and potentials);
+# the last leg is the headline
+SCF_LEGS = (("fp64", 0, 0, 0), ("fp64_batched", 0, 2, 0), ("mixed_reference_order", 1, 0, 0),
+            ("mixed_sweeps40", 1, 2, 40), ("mixed", 1, 2, 0))
+# workloads that run the sweeps40 leg (a few-second full solve each)
+SWEEPS_LEG_WORKLOADS = ("n2", "h2")
+
+
+def deck_with_sweeps(deck, n):
+    """The deck with n MCSOR sweeps per orbital and potential relaxation (the
+    mcsor card's maxsor fields, inputInterface.F90:1910-2028); n = 0 keeps it."""
+    if not n:
+        return deck
+    out = [ln for ln in deck.splitlines() if not ln.strip().lower().startswith(("mcsor", "stop"))]
+    return "\n".join(out + [f"mcsor 0 {n} {n}", f"mcsor-ce 0 {n}", "stop"]) + "\n"
 
 
 def oracle_reference(name):
@@ -307,11 +322,12 @@ def run_gpu(args):
 
     copied = [0, 0, 0]  # host-to-device bytes, device-to-host bytes, timed e2e steps
 
-    def timed_solves(prec, mode, k, warm, e2e=False, cap=None, warm_cap=None):
+    def timed_solves(prec, mode, k, warm, e2e=False, cap=None, warm_cap=None, sweeps=0):
         lat, res_last, iters = [], None, []
+        leg_deck = deck_with_sweeps(deck, sweeps)
         for step in range(warm + k):
             if not e2e:
-                case = xg.parse_deck(deck, precision=prec, batch_mode=mode)
+                case = xg.parse_deck(leg_deck, precision=prec, batch_mode=mode)
                 scf = xg.SCF(ctx, case)  # initial guess uploaded: state resident in HBM
             flush_l2(torch, flush)
             barrier()
@@ -320,7 +336,7 @@ def run_gpu(args):
             b0 = ctx.transfer_bytes()
             ev0.record(stream)
             if e2e:
-                case = xg.parse_deck(deck, precision=prec, batch_mode=mode)
+                case = xg.parse_deck(leg_deck, precision=prec, batch_mode=mode)
                 scf = xg.SCF(ctx, case)
             res = scf.run(cap if cap else (fixed if step >= warm else
                                            warm_cap or WARMUP_ITERS.get(args.workload, fixed)))
@@ -343,31 +359,33 @@ def run_gpu(args):
             scf.close()
         return lat, res_last, iters
 
-    legs = [lg for lg in SCF_LEGS if args.legs == "all" or lg[0] == args.legs]
+    legs = [lg for lg in SCF_LEGS if (args.legs == "all" and (not lg[3] or args.workload in SWEEPS_LEG_WORKLOADS))
+            or lg[0] == args.legs]
     head = legs[-1]
     sampler = ClockSampler(local)
     lat, res, its = {}, {}, {}
     launches = 0
     ctx.profile(0, xg.FP64)  # the timed steps run without the library's per-launch events
     with sampler:
-        for name, prec, mode in legs:
+        for name, prec, mode, sweeps in legs:
             # the plain FP64 form is the slow comparator: a few timed solves
             k = args.steps if not name.startswith("fp64") or len(legs) == 1 else min(args.steps, args.fp64_steps)
             l0 = ctx.launches
             # the comparator's warm-up solves stop after 50 iterations (a full
             # plain-FP64 solve takes seconds and warms nothing more)
             lat[name], res[name], its[name] = timed_solves(prec, mode, k, args.warmup,
-                                                           warm_cap=50 if name.startswith("fp64") else None)
+                                                           warm_cap=50 if name.startswith("fp64") else None,
+                                                           sweeps=sweeps)
             if name == head[0]:
                 # launches of the timed headline solves (the warm-up ones counted out)
                 launches = int((ctx.launches - l0) * k / (k + args.warmup))
-        late2e, rese2e, _ = timed_solves(head[1], head[2], max(1, args.steps // 2), 1, e2e=True)
+        late2e, rese2e, _ = timed_solves(head[1], head[2], max(1, args.steps // 2), 1, e2e=True, sweeps=head[3])
     # roofline figures: one more step of each form with the library's
     # per-launch CUDA events on (recorded on its own stream), not timed; a
     # long full-solve workload profiles its first iterations only
     prof = {}
-    for name, prec, mode in legs:
-        if name == "mixed_reference_order":
+    for name, prec, mode, sweeps in legs:
+        if name in ("mixed_reference_order", "mixed_sweeps40"):
             continue
         ctx.profile(2, prec)
         timed_solves(prec, mode, 1, 0, cap=WARMUP_ITERS.get(args.workload))
@@ -416,7 +434,8 @@ def run_gpu(args):
         d = {"value": rate[n], "unit": unit, "iterations": its[n], "total_energy": r.total_energy,
              "orbital_energies": [r.ee[i] for i in range(c.norb)], "sweeps": r.sweeps,
              "latency_p50_s": statistics.median(lat[n]),
-             "batch_mode": dict((x[0], x[2]) for x in SCF_LEGS)[n]}
+             "batch_mode": dict((x[0], x[2]) for x in SCF_LEGS)[n],
+             "sweeps_per_relaxation": dict((x[0], x[3]) for x in SCF_LEGS)[n] or c.maxsor_orb}
         if fp64_e is not None and n != "fp64":
             d["dE_vs_fp64"] = abs(r.total_energy - fp64_e)
             d["max_dee_vs_fp64"] = max(abs(r.ee[i] - res["fp64"].ee[i]) for i in range(c.norb))
@@ -447,7 +466,9 @@ def run_gpu(args):
                              "launch (batch mode 2)" if head[2] == 2 else "the reference's relaxation order"),
                  "fp64": "plain form: FP64 MCSOR in the reference's colour order and relaxation order",
                  "fp64_batched": "plain form, FP64 MCSOR in the reference's colour order, batched like the "
-                                 "headline (batch mode 2): the comparator with the same launch shape"},
+                                 "headline (batch mode 2): the comparator with the same launch shape",
+                 "mixed_sweeps40": "the headline form with 40 MCSOR sweeps per relaxation instead of the deck's "
+                                   "10 (the mcsor card's maxsor): fewer SCF iterations, same fixed point"},
         "latency_s": {"p50": statistics.median(lat[head[0]]), "p99": p99},
         "e2e": {"value": e2e_value, "unit": unit, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
@@ -472,6 +493,7 @@ def run_gpu(args):
             "point_updates_per_launch": pts_per_launch,
             "clusters_co_resident": {"plain": occ[0], "potentials_variant": occ[1],
                                      "potentials_variant_mode": args.potential_clusters},
+            "colouring": args.colouring,
             "fp64_kernel": {"kernel": "k_mcsor_f64", "achieved_gbs": sweep_gbs_64,
                             "frac_hbm": (sweep_gbs_64 / hbm) if sweep_gbs_64 else None,
                             "achieved_tflops": pts64 * FLOPS_PER_PT / (ms64 / 1e3) / 1e12 if ms64 > 0 else None,
@@ -867,11 +889,12 @@ def run_window(args):
     from x2dhf_gb300 import build
 
     warm, n = (int(x) for x in args.window.split(","))
-    name, prec, mode = [lg for lg in SCF_LEGS if args.legs == "all" or lg[0] == args.legs][-1]
+    name, prec, mode, sweeps = [lg for lg in SCF_LEGS if args.legs == "all" or lg[0] == args.legs][-1]
     build.build()
     ctx = xg.Context(0)
     _configure(ctx, args)
-    s = xg.SCF(ctx, xg.parse_deck(WORKLOADS[args.workload](), precision=prec, batch_mode=mode))
+    s = xg.SCF(ctx, xg.parse_deck(deck_with_sweeps(WORKLOADS[args.workload](), sweeps), precision=prec,
+                                  batch_mode=mode))
     s.run(warm)
     ctx.synchronize()
     l0 = ctx.launches
@@ -888,6 +911,7 @@ def _configure(ctx, args):
     """Context options the command line sets."""
     mode = getattr(args, "potential_clusters", "auto")
     ctx.set_potential_clusters("auto" if mode == "auto" else mode == "on")
+    ctx.set_mixed_colouring(getattr(args, "colouring", "reference"))
 
 
 def main():
@@ -914,6 +938,8 @@ def main():
     ap.add_argument("--potential-clusters", default="auto", choices=["auto", "on", "off"],
                     help="mixed form: cluster sweep of potential batches at two CTAs per SM "
                          "(default: for batches above the plain kernel's co-resident clusters)")
+    ap.add_argument("--colouring", default="reference", choices=["reference", "free"],
+                    help="mixed form: colouring of the on-chip cluster sweep")
     ap.add_argument("--window", default="", help="WARM,N: profile SCF iterations WARM+1..WARM+N of the headline form "
                                                  "inside a CUDA profiler range (no bench line)")
     args = ap.parse_args()

@@ -121,6 +121,9 @@ int x2g_host_cluster_plan(int nnu, int nmu, int *csize, int *maxrows, long *smem
  * off the shared band edges, level 0 near them, level-0 seam points, levels
  * 1..), plus the end.  Null arrays: counts only. */
 int x2g_host_cluster_chunks(int nnu, int nmu, int *nchunks, int *noff, int *chunks, int *off);
+/* The same for the seam-free colouring (x2g_set_mixed_colouring 1): per CTA
+ * and colour the segments A, B and an empty seam segment. */
+int x2g_host_free_chunks(int nnu, int nmu, int *nchunks, int *noff, int *chunks, int *off);
 /* Schedule of the persistent-band FP32 sweep (host only): the scheduled
  * points regrouped by colour, level and tile, packed (ext row << 16) | ext
  * col (pts, npoints values); off[(c * nlevels + l) * (ntiles + 1) + t] is
@@ -161,6 +164,15 @@ int x2g_set_mixed_on_chip(x2g_ctx *ctx, int on);
  * mode 0 never, 1 always, 2 (default) for batches larger than the clusters
  * of the plain kernel co-resident on the device.  No reference counterpart. */
 int x2g_set_potential_clusters(x2g_ctx *ctx, int mode);
+/* Colouring of the mixed form's on-chip cluster sweep: 0 the reference's
+ * (colour = position in the "middle" list mod 5, sormcsor.F90:143-386, with
+ * its seam points relaxed level by level, so that in exact arithmetic the
+ * sweep equals the FP64 one), 1 seam-free (colour (col - row) mod 5 of the
+ * extended-array point: no two points of a colour are stencil neighbours, so
+ * every colour is one parallel step).  Both converge to the same fixed point;
+ * the persistent-band sweep of large grids keeps the reference's colouring.
+ * No reference counterpart. */
+int x2g_set_mixed_colouring(x2g_ctx *ctx, int free);
 /* Co-resident clusters of the mixed form's cluster sweep (plain) and of its
  * potentials' variant (pot) for this grid on the context's device; 0 where
  * that kernel cannot run the grid.  No reference counterpart. */

@@ -1054,10 +1054,20 @@ void x2o_sweep(const x2o_state *s, int mode, int isym, int maxsor2, double omega
         for (int i = isstart; i >= isstop; i += isstep)
           relax_point(s, fun, s->indx1[i - 1] - 1, s->indx2[i - 1] - 1, lhs, rhs, b, d, omega, omega1);
       }
-    } else {
+    } else if (mode == 1) {
       for (int c = 1; c <= 5; c++)
         for (int i = c; i <= s->ngrid1; i += 5)
           relax_point(s, fun, s->indx1[i - 1] - 1, s->indx2[i - 1] - 1, lhs, rhs, b, d, omega, omega1);
+    } else {
+      /* Not a reference ordering: the GPU mixed form's seam-free colouring,
+       * colour (col - row) mod 5 of the extended-array point, the colours in
+       * turn (its points are independent; taken in list order) */
+      for (int c = 0; c < 5; c++)
+        for (int i = 1; i <= s->ngrid1; i++) {
+          const int ij = s->indx1[i - 1] - 1, row = ij / s->nni8, col = ij % s->nni8;
+          if (((col - row) % 5 + 5) % 5 != c) continue;
+          relax_point(s, fun, ij, s->indx2[i - 1] - 1, lhs, rhs, b, d, omega, omega1);
+        }
     }
     sweep_boundary(s, isym, fun);
   }

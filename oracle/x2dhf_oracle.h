@@ -92,7 +92,10 @@ void x2o_putout(int nni, int nmu, double *fun, const double *work);
 /* One relaxation call of maxsor2 micro-sweeps on an extended array.
  * mode 0: sor in list order (src/sormcsor.F90:20-132)
  * mode 1: single-thread mcsor, colour classes i = c (mod 5) of the list
- *         (src/sormcsor.F90:143-386). */
+ *         (src/sormcsor.F90:143-386)
+ * mode 2: not a reference ordering -- the checker of the GPU mixed form's
+ *         seam-free colouring: colour (col - row) mod 5 of the extended-array
+ *         point, colours in turn, then the axis extrapolation as above. */
 void x2o_sweep(const x2o_state *s, int mode, int isym, int maxsor2, double omega,
                double *uext, const double *lhs, const double *rhs,
                const double *b, const double *d, int isstart, int isstop, int isstep);

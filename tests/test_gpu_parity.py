@@ -206,6 +206,57 @@ def test_potential_cluster_variant_tracks_fp64(ctx, name):
         assert np.abs(b - e).max() <= 1e-5 * change + 1e-14, (k, s[2], np.abs(b - e).max() / change)
 
 
+@pytest.mark.parametrize("variant", [False, True])
+def test_free_colouring_tracks_oracle_sweep(ctx, variant):
+    """The seam-free colouring of the mixed form's cluster sweep, plain kernel
+    and potentials' variant, against the oracle's FP64 sweep in the same
+    colouring (mode 2): every potential of Ne (idel 0, 1 and 2), one launch,
+    within FP32 rounding of the change; a start from one FP64 sweep (axis
+    consistent with the interior), the nu x mu points compared."""
+    torch = pytest.importorskip("torch")
+    deck = golden_deck("ne_set01")
+    oc = Case(deck)
+    c, g = _grid(ctx, deck)
+    dev = torch.device("cuda:0")
+    orbs = {i: torch.tensor(oc.putin(1 if c.m[i - 1] % 2 == 0 else -1, oc.orbital(i)), device=dev)
+            for i in range(1, oc.norb + 1)}
+    omega = oc.omega()[1]
+    e, f3, gg = oc.suppl(3), oc.suppl(7), oc.suppl(9)
+    specs, starts, refs = [], [], []
+    for iorb in range(1, oc.norb + 1):
+        for k in range(1, oc.npots(iorb) + 1):
+            in1, in2, idel, isym = oc.pot_info(iorb, k)
+            rhs = (oc.orbital(in1) * oc.orbital(in2)) * gg
+            lhs = f3.copy() if idel == 0 else f3 + float(idel * idel) * e
+            u1 = oc.sweep(1, isym, 1, omega, oc.putin(isym, oc.pot(iorb, k)), lhs, rhs, oc.suppl(1), oc.suppl(2))
+            # ghosts refreshed from the swept interior, as every relaxation starts
+            u1 = oc.putin(isym, u1.reshape(c.nmu + 8, c.nnu + 8)[4:c.nmu + 4, 4:c.nnu + 4].ravel())
+            specs.append((in1, in2, idel, isym))
+            starts.append(u1)
+            refs.append(oc.sweep(2, isym, 10, omega, u1, lhs, rhs, oc.suppl(1), oc.suppl(2)))
+    bufs = [torch.tensor(x, device=dev) for x in starts]
+    jobs = [xg.Job(u=u.data_ptr(), psa=orbs[a].data_ptr(), psb=orbs[b].data_ptr(), omega=omega, isym=sy, idel=d,
+                   kind=1) for u, (a, b, d, sy) in zip(bufs, specs)]
+    ctx.set_mixed_colouring("free")
+    ctx.set_potential_clusters(variant)
+    torch.cuda.synchronize()
+    try:
+        xg.relax(ctx, g, jobs, 10, xg.MIXED)
+        ctx.synchronize()
+    finally:
+        ctx.set_mixed_colouring("reference")
+        ctx.set_potential_clusters("auto")
+
+    def part(x):
+        return x.reshape(c.nmu + 8, c.nnu + 8)[4:c.nmu + 4, 4:c.nnu + 4]
+
+    for k, (u, ref, u0, sp) in enumerate(zip(bufs, refs, starts, specs)):
+        got, exp, st = part(u.cpu().numpy()), part(ref), part(u0)
+        change = np.abs(exp - st).max()
+        assert change > 0
+        assert np.abs(got - exp).max() <= 1e-5 * change + 1e-14, (k, sp[2], np.abs(got - exp).max() / change)
+
+
 def _scf_records_match(name, niter, transform=None, tol=1e-11, batch_mode=0):
     deck = golden_deck(name)
     if transform:

@@ -87,6 +87,43 @@ def test_cluster_plan_bands(nnu, nmu):
         assert np.unique(band[tile == t]).size == 1
 
 
+@pytest.mark.parametrize("nnu,nmu", [(31, 31), (91, 121), (151, 241), (331, 481)])
+def test_free_colouring_chunks_cover_grid(nnu, nmu):
+    """The seam-free plan of the mixed form's cluster sweep: every interior
+    point exactly once, in its CTA's band, in the segment of its colour
+    (col - row) mod 5 and kind (off the shared band edges, within 4 rows of
+    one; the seam segment empty), chunks of up to 4 points of one row at
+    stride 5; no two points of one colour are neighbours on the stencil's
+    cross, so each colour is one parallel step."""
+    C, maxrows, smem, row0 = xg.host_cluster_plan(nnu, nmu)
+    ch, off = xg.host_cluster_chunks(nnu, nmu, colouring="free")
+    S = 3
+    assert off.size == C * 5 * S + 1 and off[-1] == ch.size
+    n8 = nnu + 8
+    seen = {}
+    for k in range(C):
+        for c in range(5):
+            assert off[(k * 5 + c) * S + 2] == off[(k * 5 + c) * S + 3]
+            for seg in range(2):
+                o = (k * 5 + c) * S + seg
+                for q in ch[off[o]:off[o + 1]]:
+                    lr, cl, n = int(q >> 19), int((q >> 2) & 0x1FFFF), int(q & 3) + 1
+                    row = row0[k] + lr
+                    assert row0[k] <= row < row0[k + 1]
+                    edge = (k > 0 and row < row0[k] + 4) or (k < C - 1 and row >= row0[k + 1] - 4)
+                    assert edge == (seg == 1)
+                    for j in range(n):
+                        col = cl + 5 * j
+                        assert (col - row) % 5 == c and (row, col) not in seen
+                        seen[(row, col)] = c
+    interior = {(r, q) for r in range(5, nmu) for q in range(5, nnu + 3)}
+    assert set(seen) == interior
+    for (r, q), c in seen.items():
+        for d in range(1, 5):
+            for nb in ((r + d, q), (r, q + d)):
+                assert seen.get(nb, -1) != c
+
+
 def test_large_grid_has_no_cluster_plan():
     assert xg.host_cluster_plan(781, 1201)[0] == 0
 

@@ -75,7 +75,8 @@ EXPORTS = [
     "x2g_kernel_launches", "x2g_transfer_bytes", "mcsor_pthread_", "mcsor_tpool_", "coulExch_pthread_", "coulExch_tpool_",
     "tpoolStop4mcsor_", "tpoolStop4pots_", "x2g_host_table", "x2g_host_schedule", "x2g_profile",
     "x2g_relax_noalloc", "x2g_host_cluster_plan", "x2g_set_mixed_on_chip", "x2g_set_potential_clusters", "x2g_cluster_occupancy",
-    "x2g_host_cluster_chunks", "x2g_host_band_schedule",
+    "x2g_set_mixed_colouring",
+    "x2g_host_cluster_chunks", "x2g_host_free_chunks", "x2g_host_band_schedule",
     "x2g_convert_selftest", "x2g_set_wait_limit", "x2g_host_sor_schedule",
 ]
 
@@ -136,6 +137,7 @@ def lib():
                                         C.POINTER(C.c_int)]
     L.x2g_set_mixed_on_chip.argtypes = [P, I]
     L.x2g_set_potential_clusters.argtypes = [P, I]
+    L.x2g_set_mixed_colouring.argtypes = [P, I]
     L.x2g_cluster_occupancy.argtypes = [P, P, C.POINTER(I), C.POINTER(I)]
     L.x2g_set_wait_limit.argtypes = [P, D]
     L.x2g_kernel_launches.restype = C.c_long
@@ -376,15 +378,17 @@ def host_sor_schedule(nnu, nmu):
     return pts, off, bpts, boff, d.value
 
 
-def host_cluster_chunks(nnu, nmu):
-    """(packed chunks, segment offsets) of the on-chip sweep (no GPU needed)."""
+def host_cluster_chunks(nnu, nmu, colouring="reference"):
+    """(packed chunks, segment offsets) of the on-chip sweep (no GPU needed);
+    colouring "free": the seam-free colouring's plan."""
     L = lib()
+    f = L.x2g_host_free_chunks if colouring == "free" else L.x2g_host_cluster_chunks
     nc, no = C.c_int(), C.c_int()
-    _check(L.x2g_host_cluster_chunks(nnu, nmu, C.byref(nc), C.byref(no), None, None))
+    _check(f(nnu, nmu, C.byref(nc), C.byref(no), None, None))
     ch = np.zeros(nc.value, np.int32)
     off = np.zeros(no.value, np.int32)
-    _check(L.x2g_host_cluster_chunks(nnu, nmu, C.byref(nc), C.byref(no),
-                                     ch.ctypes.data_as(C.POINTER(C.c_int)), off.ctypes.data_as(C.POINTER(C.c_int))))
+    _check(f(nnu, nmu, C.byref(nc), C.byref(no), ch.ctypes.data_as(C.POINTER(C.c_int)),
+             off.ctypes.data_as(C.POINTER(C.c_int))))
     return ch.view(np.uint32), off
 
 
@@ -438,6 +442,14 @@ class Context:
         False the plain kernel, "auto" the variant for batches above the
         plain kernel's co-resident clusters."""
         _check(self.L.x2g_set_potential_clusters(self.h, 2 if mode == "auto" else (1 if mode else 0)))
+
+    def set_mixed_colouring(self, colouring):
+        """Colouring of the mixed form's cluster sweep: "reference" (the
+        reference's list order mod 5, seams level by level) or "free"
+        (colour (col - row) mod 5, no seams)."""
+        if colouring not in ("reference", "free"):
+            raise ValueError("colouring must be 'reference' or 'free'")
+        _check(self.L.x2g_set_mixed_colouring(self.h, 1 if colouring == "free" else 0))
 
     def convert_selftest(self, n, seed=1):
         """Mismatches of the integer-pipe FP64<->FP32 conversions against the hardware ones."""

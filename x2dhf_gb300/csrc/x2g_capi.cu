@@ -194,6 +194,12 @@ int x2g_set_potential_clusters(x2g_ctx *c, int mode) {
   return X2G_OK;
 }
 
+int x2g_set_mixed_colouring(x2g_ctx *c, int free) {
+  if (!c || free < 0 || free > 1) return set_status(X2G_ERR_ARG, "colouring must be 0 or 1");
+  c->mixed_free = free;
+  return X2G_OK;
+}
+
 int x2g_round_grid(int n) {
   // nnucalc/nmucalc (inputInterface.F90:2961-3095): n = 1 (mod 6) and
   // n - 6 = 0 (mod 5) enforced alternately, always rounding down.
@@ -340,6 +346,13 @@ int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, doubl
   d.cl_wb = h.cl_wb;
   d.cl_ws = h.cl_ws;
   d.cl_pa = h.cl_pa;
+  d.cf_maxchunks = h.cf_maxchunks;
+  d.cf_wa = h.cf_wa;
+  d.cf_wb = h.cf_wb;
+  d.cf_ws = h.cf_ws;
+  d.cf_pa = h.cf_pa;
+  d.cf_pb = h.cf_pb;
+  d.cf_ps = h.cf_ps;
   d.cl_pb = h.cl_pb;
   d.cl_ps = h.cl_ps;
   if (h.cl_size > 0) {
@@ -347,8 +360,10 @@ int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, doubl
     UP(h.cl_row0, cl_row0);
     UP(h.cl_pts, cl_pts);
     UP(h.cl_off, cl_off);
+    UP(h.cf_pts, cf_pts);
+    UP(h.cf_off, cf_off);
   } else {
-    d.cl_tile0 = d.cl_row0 = d.cl_pts = d.cl_off = nullptr;
+    d.cl_tile0 = d.cl_row0 = d.cl_pts = d.cl_off = d.cf_pts = d.cf_off = nullptr;
   }
   UP(b32, borb_mu32);
   UP(p32, bpot_mu32);

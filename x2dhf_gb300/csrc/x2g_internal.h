@@ -55,6 +55,13 @@ struct HostGrid {
   int cl_size = 0, cl_maxrows = 0, cl_maxchunks = 0, cl_wa = 1, cl_wb = 1, cl_ws = 1;
   // warps per role of the potentials' variant (two CTAs per SM, 16 warps)
   int cl_pa = 1, cl_pb = 1, cl_ps = 1;
+  // the same CTA bands with the seam-free colouring of the mixed form,
+  // colour (col - row) mod 5 in ext coordinates (no two points of a colour
+  // within 4 rows or columns of each other on the stencil's cross): per
+  // (CTA, colour) the segments A (off the shared band edges), B (within 4
+  // rows of one) and an empty seam segment, chunks packed as in cl_pts
+  int cf_maxchunks = 0, cf_wa = 1, cf_wb = 1, cf_ws = 0, cf_pa = 1, cf_pb = 1, cf_ps = 0;
+  std::vector<int> cf_pts, cf_off;
   size_t cl_smem = 0;
   std::vector<int> cl_tile0, cl_row0;
   // the CTAs' points regrouped [cta][colour][segment] as chunks of up to 4
@@ -102,6 +109,8 @@ struct GridDev {
   const double *vxi, *vxisq, *veta, *vetasq;
   const int *tile_row0, *tile_row1, *pts, *off, *pts_rc;
   int cl_size, cl_maxrows, cl_maxchunks, cl_wa, cl_wb, cl_ws, cl_pa, cl_pb, cl_ps;
+  int cf_maxchunks, cf_wa, cf_wb, cf_ws, cf_pa, cf_pb, cf_ps;
+  const int *cf_pts, *cf_off;
   const int *cl_tile0, *cl_row0, *cl_pts, *cl_off;
   const int *st_pts, *st_off;
   int st_rows[17];
@@ -184,6 +193,7 @@ struct x2g_ctx {
   int no_cluster = 0;           // 1: mixed form uses the persistent-band FP32 kernel
   int auto_band = 0;            // 1: batches beyond the co-resident clusters take the persistent-band kernel
   int pot_clusters = 2;         // potentials' cluster variant: 0 never, 1 always, 2 batches above cluster_active[0]
+  int mixed_free = 0;           // cluster sweep colouring: 0 the reference's list order mod 5, 1 seam-free
   // [0] the cluster kernel, [1] its potentials' variant:
   int cluster_active[2] = {0, 0};       // clusters co-resident on the device (last shape checked)
   long cluster_checked_key[2] = {-1, -1};  // (shared bytes, cluster size, warps) last checked

@@ -730,11 +730,14 @@ __device__ void smem_boundary(const GridDev &g, float *E, int R0, int R1, int ra
 // k_mixed_cluster_pot (potentials, lhs = f3(mu) + idel^2 (e_mu(mu) -
 // e_nu(nu))) keeps the residual alone and the lhs as a row term of the
 // band's rows and a column term by ext column, after d(nu).
-size_t cluster_smem_bytes(const GridDev &g, bool sep) {
+// free: the seam-free colouring's plan (one level, cf_*), else the
+// reference colouring's (cl_*)
+size_t cluster_smem_bytes(const GridDev &g, bool sep, bool free) {
   const size_t band = size_t(g.cl_maxrows) * g.n8 * sizeof(float);
+  const int S = (free ? 1 : g.nlev) + 2, chunks = free ? g.cf_maxchunks : g.cl_maxchunks;
   return (sep ? band : 2 * band) + size_t(g.cl_maxrows + 8) * g.n8 * sizeof(float) +
-         size_t(g.cl_maxrows + g.n8) * sizeof(float) * (sep ? 2 : 1) + size_t(5 * (g.nlev + 2) + 1) * sizeof(int) +
-         size_t(g.cl_maxchunks) * sizeof(int);
+         size_t(g.cl_maxrows + g.n8) * sizeof(float) * (sep ? 2 : 1) + size_t(5 * S + 1) * sizeof(int) +
+         size_t(chunks) * sizeof(int);
 }
 constexpr int kClusterPotThreads = 512;  // potentials' variant: 16 warps, two CTAs per SM
 
@@ -862,7 +865,7 @@ __device__ __forceinline__ void seam_barrier(int nthreads) {
 }
 
 template <bool kSep>
-__device__ __forceinline__ void mixed_cluster_body(const GridDev &g, const JobTable &jobs, int nsweeps) {
+__device__ __forceinline__ void mixed_cluster_body(const GridDev &g, const JobTable &jobs, int nsweeps, int free) {
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
   const int C = int(cl.num_blocks()), rank = int(cl.block_rank());
@@ -871,9 +874,10 @@ __device__ __forceinline__ void mixed_cluster_body(const GridDev &g, const JobTa
   const bool even = (J.isym == 1);
   const float *const bt = (J.kind >= 1) ? g.bpot_mu32 : g.borb_mu32;
   extern __shared__ float2 smem2[];
-  const int n8 = g.n8, nni = g.nni, nlev = g.nlev, S = nlev + 2;
+  const int n8 = g.n8, nni = g.nni, nlev = free ? 1 : g.nlev, S = nlev + 2;
   const int R0 = g.cl_row0[rank], R1 = g.cl_row0[rank + 1];
   const int nloc = (g.cl_maxrows + 8) * n8;
+  const int *const plan_off = free ? g.cf_off : g.cl_off, *const plan_pts = free ? g.cf_pts : g.cl_pts;
   float2 *const RW = smem2;
   float *const RR = reinterpret_cast<float *>(smem2);
   float *const E = kSep ? RR + g.cl_maxrows * n8 : reinterpret_cast<float *>(RW + g.cl_maxrows * n8);
@@ -883,7 +887,7 @@ __device__ __forceinline__ void mixed_cluster_body(const GridDev &g, const JobTa
   float *const LQ = LP + g.cl_maxrows;         // kSep only
   int *const SO = reinterpret_cast<int *>(kSep ? LQ + n8 : DN + n8);  // segment offsets into PL
   unsigned *const PL = reinterpret_cast<unsigned *>(SO + 5 * S + 1);
-  const int *const coff = g.cl_off + size_t(rank) * 5 * S;
+  const int *const coff = plan_off + size_t(rank) * 5 * S;
   const int pbase = coff[0], npl = coff[5 * S] - pbase;
   for (int k = threadIdx.x; k <= 5 * S; k += blockDim.x) SO[k] = coff[k] - pbase;
   for (int k = threadIdx.x; k < nloc; k += blockDim.x) E[k] = 0.0f;
@@ -899,7 +903,7 @@ __device__ __forceinline__ void mixed_cluster_body(const GridDev &g, const JobTa
     for (int k = threadIdx.x; k < n8; k += blockDim.x)
       LQ[k] = (k >= 4 && k < nni + 4) ? narrow_f64(J.idel2 * g.e_nu[k - 4]) : 0.0f;
   }
-  for (int k = threadIdx.x; k < npl; k += blockDim.x) PL[k] = unsigned(g.cl_pts[pbase + k]);
+  for (int k = threadIdx.x; k < npl; k += blockDim.x) PL[k] = unsigned(plan_pts[pbase + k]);
   const int ra = (R0 < 5) ? 5 : R0, ncols = nni - 2, nband = (R1 - ra) * ncols;
   {
     // four points per thread in flight: all loads before the stores
@@ -953,7 +957,9 @@ __device__ __forceinline__ void mixed_cluster_body(const GridDev &g, const JobTa
   B.up = (rank > 0) ? cl.map_shared_rank(E, rank - 1) + (R0 - g.cl_row0[rank - 1]) * n8 : nullptr;
   B.dn = (rank < C - 1) ? cl.map_shared_rank(E, rank + 1) + (R0 - R1) * n8 : nullptr;
   // warp roles: interior, edge, seam
-  const int wa = kSep ? g.cl_pa : g.cl_wa, wb = kSep ? g.cl_pb : g.cl_wb, ws = kSep ? g.cl_ps : g.cl_ws;
+  const int wa = free ? (kSep ? g.cf_pa : g.cf_wa) : (kSep ? g.cl_pa : g.cl_wa);
+  const int wb = free ? (kSep ? g.cf_pb : g.cf_wb) : (kSep ? g.cl_pb : g.cl_wb);
+  const int ws = free ? (kSep ? g.cf_ps : g.cf_ws) : (kSep ? g.cl_ps : g.cl_ws);
   const int warp = threadIdx.x >> 5;
   const int role = (warp < wa) ? 0 : (warp < wa + wb) ? 1 : 2;
   const int rbase = (role == 0) ? 0 : (role == 1) ? wa : wa + wb;
@@ -1036,16 +1042,16 @@ __device__ __forceinline__ void mixed_cluster_body(const GridDev &g, const JobTa
 }
 
 __global__ void __launch_bounds__(kClusterMaxThreads, 1) k_mixed_cluster(GridDev g, const __grid_constant__ JobTable jobs,
-                                                                        int nsweeps) {
-  mixed_cluster_body<false>(g, jobs, nsweeps);
+                                                                        int nsweeps, int free) {
+  mixed_cluster_body<false>(g, jobs, nsweeps, free);
 }
 
 // Potentials only (job kind 1): two CTAs per SM, so that twice the clusters
 // are co-resident for the batches of an SCF iteration's potentials
 __global__ void __launch_bounds__(kClusterPotThreads, 2) k_mixed_cluster_pot(GridDev g,
                                                                             const __grid_constant__ JobTable jobs,
-                                                                            int nsweeps) {
-  mixed_cluster_body<true>(g, jobs, nsweeps);
+                                                                            int nsweeps, int free) {
+  mixed_cluster_body<true>(g, jobs, nsweeps, free);
 }
 
 // ----------------------------------------------------------------------
@@ -2064,8 +2070,10 @@ static bool cluster_attributes(x2g_ctx *ctx) {
   return true;
 }
 
-// block size of the cluster sweep (pot: the potentials' variant)
-static int cluster_threads(const GridDev &g, bool pot) {
+// block size of the cluster sweep (pot: the potentials' variant; free: the
+// seam-free colouring's plan)
+static int cluster_threads(const GridDev &g, bool pot, bool free) {
+  if (free) return 32 * (pot ? g.cf_pa + g.cf_pb + g.cf_ps : g.cf_wa + g.cf_wb + g.cf_ws);
   return 32 * (pot ? g.cl_pa + g.cl_pb + g.cl_ps : g.cl_wa + g.cl_wb + g.cl_ws);
 }
 
@@ -2074,8 +2082,9 @@ static int cluster_threads(const GridDev &g, bool pot) {
 // per shape: shared memory per CTA, cluster size, block size)
 static bool cluster_usable(x2g_ctx *ctx, const GridDev &g, bool pot = false) {
   if (g.cl_size < 2 || ctx->no_cluster) return false;
-  const size_t smem = cluster_smem_bytes(g, pot);
-  const long key = (long(smem) * 64 + g.cl_size) * 32 + cluster_threads(g, pot) / 32;
+  const bool free = ctx->mixed_free != 0;
+  const size_t smem = cluster_smem_bytes(g, pot, free);
+  const long key = (long(smem) * 64 + g.cl_size) * 32 + cluster_threads(g, pot, free) / 32;
   const int v = pot ? 1 : 0;
   if (ctx->cluster_checked_key[v] != key) {
     ctx->cluster_checked_key[v] = key;
@@ -2084,7 +2093,7 @@ static bool cluster_usable(x2g_ctx *ctx, const GridDev &g, bool pot = false) {
     if (attr_ok) {
       cudaLaunchConfig_t q = {};
       q.gridDim = dim3(unsigned(g.cl_size));
-      q.blockDim = dim3(unsigned(cluster_threads(g, pot)));
+      q.blockDim = dim3(unsigned(cluster_threads(g, pot, free)));
       q.dynamicSmemBytes = smem;
       cudaLaunchAttribute qa[1];
       qa[0].id = cudaLaunchAttributeClusterDimension;
@@ -2193,12 +2202,13 @@ static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, 
     cudaEventRecord(pe.a, ctx->stream);
   }
   if (on_chip) {
-    const size_t smem = cluster_smem_bytes(g, pot);
+    const int free = ctx->mixed_free;
+    const size_t smem = cluster_smem_bytes(g, pot, free != 0);
     if (!cluster_attributes(ctx) || smem > ctx->cluster_smem_set)
       return set_status(X2G_ERR_CUDA, "cluster kernel attributes could not be set");
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(unsigned(njobs * g.cl_size));
-    cfg.blockDim = dim3(unsigned(cluster_threads(g, pot)));
+    cfg.blockDim = dim3(unsigned(cluster_threads(g, pot, free != 0)));
     cfg.dynamicSmemBytes = smem;
     cfg.stream = ctx->stream;
     cudaLaunchAttribute attr[1];
@@ -2209,8 +2219,8 @@ static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, 
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     GridDev gd = g;
-    err = pot ? cudaLaunchKernelEx(&cfg, k_mixed_cluster_pot, gd, jt, nsweeps)
-              : cudaLaunchKernelEx(&cfg, k_mixed_cluster, gd, jt, nsweeps);
+    err = pot ? cudaLaunchKernelEx(&cfg, k_mixed_cluster_pot, gd, jt, nsweeps, free)
+              : cudaLaunchKernelEx(&cfg, k_mixed_cluster, gd, jt, nsweeps, free);
     if (err != cudaSuccess) return cuda_status(err, "cluster MCSOR launch");
     ctx->launches += 1;
     if (ctx->profiling) {

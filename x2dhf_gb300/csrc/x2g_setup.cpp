@@ -143,6 +143,82 @@ std::string build_sor_schedule(HostGrid &g, const std::vector<int> &pos, const i
 
 }  // namespace
 
+// Chunks of one segment appended to `chunks`: the segment's points (ext
+// row, col) of one CTA band starting at ext row r0 grouped into runs of up to
+// 4 points of one row at stride 5, packed (band row << 19) | (col << 2) |
+// (count - 1), and dealt round-robin over buckets of the shared-memory bank
+// of their first correction value, so that a warp's 32 chunks start on
+// distinct banks where the buckets allow.
+static void append_chunks(std::vector<std::pair<int, int>> &pts, int r0, int n8, std::vector<int> &chunks) {
+  std::sort(pts.begin(), pts.end());
+  std::vector<std::vector<int>> bank(32);
+  for (size_t i = 0; i < pts.size();) {
+    size_t n = 1;
+    while (n < 4 && i + n < pts.size() && pts[i + n].first == pts[i].first &&
+           pts[i + n].second == pts[i + n - 1].second + 5)
+      ++n;
+    const int lr = pts[i].first - r0;
+    bank[((lr + 4) * n8 + pts[i].second) % 32].push_back(
+        int((unsigned(lr) << 19) | (unsigned(pts[i].second) << 2) | unsigned(n - 1)));
+    i += n;
+  }
+  for (size_t depth = 0, left = 1; left;) {
+    left = 0;
+    for (auto &bk : bank)
+      if (depth < bk.size()) {
+        chunks.push_back(bk[depth]);
+        left = 1;
+      }
+    ++depth;
+  }
+}
+
+// Seam-free colouring of the mixed form's cluster sweep on the CTA bands r0:
+// colour (col - row) mod 5 of the ext point, so the stencil's neighbours at
+// distance 1..4 along a row or a column always have another colour and the
+// points of one colour are independent.  No level chain: per (CTA, colour)
+// segment A (no halo read or write), B (within 4 rows of a shared band
+// edge), and an empty seam segment.
+template <class Fit>
+static void build_free_plan(HostGrid &g, const std::vector<int> &r0, Fit fit) {
+  const int C = int(r0.size()) - 1, S = 3;
+  g.cf_pts.clear();
+  g.cf_off.assign(size_t(C) * 5 * S + 1, 0);
+  int maxchunks = 0, maxa = 0, maxb = 0;
+  for (int k = 0; k < C; ++k) {
+    const int first = int(g.cf_pts.size());
+    auto edge = [&](int row) { return (k > 0 && row < r0[k] + 4) || (k < C - 1 && row >= r0[k + 1] - 4); };
+    const int ra = std::max(r0[k], 5), rb = std::min(r0[k + 1], g.nmu);
+    for (int c = 0; c < 5; ++c)
+      for (int seg = 0; seg < S; ++seg) {
+        const int seg0 = int(g.cf_pts.size());
+        g.cf_off[(size_t(k) * 5 + c) * S + seg] = seg0;
+        if (seg == 2) continue;
+        std::vector<std::pair<int, int>> pts;
+        for (int row = ra; row < rb; ++row) {
+          if (edge(row) != (seg == 1)) continue;
+          for (int col = 5; col <= g.nni + 2; ++col)
+            if (((col - row) % 5 + 5) % 5 == c) pts.push_back({row, col});
+        }
+        append_chunks(pts, r0[k], g.n8, g.cf_pts);
+        const int n = int(g.cf_pts.size()) - seg0;
+        if (seg == 0) maxa = std::max(maxa, n);
+        else maxb = std::max(maxb, n);
+      }
+    maxchunks = std::max(maxchunks, int(g.cf_pts.size()) - first);
+  }
+  g.cf_off[size_t(C) * 5 * S] = int(g.cf_pts.size());
+  g.cf_maxchunks = maxchunks;
+  g.cf_wa = std::max(1, (maxa + 31) / 32);
+  g.cf_wb = std::max(1, (maxb + 31) / 32);
+  g.cf_ws = 0;
+  g.cf_pa = g.cf_wa;
+  g.cf_pb = g.cf_wb;
+  g.cf_ps = 0;
+  fit(g.cf_wa, g.cf_wb, g.cf_ws, 24);
+  fit(g.cf_pa, g.cf_pb, g.cf_ps, 16);
+}
+
 std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf, double z1, double z2,
                             int mpole) {
   if (nni < 13 || nmu < 13 || (nni - 1) % 6 || (nmu - 1) % 6 || (nni - 6) % 5 || (nmu - 6) % 5)
@@ -477,31 +553,7 @@ std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf
                 pts.push_back({row, col});
               }
             }
-            std::sort(pts.begin(), pts.end());
-            // chunks bucketed by the shared-memory bank of their first point;
-            // dealing the buckets round-robin gives every warp's 32 chunks
-            // distinct banks where the buckets allow (the stencil reads of a
-            // chunk sit at fixed offsets from its first point)
-            std::vector<std::vector<int>> bank(32);
-            for (size_t i = 0; i < pts.size();) {
-              size_t n = 1;
-              while (n < 4 && i + n < pts.size() && pts[i + n].first == pts[i].first &&
-                     pts[i + n].second == pts[i + n - 1].second + 5)
-                ++n;
-              const int lr = pts[i].first - r0[k];
-              bank[((lr + 4) * g.n8 + pts[i].second) % 32].push_back(
-                  int((unsigned(lr) << 19) | (unsigned(pts[i].second) << 2) | unsigned(n - 1)));
-              i += n;
-            }
-            for (size_t depth = 0, left = 1; left;) {
-              left = 0;
-              for (auto &bk : bank)
-                if (depth < bk.size()) {
-                  chunks.push_back(bk[depth]);
-                  left = 1;
-                }
-              ++depth;
-            }
+            append_chunks(pts, r0[k], g.n8, chunks);
             const int n = int(chunks.size()) - seg0;
             if (seg == 0) maxa = std::max(maxa, n);
             else if (seg == 1) maxb = std::max(maxb, n);
@@ -545,6 +597,7 @@ std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf
         g.cl_row0 = r0;
         g.cl_pts = chunks;
         g.cl_off = coff;
+        build_free_plan(g, r0, fit);
       }
     }
   }
@@ -659,6 +712,19 @@ extern "C" int x2g_host_cluster_chunks(int nnu, int nmu, int *nchunks, int *noff
   if (noff) *noff = int(g.cl_off.size());
   if (chunks) std::copy(g.cl_pts.begin(), g.cl_pts.end(), chunks);
   if (off) std::copy(g.cl_off.begin(), g.cl_off.end(), off);
+  return X2G_OK;
+}
+
+// The same for the seam-free colouring of the mixed form (colour (col - row)
+// mod 5; per CTA and colour the segments A, B and an empty seam segment).
+extern "C" int x2g_host_free_chunks(int nnu, int nmu, int *nchunks, int *noff, int *chunks, int *off) {
+  x2g::HostGrid g;
+  std::string msg = x2g::build_host_grid(g, nnu, nmu, 2.0, 40.0, 1.0, 1.0, 4);
+  if (!msg.empty()) return X2G_ERR_SCHEDULE;
+  if (nchunks) *nchunks = int(g.cf_pts.size());
+  if (noff) *noff = int(g.cf_off.size());
+  if (chunks) std::copy(g.cf_pts.begin(), g.cf_pts.end(), chunks);
+  if (off) std::copy(g.cf_off.begin(), g.cf_off.end(), off);
   return X2G_OK;
 }
 
