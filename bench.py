@@ -650,12 +650,15 @@ def run_serve(args):
             out[name] = dict(serve.summary(done, wall), peak_footprint_bytes=srv.peak_bytes, hbm_budget_bytes=budget,
                              budget_waits=srv.budget_waits)
             out[name + "_energies"] = [c.total_energy for c in done]
+            out[name + "_converged"] = [c.converged for c in done]
             if name == "mixed":
                 # every request: template, grid, bond length, SCF iterations, exit (0: the iteration cap
                 # or stagnation, 1: energy threshold, 2: norm threshold)
                 out[name]["per_request"] = [[q.template, q.nnu, q.nmu, round(q.r, 4), c.iterations, c.converged]
                                             for q, c in zip(reqs, done)]
     de = max(abs(a - b) for a, b in zip(out["mixed_energies"], out["fp64_energies"]))
+    both = [i for i, (a, b) in enumerate(zip(out["mixed_converged"], out["fp64_converged"])) if a and b]
+    de_conv = max((abs(out["mixed_energies"][i] - out["fp64_energies"][i]) for i in both), default=None)
     same = out["mixed_energies"] == out["mixed_tight_budget_energies"]
     mx, f64 = out["mixed"], out["fp64"]
     return {"metric": "served SCF solves/s and p99 latency (Poisson arrivals), mixed vs FP64", "value":
@@ -668,7 +671,8 @@ def run_serve(args):
             "latency_s": {"p50": mx["latency_p50_s"], "p99": mx["latency_p99_s"],
                           "fp64_p50": f64["latency_p50_s"], "fp64_p99": f64["latency_p99_s"]},
             "mixed": mx, "fp64": f64, "mixed_tight_budget": out["mixed_tight_budget"],
-            "max_dE_mixed_vs_fp64": de, "tight_budget_energies_identical": same, "clocks": sampler.summary()}
+            "max_dE_mixed_vs_fp64": de, "max_dE_mixed_vs_fp64_both_converged": de_conv,
+            "both_converged": len(both), "tight_budget_energies_identical": same, "clocks": sampler.summary()}
 
 
 def C_double_pair(xg, nnu, nmu):

@@ -1708,57 +1708,90 @@ struct OrthoPlan {
   int nrounds;
 };
 
-__device__ void scale_item(const GridDev &g, const OrthoItem &I, double norm) {
-  const double zarea = D(1.0, sqrt(norm));
-  const int stride = gridDim.x * blockDim.x;
-  if (I.ihomo == 0) {
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += stride) {
-      const int mu = k / g.nni, nu = k - mu * g.nni;
-      const int ij = (mu + 4) * g.n8 + nu + 4;
-      I.psi[ij] = M(zarea, I.psi[ij]);
-    }
-    return;
-  }
-  const int n2 = g.nni / 2 + 1;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n2 * g.nmu; k += stride) {
-    const int mu = k / n2, ni = k - mu * n2;
-    const int row = (mu + 4) * g.n8 + 4;
-    if (ni < n2 - 1) {
-      const double v = M(zarea, I.psi[row + ni]);
-      I.psi[row + ni] = v;
-      I.psi[row + (g.nni - 1 - ni)] = (I.ihomo == 1) ? v : -v;
-    } else {
-      I.psi[row + ni] = (I.ihomo == 1) ? M(zarea, I.psi[row + ni]) : 0.0;
+// The phases below take up to kGroup orbitals (or orbital-partner pairs) of
+// a round in one pass over the points, so that their loads are in flight
+// together; each orbital's (pair's) per-thread sum still runs over the same
+// points in the same order, and block_sum_store reduces every slot the same
+// way whatever the number of slots stored, so the sums are those of the
+// one-orbital kernels.
+constexpr int kGroup = 8;
+
+// scaling (and setCiOrb) of items [a, b) of the plan with zarea[j]
+__device__ void scale_items(const GridDev &g, const OrthoPlan &P, int a, int b, const double *zarea) {
+  const int stride = gridDim.x * blockDim.x, n2 = g.nni / 2 + 1;
+  const int homo = P.it[a].ihomo != 0;  // one kind per call (the caller groups them)
+  const int n = homo ? n2 * g.nmu : g.mxsize;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+#pragma unroll
+    for (int j = 0; j < kGroup; ++j) {
+      if (a + j >= b) break;
+      const OrthoItem &I = P.it[a + j];
+      if (!homo) {
+        const int mu = k / g.nni, nu = k - mu * g.nni;
+        const int ij = (mu + 4) * g.n8 + nu + 4;
+        I.psi[ij] = M(zarea[j], I.psi[ij]);
+      } else {
+        const int mu = k / n2, ni = k - mu * n2;
+        const int row = (mu + 4) * g.n8 + 4;
+        if (ni < n2 - 1) {
+          const double v = M(zarea[j], I.psi[row + ni]);
+          I.psi[row + ni] = v;
+          I.psi[row + (g.nni - 1 - ni)] = (I.ihomo == 1) ? v : -v;
+        } else {
+          I.psi[row + ni] = (I.ihomo == 1) ? M(zarea[j], I.psi[row + ni]) : 0.0;
+        }
+      }
     }
   }
 }
 
 __global__ void __launch_bounds__(kThreads) k_orthonormalise(GridDev g, const __grid_constant__ OrthoPlan P,
                                                              double *partials, BarrierDev bar) {
-  __shared__ double s_ovl[kMaxK];
+  __shared__ double s_val[kGroup * kMaxK];
+  __shared__ int s_item[kMaxK], s_q[kMaxK];
   const int nb = int(gridDim.x);
   for (int r = 0; r < P.nrounds; ++r) {
     const int i0 = P.round_off[r], i1 = P.round_off[r + 1];
     bool partners = false;
-    for (int i = i0; i < i1; ++i) {
-      const OrthoItem &I = P.it[i];
-      partners = partners || I.n > 0;
-      double v[1] = {0.0};
+    for (int i = i0; i < i1; ++i) partners = partners || P.it[i].n > 0;
+    // norms: partial sums of every item of the round, kGroup at a time
+    for (int a = i0; a < i1; a += kGroup) {
+      double v[kGroup];
+#pragma unroll
+      for (int j = 0; j < kGroup; ++j) v[j] = 0.0;
       for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
         const int mu = k / g.nni, nu = k - mu * g.nni;
-        const double p = I.psi[(mu + 4) * g.n8 + nu + 4];
-        v[0] += g.wgt2[k] * M(M(p, p), g.f4[k]);
+        const int ij = (mu + 4) * g.n8 + nu + 4;
+        const double w2 = g.wgt2[k], f4 = g.f4[k];
+#pragma unroll
+        for (int j = 0; j < kGroup; ++j) {
+          if (a + j >= i1) break;
+          const double p = P.it[a + j].psi[ij];
+          v[j] += w2 * M(M(p, p), f4);
+        }
       }
-      block_sum_store<1>(v, partials + size_t(i - i0) * nb);
-      __syncthreads();
+#pragma unroll
+      for (int j = 0; j < kGroup; ++j) {
+        if (a + j >= i1) break;
+        double w[1] = {v[j]};
+        block_sum_store<1>(w, partials + size_t(a + j - i0) * nb);
+        __syncthreads();
+      }
     }
     __threadfence();
     if (!grid_barrier(bar, unsigned(nb))) return;
-    for (int i = i0; i < i1; ++i) {
-      const OrthoItem &I = P.it[i];
-      const double norm = sum_partials(partials + size_t(i - i0) * nb, 1, 0, nb);
-      if (blockIdx.x == 0 && threadIdx.x == 0) *I.norm_out = norm;
-      scale_item(g, I, norm);
+    // totals (every block, in block order), then the scaling, grouped by kind
+    for (int a = i0; a < i1;) {
+      int b = a;
+      while (b < i1 && b - a < kGroup && (P.it[b].ihomo != 0) == (P.it[a].ihomo != 0)) ++b;
+      double zarea[kGroup];
+      for (int j = 0; j < b - a; ++j) {
+        const double norm = sum_partials(partials + size_t(a + j - i0) * nb, 1, 0, nb);
+        if (blockIdx.x == 0 && threadIdx.x == 0) *P.it[a + j].norm_out = norm;
+        zarea[j] = D(1.0, sqrt(norm));
+      }
+      scale_items(g, P, a, b, zarea);
+      a = b;
     }
     if (!partners) {
       __threadfence();
@@ -1767,43 +1800,86 @@ __global__ void __launch_bounds__(kThreads) k_orthonormalise(GridDev g, const __
     }
     __threadfence();
     if (!grid_barrier(bar, unsigned(nb))) return;
-    for (int i = i0; i < i1; ++i) {
-      const OrthoItem &I = P.it[i];
-      if (I.n == 0) continue;
+    // overlaps: (item, partner) slots of the round, kMaxK at a time; values
+    // other blocks wrote in this launch are read through L2
+    int slot0 = 0;
+    for (int i = i0; i < i1;) {
+      // a slot group: at most kGroup items and kMaxK (item, partner) slots
+      int nslot = 0, iend = i;
+      while (iend < i1 && iend - i < kGroup && nslot + P.it[iend].n <= kMaxK) nslot += P.it[iend++].n;
+      if (iend == i) break;  // an item alone has at most kMaxK partners
+      if (threadIdx.x == 0) {
+        int t = 0;
+        for (int x = i; x < iend; ++x)
+          for (int q = 0; q < P.it[x].n; ++q, ++t) {
+            s_item[t] = x;
+            s_q[t] = q;
+          }
+      }
+      __syncthreads();
       double v[kMaxK];
-      for (int q = 0; q < kMaxK; ++q) v[q] = 0.0;
+#pragma unroll
+      for (int t = 0; t < kMaxK; ++t) v[t] = 0.0;
       for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
         const int mu = k / g.nni, nu = k - mu * g.nni;
         const int ij = (mu + 4) * g.n8 + nu + 4;
-        // values other blocks wrote in this launch: read through L2
-        const double p = __ldcg(I.psi + ij), w = g.wgt2[k], f4 = g.f4[k];
-        for (int q = 0; q < I.n; ++q) v[q] += w * M(M(p, __ldcg(I.o[q] + ij)), f4);
+        const double w = g.wgt2[k], f4 = g.f4[k];
+#pragma unroll
+        for (int t = 0; t < kMaxK; ++t) {
+          if (t >= nslot) break;
+          const OrthoItem &I = P.it[s_item[t]];
+          const double p = __ldcg(I.psi + ij);
+          v[t] += w * M(M(p, __ldcg(I.o[s_q[t]] + ij)), f4);
+        }
       }
-      block_sum_store<kMaxK>(v, partials + size_t(i - i0) * nb * kMaxK);
+      block_sum_store<kMaxK>(v, partials + size_t(slot0) * nb);
       __syncthreads();
+      slot0 += kMaxK;
+      i = iend;
     }
     __threadfence();
     if (!grid_barrier(bar, unsigned(nb))) return;
-    for (int i = i0; i < i1; ++i) {
-      const OrthoItem &I = P.it[i];
-      if (I.n == 0) continue;
-      for (int q = 0; q < I.n; ++q) {
-        const double t = sum_partials(partials + size_t(i - i0) * nb * kMaxK, kMaxK, q, nb);
-        if (threadIdx.x == 0) s_ovl[q] = t;
+    // totals, then the Gram-Schmidt step of up to kGroup items at a time
+    slot0 = 0;
+    for (int i = i0; i < i1;) {
+      int nslot = 0, iend = i;
+      while (iend < i1 && iend - i < kGroup && nslot + P.it[iend].n <= kMaxK) nslot += P.it[iend++].n;
+      if (iend == i) break;
+      for (int x = i, t = 0; x < iend; ++x)
+        for (int q = 0; q < P.it[x].n; ++q, ++t) {
+          const double tot = sum_partials(partials + size_t(slot0) * nb, kMaxK, t, nb);
+          if (threadIdx.x == 0) s_val[(x - i) * kMaxK + q] = tot;
+          if (blockIdx.x == 0 && threadIdx.x == 0) P.it[x].ovl_out[q] = tot;
+        }
+      __syncthreads();
+      {
+        const int a = i, b = iend;
+        double ano[kGroup];
+        for (int j = 0; j < b - a; ++j) {
+          const OrthoItem &I = P.it[a + j];
+          const double *ovl = s_val + j * kMaxK;
+          double x = 0.0;
+          for (int q = 0; q < I.n; ++q) x = A(x, M(ovl[q], ovl[q]));
+          ano[j] = D(sqrt(A(1.0, x)), S(1.0, M(x, x)));
+        }
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+          const int mu = k / g.nni, nu = k - mu * g.nni;
+          const int ij = (mu + 4) * g.n8 + nu + 4;
+#pragma unroll
+          for (int j = 0; j < kGroup; ++j) {
+            if (a + j >= b) break;
+            const OrthoItem &I = P.it[a + j];
+            if (I.n == 0) continue;
+            const double *ovl = s_val + j * kMaxK;
+            double v = __ldcg(I.psi + ij);
+            for (int q = 0; q < I.n; ++q) v = A(M(-ovl[q], __ldcg(I.o[q] + ij)), v);
+            I.psi[ij] = M(ano[j], v);
+          }
+        }
       }
       __syncthreads();
-      if (blockIdx.x == 0 && threadIdx.x < I.n) I.ovl_out[threadIdx.x] = s_ovl[threadIdx.x];
-      double ano = 0.0;
-      for (int q = 0; q < I.n; ++q) ano = A(ano, M(s_ovl[q], s_ovl[q]));
-      ano = D(sqrt(A(1.0, ano)), S(1.0, M(ano, ano)));
-      for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
-        const int mu = k / g.nni, nu = k - mu * g.nni;
-        const int ij = (mu + 4) * g.n8 + nu + 4;
-        double v = __ldcg(I.psi + ij);
-        for (int q = 0; q < I.n; ++q) v = A(M(-s_ovl[q], __ldcg(I.o[q] + ij)), v);
-        I.psi[ij] = M(ano, v);
-      }
-      __syncthreads();
+      slot0 += kMaxK;
+      i = iend;
     }
     __threadfence();
     if (r + 1 < P.nrounds && !grid_barrier(bar, unsigned(nb))) return;
