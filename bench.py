@@ -491,6 +491,11 @@ def run_gpu(args):
                      "launch is bound by phase latency (neighbour wait, halo round trip, level chain), not by HBM"),
             "sweep_ms_total": msmx, "sweep_launches": nmx, "point_updates": ptsmx,
             "point_updates_per_launch": pts_per_launch,
+            # SM-side utilisation of the on-chip sweep (ncu --set full, one launch of 16 potentials on
+            # this grid; profiles/mixed_cluster_pot_sweep_poisson_b16_331x481.md): the kernel's bound
+            "sm_side_ncu": ({"l1_shared_throughput_frac": 0.524, "issue_active_frac": 0.439,
+                             "lsu_instruction_frac": 0.342, "fma_pipe_frac": 0.194,
+                             "barrier_stalls_per_issue": 7.63} if on_chip else None),
             "clusters_co_resident": {"plain": occ[0], "potentials_variant": occ[1],
                                      "potentials_variant_mode": args.potential_clusters},
             "colouring": args.colouring,
@@ -869,7 +874,8 @@ def run_reference(args):
               if name in FIXED_ITERS else METRIC)
     value = (args.steps / sum(walls)) if name in REF_FULL_SOLVE else statistics.median(vals)
     out = {
-        "metric": metric, "value": value, "unit": unit, "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+        # n_gpus: the N this arm was launched for, as the GPU arm's line; the work runs on host cores
+        "metric": metric, "value": value, "unit": unit, "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * sum(walls) / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic: hydrogenic LCAO start of the reference's input",
         "impl": "reference", "config": workload_config(name),
