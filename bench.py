@@ -499,6 +499,7 @@ def run_gpu(args):
             "clusters_co_resident": {"plain": occ[0], "potentials_variant": occ[1],
                                      "potentials_variant_mode": args.potential_clusters},
             "colouring": args.colouring,
+            "residual_overlap": args.residual_overlap,
             "fp64_kernel": {"kernel": "k_mcsor_f64", "achieved_gbs": sweep_gbs_64,
                             "frac_hbm": (sweep_gbs_64 / hbm) if sweep_gbs_64 else None,
                             "achieved_tflops": pts64 * FLOPS_PER_PT / (ms64 / 1e3) / 1e12 if ms64 > 0 else None,
@@ -922,6 +923,7 @@ def _configure(ctx, args):
     mode = getattr(args, "potential_clusters", "auto")
     ctx.set_potential_clusters("auto" if mode == "auto" else mode == "on")
     ctx.set_mixed_colouring(getattr(args, "colouring", "reference"))
+    ctx.set_residual_overlap(getattr(args, "residual_overlap", "on") == "on")
 
 
 def main():
@@ -948,6 +950,8 @@ def main():
     ap.add_argument("--potential-clusters", default="auto", choices=["auto", "on", "off"],
                     help="mixed form: cluster sweep of potential batches at two CTAs per SM "
                          "(default: for batches above the plain kernel's co-resident clusters)")
+    ap.add_argument("--residual-overlap", default="on", choices=["on", "off"],
+                    help="mixed form: second-wave potentials' FP64 residual beside the first wave's sweep")
     ap.add_argument("--colouring", default="reference", choices=["reference", "free"],
                     help="mixed form: colouring of the on-chip cluster sweep")
     ap.add_argument("--window", default="", help="WARM,N: profile SCF iterations WARM+1..WARM+N of the headline form "

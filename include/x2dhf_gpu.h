@@ -164,6 +164,13 @@ int x2g_set_mixed_on_chip(x2g_ctx *ctx, int on);
  * mode 0 never, 1 always, 2 (default) for batches larger than the clusters
  * of the plain kernel co-resident on the device.  No reference counterpart. */
 int x2g_set_potential_clusters(x2g_ctx *ctx, int mode);
+/* Mixed form, potential batches larger than the co-resident clusters of
+ * the potentials' cluster variant: 1 (default) the batch runs in waves of
+ * that size and the FP64 residuals of the later waves run on the context's
+ * low-priority auxiliary stream beside the earlier waves' sweeps (on the SMs
+ * they leave free), 0 every residual before the first sweep.  Same kernels,
+ * same results.  No reference counterpart. */
+int x2g_set_residual_overlap(x2g_ctx *ctx, int on);
 /* Colouring of the mixed form's on-chip cluster sweep: 0 the reference's
  * (colour = position in the "middle" list mod 5, sormcsor.F90:143-386, with
  * its seam points relaxed level by level, so that in exact arithmetic the

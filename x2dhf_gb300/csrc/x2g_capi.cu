@@ -76,13 +76,31 @@ int x2g_create(x2g_ctx **out, int device) {
     return set_status(X2G_ERR_UNSUPPORTED, "device lacks cooperative launch");
   }
   c->num_sms = prop.multiProcessorCount;
-  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+  // the context's stream at the highest priority, an auxiliary stream at
+  // the lowest: work queued on the auxiliary stream fills the SMs the main
+  // stream's kernels leave free (the FP64 residual of a second group of
+  // potentials while the first group sweeps)
+  int least = 0, greatest = 0;
+  if ((e = cudaDeviceGetStreamPriorityRange(&least, &greatest)) != cudaSuccess ||
+      (e = cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, greatest)) != cudaSuccess) {
     delete c;
     return cuda_status(e, "cudaStreamCreate");
+  }
+  if ((e = cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, least)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&c->ev_split[0], cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&c->ev_split[1], cudaEventDisableTiming)) != cudaSuccess) {
+    cudaStreamDestroy(c->stream);
+    if (c->aux) cudaStreamDestroy(c->aux);
+    if (c->ev_split[0]) cudaEventDestroy(c->ev_split[0]);
+    delete c;
+    return cuda_status(e, "auxiliary stream");
   }
   if ((e = cudaMalloc(&c->bar, kBarWords * sizeof(unsigned))) != cudaSuccess ||
       (e = cudaMemset(c->bar, 0, kBarWords * sizeof(unsigned))) != cudaSuccess) {
     cudaStreamDestroy(c->stream);
+    cudaStreamDestroy(c->aux);
+    cudaEventDestroy(c->ev_split[0]);
+    cudaEventDestroy(c->ev_split[1]);
     delete c;
     return cuda_status(e, "barrier allocation");
   }
@@ -111,6 +129,10 @@ int x2g_destroy(x2g_ctx *c) {
   if (c->red) cudaFree(c->red);
   if (c->bar) cudaFree(c->bar);
   if (c->host_red) cudaFreeHost(c->host_red);
+  cudaStreamSynchronize(c->aux);
+  cudaEventDestroy(c->ev_split[0]);
+  cudaEventDestroy(c->ev_split[1]);
+  cudaStreamDestroy(c->aux);
   cudaStreamDestroy(c->stream);
   delete c;
   return X2G_OK;
@@ -191,6 +213,12 @@ int x2g_set_mixed_on_chip(x2g_ctx *c, int on) {
 int x2g_set_potential_clusters(x2g_ctx *c, int mode) {
   if (!c || mode < 0 || mode > 2) return set_status(X2G_ERR_ARG, "mode must be 0, 1 or 2");
   c->pot_clusters = mode;
+  return X2G_OK;
+}
+
+int x2g_set_residual_overlap(x2g_ctx *c, int on) {
+  if (!c || on < 0 || on > 1) return set_status(X2G_ERR_ARG, "on must be 0 or 1");
+  c->residual_overlap = on;
   return X2G_OK;
 }
 

@@ -178,7 +178,10 @@ constexpr unsigned long long kDefaultWaitLimitNs = 2000000000ull;  // 2 s
 struct x2g_ctx {
   int device = 0;
   int num_sms = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;  // highest priority
+  cudaStream_t aux = nullptr;     // lowest priority, joined back into stream by events
+  cudaEvent_t ev_split[2] = {nullptr, nullptr};
+  int residual_overlap = 1;       // potential batches in two waves: the second wave's residual under the first's sweep
   // barrier words + error flag (4 ints)
   unsigned int *bar = nullptr;
   // reusable device workspace

@@ -2257,11 +2257,82 @@ static int f64_block_limit(x2g_ctx *ctx) {
 }
 
 // One launch batch (at most kParamJobs jobs) of launch_relax.
+// One launch of the on-chip cluster sweep over the jobs of jt, timed with the
+// context's events when profiling.
+static int cluster_sweep(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, int nsweeps, bool pot) {
+  x2g_ctx::Pending pe{};
+  if (ctx->profiling) {
+    int rc;
+    if ((rc = take_event(ctx, &pe.a)) || (rc = take_event(ctx, &pe.b))) return rc;
+    pe.precision = 1;
+    pe.points = double(njobs) * double(g.nni - 2) * double(g.nmu - 5) * double(nsweeps);
+    cudaEventRecord(pe.a, ctx->stream);
+  }
+  const int free = ctx->mixed_free;
+  const size_t smem = cluster_smem_bytes(g, pot, free != 0);
+  if (!cluster_attributes(ctx) || smem > ctx->cluster_smem_set)
+    return set_status(X2G_ERR_CUDA, "cluster kernel attributes could not be set");
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(unsigned(njobs * g.cl_size));
+  cfg.blockDim = dim3(unsigned(cluster_threads(g, pot, free != 0)));
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = ctx->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = unsigned(g.cl_size);
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  GridDev gd = g;
+  cudaError_t err = pot ? cudaLaunchKernelEx(&cfg, k_mixed_cluster_pot, gd, jt, nsweeps, free)
+                        : cudaLaunchKernelEx(&cfg, k_mixed_cluster, gd, jt, nsweeps, free);
+  if (err != cudaSuccess) return cuda_status(err, "cluster MCSOR launch");
+  ctx->launches += 1;
+  if (ctx->profiling) {
+    cudaEventRecord(pe.b, ctx->stream);
+    ctx->pending.push_back(pe);
+  }
+  return X2G_OK;
+}
+
+// One launch batch (at most kParamJobs jobs) of launch_relax.
 static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, int nsweeps, bool mixed,
                        bool on_chip, bool pot, int G, size_t smem) {
   cudaError_t err;
   x2g_ctx::Pending pe{};
   const double points = double(njobs) * double(g.nni - 2) * double(g.nmu - 5) * double(nsweeps);
+  const int wave = ctx->cluster_active[1];
+  if (mixed && on_chip && pot && ctx->residual_overlap && wave > 0 && njobs > wave) {
+    // waves of the potentials' cluster variant: the first wave's FP64
+    // residual, then the later waves' residuals on the low-priority
+    // auxiliary stream, beside the sweeps (on the SMs they leave free);
+    // each sweep waits for its own wave's residual
+    const int nw = (njobs + wave - 1) / wave;
+    std::vector<JobTable> w(size_t(nw), JobTable{});
+    const unsigned nblk = unsigned(grid_blocks((g.nni - 2) * (g.nmu - 5)));
+    for (int c = 0; c < nw; ++c)
+      for (int i = c * wave; i < njobs && i < (c + 1) * wave; ++i) w[c].j[i - c * wave] = jt.j[i];
+    auto size = [&](int c) { return std::min(njobs, (c + 1) * wave) - c * wave; };
+    k_residual<false><<<dim3(nblk, size(0)), kThreads, 0, ctx->stream>>>(g, w[0], 0, 0);
+    ctx->launches += 1;
+    if ((err = cudaEventRecord(ctx->ev_split[0], ctx->stream)) != cudaSuccess ||
+        (err = cudaStreamWaitEvent(ctx->aux, ctx->ev_split[0], 0)) != cudaSuccess)
+      return cuda_status(err, "residual overlap");
+    for (int c = 0; c < nw; ++c) {
+      cudaEvent_t ev = ctx->ev_split[(c + 1) & 1];
+      if (c + 1 < nw) {
+        k_residual<false><<<dim3(nblk, size(c + 1)), kThreads, 0, ctx->aux>>>(g, w[c + 1], 0, 0);
+        ctx->launches += 1;
+        if ((err = cudaEventRecord(ev, ctx->aux)) != cudaSuccess) return cuda_status(err, "residual overlap");
+      }
+      int rc = cluster_sweep(ctx, g, w[c], size(c), nsweeps, true);
+      if (rc) return rc;
+      if (c + 1 < nw && (err = cudaStreamWaitEvent(ctx->stream, ev, 0)) != cudaSuccess)
+        return cuda_status(err, "residual overlap");
+    }
+    return X2G_OK;
+  }
   if (mixed) {
     dim3 gr(grid_blocks((g.nni - 2) * (g.nmu - 5)), njobs);
     if (on_chip)
@@ -2270,6 +2341,7 @@ static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, 
       k_residual<true><<<gr, kThreads, 0, ctx->stream>>>(g, jt, 1, 1);
     ctx->launches += 1;
   }
+  if (on_chip) return cluster_sweep(ctx, g, jt, njobs, nsweeps, pot);
   if (ctx->profiling) {
     int rc;
     if ((rc = take_event(ctx, &pe.a)) || (rc = take_event(ctx, &pe.b))) return rc;
@@ -2277,33 +2349,7 @@ static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, 
     pe.points = points;
     cudaEventRecord(pe.a, ctx->stream);
   }
-  if (on_chip) {
-    const int free = ctx->mixed_free;
-    const size_t smem = cluster_smem_bytes(g, pot, free != 0);
-    if (!cluster_attributes(ctx) || smem > ctx->cluster_smem_set)
-      return set_status(X2G_ERR_CUDA, "cluster kernel attributes could not be set");
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(unsigned(njobs * g.cl_size));
-    cfg.blockDim = dim3(unsigned(cluster_threads(g, pot, free != 0)));
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = ctx->stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = unsigned(g.cl_size);
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    GridDev gd = g;
-    err = pot ? cudaLaunchKernelEx(&cfg, k_mixed_cluster_pot, gd, jt, nsweeps, free)
-              : cudaLaunchKernelEx(&cfg, k_mixed_cluster, gd, jt, nsweeps, free);
-    if (err != cudaSuccess) return cuda_status(err, "cluster MCSOR launch");
-    ctx->launches += 1;
-    if (ctx->profiling) {
-      cudaEventRecord(pe.b, ctx->stream);
-      ctx->pending.push_back(pe);
-    }
-  } else {
+  {
     // persistent cooperative kernels: the FP64 sweep with grid barriers,
     // the mixed form's persistent-band sweep with neighbour waits.  Only the
     // arrival count and generation are reset: the error word keeps an
