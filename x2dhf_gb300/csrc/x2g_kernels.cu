@@ -1695,9 +1695,9 @@ __global__ void k_ortho_round(GridDev g, const __grid_constant__ OrthoRound R) {
 }
 
 // Every round of an iteration's orthonormalisation in one cooperative
-// launch: per round the norms, the scaling (and setCiOrb), the overlaps
-// with the partners and the Gram-Schmidt step of each of its orbitals,
-// separated by grid barriers.  Each block stores the same per-block partial
+// launch: the norms and scalings (and setCiOrb) of every orbital, then per
+// round the overlaps with the partners and the Gram-Schmidt step of each of
+// its orbitals, separated by grid barriers.  Each block stores the same per-block partial
 // sums as k_norm_round / k_overlaps_round (same blocks, same points, same
 // order) and every block adds them up in the order of block_sum_finish, so
 // the results equal the per-round launches bit for bit.
@@ -1750,54 +1750,56 @@ __global__ void __launch_bounds__(kThreads) k_orthonormalise(GridDev g, const __
   __shared__ double s_val[kGroup * kMaxK];
   __shared__ int s_item[kMaxK], s_q[kMaxK];
   const int nb = int(gridDim.x);
+  // An orbital is changed only in its own round, after its partners'
+  // rounds: its norm and scaling read nothing another round writes, so the
+  // norms and scalings of every round run first, in one pass, and the rounds
+  // keep only their overlaps and Gram-Schmidt steps.
+  const int n = P.round_off[P.nrounds];
+  for (int a = 0; a < n; a += kGroup) {
+    double v[kGroup];
+#pragma unroll
+    for (int j = 0; j < kGroup; ++j) v[j] = 0.0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+      const int mu = k / g.nni, nu = k - mu * g.nni;
+      const int ij = (mu + 4) * g.n8 + nu + 4;
+      const double w2 = g.wgt2[k], f4 = g.f4[k];
+#pragma unroll
+      for (int j = 0; j < kGroup; ++j) {
+        if (a + j >= n) break;
+        const double p = P.it[a + j].psi[ij];
+        v[j] += w2 * M(M(p, p), f4);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kGroup; ++j) {
+      if (a + j >= n) break;
+      double w[1] = {v[j]};
+      block_sum_store<1>(w, partials + size_t(a + j) * nb);
+      __syncthreads();
+    }
+  }
+  __threadfence();
+  if (!grid_barrier(bar, unsigned(nb))) return;
+  // totals (every block, in block order), then the scaling, grouped by kind
+  for (int a = 0; a < n;) {
+    int b = a;
+    while (b < n && b - a < kGroup && (P.it[b].ihomo != 0) == (P.it[a].ihomo != 0)) ++b;
+    double zarea[kGroup];
+    for (int j = 0; j < b - a; ++j) {
+      const double norm = sum_partials(partials + size_t(a + j) * nb, 1, 0, nb);
+      if (blockIdx.x == 0 && threadIdx.x == 0) *P.it[a + j].norm_out = norm;
+      zarea[j] = D(1.0, sqrt(norm));
+    }
+    scale_items(g, P, a, b, zarea);
+    a = b;
+  }
   for (int r = 0; r < P.nrounds; ++r) {
     const int i0 = P.round_off[r], i1 = P.round_off[r + 1];
     bool partners = false;
     for (int i = i0; i < i1; ++i) partners = partners || P.it[i].n > 0;
-    // norms: partial sums of every item of the round, kGroup at a time
-    for (int a = i0; a < i1; a += kGroup) {
-      double v[kGroup];
-#pragma unroll
-      for (int j = 0; j < kGroup; ++j) v[j] = 0.0;
-      for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
-        const int mu = k / g.nni, nu = k - mu * g.nni;
-        const int ij = (mu + 4) * g.n8 + nu + 4;
-        const double w2 = g.wgt2[k], f4 = g.f4[k];
-#pragma unroll
-        for (int j = 0; j < kGroup; ++j) {
-          if (a + j >= i1) break;
-          const double p = P.it[a + j].psi[ij];
-          v[j] += w2 * M(M(p, p), f4);
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < kGroup; ++j) {
-        if (a + j >= i1) break;
-        double w[1] = {v[j]};
-        block_sum_store<1>(w, partials + size_t(a + j - i0) * nb);
-        __syncthreads();
-      }
-    }
-    __threadfence();
-    if (!grid_barrier(bar, unsigned(nb))) return;
-    // totals (every block, in block order), then the scaling, grouped by kind
-    for (int a = i0; a < i1;) {
-      int b = a;
-      while (b < i1 && b - a < kGroup && (P.it[b].ihomo != 0) == (P.it[a].ihomo != 0)) ++b;
-      double zarea[kGroup];
-      for (int j = 0; j < b - a; ++j) {
-        const double norm = sum_partials(partials + size_t(a + j - i0) * nb, 1, 0, nb);
-        if (blockIdx.x == 0 && threadIdx.x == 0) *P.it[a + j].norm_out = norm;
-        zarea[j] = D(1.0, sqrt(norm));
-      }
-      scale_items(g, P, a, b, zarea);
-      a = b;
-    }
-    if (!partners) {
-      __threadfence();
-      if (r + 1 < P.nrounds && !grid_barrier(bar, unsigned(nb))) return;
-      continue;
-    }
+    if (!partners) continue;
+    // the scalings and the earlier rounds' Gram-Schmidt steps done
+    // everywhere before this round's overlaps
     __threadfence();
     if (!grid_barrier(bar, unsigned(nb))) return;
     // overlaps: (item, partner) slots of the round, kMaxK at a time; values
@@ -1881,8 +1883,6 @@ __global__ void __launch_bounds__(kThreads) k_orthonormalise(GridDev g, const __
       slot0 += kMaxK;
       i = iend;
     }
-    __threadfence();
-    if (r + 1 < P.nrounds && !grid_barrier(bar, unsigned(nb))) return;
   }
 }
 
@@ -2758,11 +2758,11 @@ bool launch_orthonormalise(x2g_ctx *ctx, const GridDev &g, const OrthoOrbital *o
     I.norm_out = x.norm_out;
     I.ovl_out = x.ovl_out;
   }
-  int most = 0;
+  int most = n;  // the norms of every item, or a round's overlap slot groups (kMaxK slots each)
   for (int r = 0; r <= nrounds; ++r) P.round_off[r] = round_off[r];
-  for (int r = 0; r < nrounds; ++r) most = std::max(most, round_off[r + 1] - round_off[r]);
+  for (int r = 0; r < nrounds; ++r) most = std::max(most, kMaxK * (round_off[r + 1] - round_off[r]));
   P.nrounds = nrounds;
-  double *part = reduction_partials(ctx, kMaxK * most);
+  double *part = reduction_partials(ctx, most);
   if (!part) return false;
   if (cudaMemsetAsync(ctx->bar, 0, 2 * sizeof(unsigned), ctx->stream) != cudaSuccess) return false;
   BarrierDev bar{ctx->bar, ctx->bar + 1, reinterpret_cast<int *>(ctx->bar + 2), ctx->wait_limit_ns};
