@@ -20,6 +20,12 @@ constexpr int kMaxLevels = 8;
 // sweep's per-block phase counts from word kPhaseWords (kPhaseBlocks, one
 // 128-byte line each)
 constexpr int kMomentTickets = 288;
+// most warps per CTA of the potentials' cluster variant (two CTAs per SM:
+// the register file holds 2 x 32 x warps threads at <= 65536 / that
+// registers each): 16 with the reference colouring (measured faster than 20
+// at 48 registers), 20 with the seam-free one, whose two segments then take
+// every chunk of a colour in one pass
+constexpr int kPotWarpsRef = 16, kPotWarpsFree = 20;
 constexpr int kPhaseWords = 352, kPhaseBlocks = 320, kPhaseStride = 32;
 constexpr int kBarWords = kPhaseWords + kPhaseBlocks * kPhaseStride;
 
@@ -53,7 +59,7 @@ struct HostGrid {
   // cluster plan of the on-chip FP32 sweep: cl_size CTAs per job, CTA k
   // owns tiles [cl_tile0[k], cl_tile0[k+1]) = ext rows [cl_row0[k], cl_row0[k+1])
   int cl_size = 0, cl_maxrows = 0, cl_maxchunks = 0, cl_wa = 1, cl_wb = 1, cl_ws = 1;
-  // warps per role of the potentials' variant (two CTAs per SM, 16 warps)
+  // warps per role of the potentials' variant (two CTAs per SM, at most kPotWarpsRef)
   int cl_pa = 1, cl_pb = 1, cl_ps = 1;
   // the same CTA bands with the seam-free colouring of the mixed form,
   // colour (col - row) mod 5 in ext coordinates (no two points of a colour

@@ -739,7 +739,7 @@ size_t cluster_smem_bytes(const GridDev &g, bool sep, bool free) {
          size_t(g.cl_maxrows + g.n8) * sizeof(float) * (sep ? 2 : 1) + size_t(5 * S + 1) * sizeof(int) +
          size_t(chunks) * sizeof(int);
 }
-constexpr int kClusterPotThreads = 512;  // potentials' variant: 16 warps, two CTAs per SM
+
 
 // split cluster barrier: arrive releases this thread's earlier shared and
 // distributed-shared writes, wait acquires every CTA's released writes
@@ -1047,11 +1047,18 @@ __global__ void __launch_bounds__(kClusterMaxThreads, 1) k_mixed_cluster(GridDev
 }
 
 // Potentials only (job kind 1): two CTAs per SM, so that twice the clusters
-// are co-resident for the batches of an SCF iteration's potentials
-__global__ void __launch_bounds__(kClusterPotThreads, 2) k_mixed_cluster_pot(GridDev g,
-                                                                            const __grid_constant__ JobTable jobs,
-                                                                            int nsweeps, int free) {
+// are co-resident for the batches of an SCF iteration's potentials; at most
+// kWarps warps per CTA (kPotWarpsRef for the reference colouring,
+// kPotWarpsFree for the seam-free one)
+template <int kWarps>
+__global__ void __launch_bounds__(32 * kWarps, 2) k_mixed_cluster_pot(GridDev g, const __grid_constant__ JobTable jobs,
+                                                                     int nsweeps, int free) {
   mixed_cluster_body<true>(g, jobs, nsweeps, free);
+}
+
+// the potentials' variant for a colouring
+static const void *pot_kernel(bool free) {
+  return free ? (const void *)k_mixed_cluster_pot<kPotWarpsFree> : (const void *)k_mixed_cluster_pot<kPotWarpsRef>;
 }
 
 // ----------------------------------------------------------------------
@@ -2134,10 +2141,10 @@ static bool cluster_attributes(x2g_ctx *ctx) {
           cudaSuccess ||
       cudaFuncSetAttribute((const void *)k_mixed_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
           cudaSuccess ||
-      cudaFuncSetAttribute((const void *)k_mixed_cluster_pot, cudaFuncAttributeMaxDynamicSharedMemorySize, optin) !=
-          cudaSuccess ||
-      cudaFuncSetAttribute((const void *)k_mixed_cluster_pot, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
-          cudaSuccess) {
+      cudaFuncSetAttribute(pot_kernel(false), cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess ||
+      cudaFuncSetAttribute(pot_kernel(false), cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess ||
+      cudaFuncSetAttribute(pot_kernel(true), cudaFuncAttributeMaxDynamicSharedMemorySize, optin) != cudaSuccess ||
+      cudaFuncSetAttribute(pot_kernel(true), cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
     (void)cudaGetLastError();
     return false;
   }
@@ -2179,7 +2186,7 @@ static bool cluster_usable(x2g_ctx *ctx, const GridDev &g, bool pot = false) {
       q.attrs = qa;
       q.numAttrs = 1;
       int nclusters = 0;
-      const void *fn = pot ? (const void *)k_mixed_cluster_pot : (const void *)k_mixed_cluster;
+      const void *fn = pot ? pot_kernel(free) : (const void *)k_mixed_cluster;
       if (cudaOccupancyMaxActiveClusters(&nclusters, fn, &q) == cudaSuccess && nclusters > 0) {
         ctx->cluster_ok[v] = 1;
         ctx->cluster_active[v] = nclusters;
@@ -2285,8 +2292,9 @@ static int cluster_sweep(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   GridDev gd = g;
-  cudaError_t err = pot ? cudaLaunchKernelEx(&cfg, k_mixed_cluster_pot, gd, jt, nsweeps, free)
-                        : cudaLaunchKernelEx(&cfg, k_mixed_cluster, gd, jt, nsweeps, free);
+  cudaError_t err = !pot ? cudaLaunchKernelEx(&cfg, k_mixed_cluster, gd, jt, nsweeps, free)
+                    : free ? cudaLaunchKernelEx(&cfg, k_mixed_cluster_pot<kPotWarpsFree>, gd, jt, nsweeps, free)
+                           : cudaLaunchKernelEx(&cfg, k_mixed_cluster_pot<kPotWarpsRef>, gd, jt, nsweeps, free);
   if (err != cudaSuccess) return cuda_status(err, "cluster MCSOR launch");
   ctx->launches += 1;
   if (ctx->profiling) {

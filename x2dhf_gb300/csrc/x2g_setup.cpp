@@ -216,7 +216,7 @@ static void build_free_plan(HostGrid &g, const std::vector<int> &r0, Fit fit) {
   g.cf_pb = g.cf_wb;
   g.cf_ps = 0;
   fit(g.cf_wa, g.cf_wb, g.cf_ws, 24);
-  fit(g.cf_pa, g.cf_pb, g.cf_ps, 16);
+  fit(g.cf_pa, g.cf_pb, g.cf_ps, kPotWarpsFree);
 }
 
 std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf, double z1, double z2,
@@ -591,7 +591,7 @@ std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf
         g.cl_pb = g.cl_wb;
         g.cl_ps = g.cl_ws;
         fit(g.cl_wa, g.cl_wb, g.cl_ws, 24);
-        fit(g.cl_pa, g.cl_pb, g.cl_ps, 16);
+        fit(g.cl_pa, g.cl_pb, g.cl_ps, kPotWarpsRef);
         g.cl_smem = smem;
         g.cl_tile0 = t0;
         g.cl_row0 = r0;
