@@ -124,6 +124,22 @@ def test_free_colouring_chunks_cover_grid(nnu, nmu):
                 assert seen.get(nb, -1) != c
 
 
+def test_schedule_cache_returns_the_built_schedules():
+    """The sweep schedules depend on the grid size only and are kept in a
+    process-wide cache of recent sizes: a size built again (after others in
+    between, and more sizes than the cache holds) gives the same schedules."""
+    first = {n: xg.host_cluster_chunks(*n) for n in [(151, 241), (331, 481)]}
+    sor_first = xg.host_sor_schedule(331, 481)
+    for n in [(91, 121), (121, 181), (181, 241), (211, 301), (241, 331), (271, 361), (301, 421), (361, 481),
+              (331, 481), (151, 241)]:
+        xg.host_cluster_chunks(*n)
+    for n, (ch, off) in first.items():
+        ch2, off2 = xg.host_cluster_chunks(*n)
+        assert np.array_equal(ch, ch2) and np.array_equal(off, off2)
+    for a, b in zip(sor_first[:4], xg.host_sor_schedule(331, 481)[:4]):
+        assert np.array_equal(a, b)
+
+
 def test_large_grid_has_no_cluster_plan():
     assert xg.host_cluster_plan(781, 1201)[0] == 0
 

@@ -4,6 +4,8 @@
 // written out in 0-based C++; the schedule (row bands, colour levels) is this
 // library's own.
 #include <algorithm>
+#include <memory>
+#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <numeric>
@@ -219,6 +221,8 @@ static void build_free_plan(HostGrid &g, const std::vector<int> &r0, Fit fit) {
   fit(g.cf_pa, g.cf_pb, g.cf_ps, kPotWarpsFree);
 }
 
+std::string attach_schedule(HostGrid &g);
+
 std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf, double z1, double z2,
                             int mpole) {
   if (nni < 13 || nmu < 13 || (nni - 1) % 6 || (nmu - 1) % 6 || (nni - 6) % 5 || (nmu - 6) % 5)
@@ -369,6 +373,17 @@ std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf
       }
     }
 
+  return attach_schedule(g);
+}
+
+// The sweep schedules of a grid -- "middle" ordering, colour levels, tiles,
+// cluster plans, persistent-band and SOR schedules -- depend on N_nu and
+// N_mu only.  build_schedule makes them; attach_schedule copies them from a
+// process-wide cache of the most recent grid sizes (they take tens of
+// milliseconds to build; a serving loop or repeated solves on one grid size
+// build them once).
+static std::string build_schedule(HostGrid &g) {
+  const int nni = g.nni, nmu = g.nmu;
   // ------------------------------------------------------------------
   // "middle" ordering of the interior points (mesh:2503-2544), 1-based
   // ext rows ii in 6..nmu, cols jj in 6..nni+3, middle-outward.
@@ -609,6 +624,84 @@ std::string build_host_grid(HostGrid &g, int nni, int nmu, double r, double rinf
     if (!(lev[d.second] > lev[d.first])) return "schedule check: level order violated";
   }
   return build_sor_schedule(g, pos, offs);
+}
+
+
+namespace {
+struct ScheduleCache {
+  std::mutex m;
+  std::vector<std::shared_ptr<const HostGrid>> entries;  // most recent last
+};
+ScheduleCache &schedule_cache() {
+  static ScheduleCache c;
+  return c;
+}
+void copy_schedule(HostGrid &to, const HostGrid &from) {
+  to.order = from.order;
+  to.ntiles = from.ntiles;
+  to.nlev = from.nlev;
+  to.tile_row0 = from.tile_row0;
+  to.tile_row1 = from.tile_row1;
+  to.pts = from.pts;
+  to.off = from.off;
+  to.pts_rc = from.pts_rc;
+  to.cl_size = from.cl_size;
+  to.cl_maxrows = from.cl_maxrows;
+  to.cl_maxchunks = from.cl_maxchunks;
+  to.cl_wa = from.cl_wa;
+  to.cl_wb = from.cl_wb;
+  to.cl_ws = from.cl_ws;
+  to.cl_pa = from.cl_pa;
+  to.cl_pb = from.cl_pb;
+  to.cl_ps = from.cl_ps;
+  to.cl_smem = from.cl_smem;
+  to.cl_tile0 = from.cl_tile0;
+  to.cl_row0 = from.cl_row0;
+  to.cl_pts = from.cl_pts;
+  to.cl_off = from.cl_off;
+  to.cf_maxchunks = from.cf_maxchunks;
+  to.cf_wa = from.cf_wa;
+  to.cf_wb = from.cf_wb;
+  to.cf_ws = from.cf_ws;
+  to.cf_pa = from.cf_pa;
+  to.cf_pb = from.cf_pb;
+  to.cf_ps = from.cf_ps;
+  to.cf_pts = from.cf_pts;
+  to.cf_off = from.cf_off;
+  to.st_pts = from.st_pts;
+  to.st_off = from.st_off;
+  for (int k = 0; k <= HostGrid::kBandRuns; ++k) to.st_rows[k] = from.st_rows[k];
+  to.sor_nlev = from.sor_nlev;
+  to.sor_nblev = from.sor_nblev;
+  to.sor_delta = from.sor_delta;
+  to.sor_pts = from.sor_pts;
+  to.sor_off = from.sor_off;
+  to.sor_bpts = from.sor_bpts;
+  to.sor_boff = from.sor_boff;
+}
+constexpr size_t kScheduleCacheEntries = 8;
+}  // namespace
+
+std::string attach_schedule(HostGrid &g) {
+  ScheduleCache &c = schedule_cache();
+  {
+    std::lock_guard<std::mutex> lock(c.m);
+    for (auto &e : c.entries)
+      if (e->nni == g.nni && e->nmu == g.nmu) {
+        copy_schedule(g, *e);
+        return "";
+      }
+  }
+  std::string msg = build_schedule(g);
+  if (!msg.empty()) return msg;
+  auto keep = std::make_shared<HostGrid>();
+  keep->nni = g.nni;
+  keep->nmu = g.nmu;
+  copy_schedule(*keep, g);
+  std::lock_guard<std::mutex> lock(c.m);
+  c.entries.push_back(std::move(keep));
+  if (c.entries.size() > kScheduleCacheEntries) c.entries.erase(c.entries.begin());
+  return "";
 }
 
 }  // namespace x2g
