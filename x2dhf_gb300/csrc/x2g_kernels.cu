@@ -1577,6 +1577,36 @@ __device__ double sum_partials(const double *partials, int K, int q, int nblocks
   return r;
 }
 
+// sum_partials of nq <= kMaxK slots at once, slot q of block b at
+// base[b * bstride + q * qstride]: the same sums in the same order, with one
+// pass over the partials and two block barriers for all of them; out[] in
+// shared memory, valid in every thread on return
+__device__ void sum_partials_multi(const double *base, int bstride, int qstride, int nq, int nblocks, double *out) {
+  __shared__ double sh[kThreads / 32][kMaxK];
+  double s[kMaxK];
+#pragma unroll
+  for (int q = 0; q < kMaxK; ++q) s[q] = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < kMaxK; ++q)
+      if (q < nq) s[q] += __ldcg(base + size_t(b) * bstride + size_t(q) * qstride);
+  }
+#pragma unroll
+  for (int q = 0; q < kMaxK; ++q) {
+    if (q >= nq) break;
+    double x = s[q];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5][q] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < nq) {
+    double t = 0.0;
+    for (int i = 0; i < kThreads / 32; ++i) t += sh[i][threadIdx.x];
+    out[threadIdx.x] = t;
+  }
+  __syncthreads();
+}
+
 template <int K>
 __device__ bool block_sum_finish(double (&v)[K], double *partials, double *out, int nout, unsigned *ticket) {
   __shared__ bool s_last;
@@ -1766,6 +1796,7 @@ __global__ void __launch_bounds__(kThreads) k_orthonormalise(GridDev g, const __
     double v[kGroup];
 #pragma unroll
     for (int j = 0; j < kGroup; ++j) v[j] = 0.0;
+#pragma unroll 4
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
       const int mu = k / g.nni, nu = k - mu * g.nni;
       const int ij = (mu + 4) * g.n8 + nu + 4;
@@ -1792,11 +1823,13 @@ __global__ void __launch_bounds__(kThreads) k_orthonormalise(GridDev g, const __
     int b = a;
     while (b < n && b - a < kGroup && (P.it[b].ihomo != 0) == (P.it[a].ihomo != 0)) ++b;
     double zarea[kGroup];
+    sum_partials_multi(partials + size_t(a) * nb, 1, nb, b - a, nb, s_val);
     for (int j = 0; j < b - a; ++j) {
-      const double norm = sum_partials(partials + size_t(a + j) * nb, 1, 0, nb);
+      const double norm = s_val[j];
       if (blockIdx.x == 0 && threadIdx.x == 0) *P.it[a + j].norm_out = norm;
       zarea[j] = D(1.0, sqrt(norm));
     }
+    __syncthreads();  // s_val is reused below
     scale_items(g, P, a, b, zarea);
     a = b;
   }
@@ -1854,12 +1887,16 @@ __global__ void __launch_bounds__(kThreads) k_orthonormalise(GridDev g, const __
       int nslot = 0, iend = i;
       while (iend < i1 && iend - i < kGroup && nslot + P.it[iend].n <= kMaxK) nslot += P.it[iend++].n;
       if (iend == i) break;
-      for (int x = i, t = 0; x < iend; ++x)
-        for (int q = 0; q < P.it[x].n; ++q, ++t) {
-          const double tot = sum_partials(partials + size_t(slot0) * nb, kMaxK, t, nb);
-          if (threadIdx.x == 0) s_val[(x - i) * kMaxK + q] = tot;
-          if (blockIdx.x == 0 && threadIdx.x == 0) P.it[x].ovl_out[q] = tot;
-        }
+      {
+        __shared__ double tot[kMaxK];
+        sum_partials_multi(partials + size_t(slot0) * nb, kMaxK, 1, nslot, nb, tot);
+        if (threadIdx.x == 0)
+          for (int x = i, t = 0; x < iend; ++x)
+            for (int q = 0; q < P.it[x].n; ++q, ++t) {
+              s_val[(x - i) * kMaxK + q] = tot[t];
+              if (blockIdx.x == 0) P.it[x].ovl_out[q] = tot[t];
+            }
+      }
       __syncthreads();
       {
         const int a = i, b = iend;
