@@ -662,6 +662,16 @@ def run_serve(args):
                 # or stagnation, 1: energy threshold, 2: norm threshold)
                 out[name]["per_request"] = [[q.template, q.nnu, q.nmu, round(q.r, 4), c.iterations, c.converged]
                                             for q, c in zip(reqs, done)]
+        # the mixed form at other arrival rates (the same seeded stream,
+        # arrival times scaled): throughput and latency against the load
+        sweep = []
+        for rate in [float(x) for x in args.rates.split(",") if x.strip()] if args.rates else []:
+            rq = serve.make_requests(templates, args.requests, rate=rate, seed=42)
+            srv = serve.Server(slots=args.slots, precision=xg.MIXED)
+            done, wall = srv.run(rq)
+            sm = serve.summary(done, wall)
+            sweep.append({"rate": rate, "solves_per_s": sm["solves_per_s"], "latency_p50_s": sm["latency_p50_s"],
+                          "latency_p99_s": sm["latency_p99_s"], "converged": sm["converged"]})
     de = max(abs(a - b) for a, b in zip(out["mixed_energies"], out["fp64_energies"]))
     both = [i for i, (a, b) in enumerate(zip(out["mixed_converged"], out["fp64_converged"])) if a and b]
     de_conv = max((abs(out["mixed_energies"][i] - out["fp64_energies"][i]) for i in both), default=None)
@@ -678,7 +688,8 @@ def run_serve(args):
                           "fp64_p50": f64["latency_p50_s"], "fp64_p99": f64["latency_p99_s"]},
             "mixed": mx, "fp64": f64, "mixed_tight_budget": out["mixed_tight_budget"],
             "max_dE_mixed_vs_fp64": de, "max_dE_mixed_vs_fp64_both_converged": de_conv,
-            "both_converged": len(both), "tight_budget_energies_identical": same, "clocks": sampler.summary()}
+            "both_converged": len(both), "tight_budget_energies_identical": same, "rate_sweep": sweep,
+            "clocks": sampler.summary()}
 
 
 def C_double_pair(xg, nnu, nmu):
@@ -937,6 +948,8 @@ def main():
     ap.add_argument("--requests", type=int, default=48, help="serve workload: requests in the stream")
     ap.add_argument("--rate", type=float, default=4.0, help="serve workload: mean arrivals per second")
     ap.add_argument("--slots", type=int, default=4, help="serve workload: concurrent solves")
+    ap.add_argument("--rates", default="", help="serve workload: comma-separated further arrival rates for the "
+                                                "mixed form (a load sweep)")
     ap.add_argument("--cpu-iters", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--legs", default="all", choices=["all"] + [lg[0] for lg in SCF_LEGS],
