@@ -64,3 +64,18 @@ def test_reference_solve_fixture_present():
     for name, grid in (("h2", [151, 241]), ("n2", [331, 481])):
         assert d[name]["grid"] == grid and d[name]["iterations"] > 100
         assert d[name]["total_energy"] < 0
+
+
+def test_sweeps_leg_deck_sets_maxsor():
+    """The 40-sweep leg rewrites the deck's mcsor / mcsor-ce cards only: the
+    MCSOR schemes stay and both sweep counts become 40; 0 keeps the deck."""
+    import bench
+    import x2dhf_gb300 as xg
+
+    deck = bench.n2_deck()
+    assert bench.deck_with_sweeps(deck, 0) == deck
+    c0, c40 = xg.parse_deck(deck), xg.parse_deck(bench.deck_with_sweeps(deck, 40))
+    assert (c0.maxsor_orb, c0.maxsor_pot) == (10, 10)
+    assert (c40.maxsor_orb, c40.maxsor_pot) == (40, 40)
+    assert (c40.orb_scheme, c40.pot_scheme) == (c0.orb_scheme, c0.pot_scheme) == (1, 1)
+    assert (c40.nnu, c40.nmu, c40.r) == (c0.nnu, c0.nmu, c0.r)
