@@ -500,6 +500,7 @@ def run_gpu(args):
                                      "potentials_variant_mode": args.potential_clusters},
             "colouring": args.colouring,
             "residual_overlap": args.residual_overlap,
+            "orthonormalise": args.orthonormalise,
             "fp64_kernel": {"kernel": "k_mcsor_f64", "achieved_gbs": sweep_gbs_64,
                             "frac_hbm": (sweep_gbs_64 / hbm) if sweep_gbs_64 else None,
                             "achieved_tflops": pts64 * FLOPS_PER_PT / (ms64 / 1e3) / 1e12 if ms64 > 0 else None,
@@ -935,6 +936,7 @@ def _configure(ctx, args):
     ctx.set_potential_clusters("auto" if mode == "auto" else mode == "on")
     ctx.set_mixed_colouring(getattr(args, "colouring", "reference"))
     ctx.set_residual_overlap(getattr(args, "residual_overlap", "on") == "on")
+    ctx.set_gram_orthonormalise(getattr(args, "orthonormalise", "rounds") == "gram")
 
 
 def main():
@@ -965,6 +967,8 @@ def main():
                          "(default: for batches above the plain kernel's co-resident clusters)")
     ap.add_argument("--residual-overlap", default="on", choices=["on", "off"],
                     help="mixed form: second-wave potentials' FP64 residual beside the first wave's sweep")
+    ap.add_argument("--orthonormalise", default="rounds", choices=["rounds", "gram"],
+                    help="batch mode 2: orthonormalisation in rounds (the loop's sums) or through the Gram matrix")
     ap.add_argument("--colouring", default="reference", choices=["reference", "free"],
                     help="mixed form: colouring of the on-chip cluster sweep")
     ap.add_argument("--window", default="", help="WARM,N: profile SCF iterations WARM+1..WARM+N of the headline form "

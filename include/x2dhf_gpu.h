@@ -164,6 +164,17 @@ int x2g_set_mixed_on_chip(x2g_ctx *ctx, int on);
  * mode 0 never, 1 always, 2 (default) for batches larger than the clusters
  * of the plain kernel co-resident on the device.  No reference counterpart. */
 int x2g_set_potential_clusters(x2g_ctx *ctx, int mode);
+/* Batch mode 2, no orbital frozen: the orthonormalisation of an SCF
+ * iteration (normOrtho.F90:14-59,103-207 for every orbital in the
+ * reference's order) as 0 (default) rounds of independent orbitals with the
+ * loop's own sums and operations (bit-identical to the orbital-by-orbital
+ * loop), or 1 its Gram-matrix form -- the norms and every inner product of
+ * the orbitals of a symmetry block in one pass, the coefficients of the
+ * final orbitals from them, one pass applying them: equal in exact
+ * arithmetic, faster, the rounding differs (so does the iteration at which
+ * an SCF near its noise floor meets the convergence test).  No reference
+ * counterpart. */
+int x2g_set_gram_orthonormalise(x2g_ctx *ctx, int on);
 /* Mixed form, potential batches larger than the co-resident clusters of
  * the potentials' cluster variant: 1 (default) the batch runs in waves of
  * that size and the FP64 residuals of the later waves run on the context's

@@ -372,6 +372,47 @@ def test_scf_kf_batched_trajectory_matches_oracle(batch_mode):
     _scf_records_match("kf_set01", 5, _kf_small, batch_mode=batch_mode)
 
 
+def test_gram_orthonormalise_matches_rounds():
+    """Batch mode 2 orthonormalises an iteration's orbitals in rounds with
+    the loop's own sums by default, or through their Gram matrix.  Equal in
+    exact arithmetic: N2 (331x481, mixed) solved both ways lands on the same
+    energies, and Ne in FP64 follows the same trajectory for 60 iterations
+    past its frozen-orbital start."""
+    import bench
+
+    ctx = xg.Context(0)
+    out = {}
+    for gram in (True, False):
+        ctx.set_gram_orthonormalise(gram)
+        s = xg.SCF(ctx, xg.parse_deck(bench.n2_deck(), precision=xg.MIXED, batch_mode=2))
+        r = s.run()
+        out[gram] = (r.iterations, r.total_energy, [r.ee[i] for i in range(6)])
+        s.close()
+    # each exits at its own iteration of the same converging trajectory: the
+    # energies agree to the exit's own accuracy, and both lie within the
+    # tolerance of the FP64 oracle solved to 1000 iterations
+    ref = golden_json("n2_331x481_oracle")["total_energy"]
+    for gram in (True, False):
+        assert abs(out[gram][1] - ref) < 1e-9, (gram, out[gram][1], ref)
+    assert abs(out[True][1] - out[False][1]) < 5e-10, out
+    assert max(abs(a - b) for a, b in zip(out[True][2], out[False][2])) < 5e-10, out
+    assert abs(out[True][0] - out[False][0]) <= 30, out
+    recs = {}
+    deck = _all_mcsor(golden_deck("ne_set01"))
+    for gram in (True, False):
+        ctx.set_gram_orthonormalise(gram)
+        s = xg.SCF(ctx, xg.parse_deck(deck, batch_mode=2))
+        s.run(80)
+        recs[gram] = s.records()
+        s.close()
+    ctx.set_gram_orthonormalise(False)
+    assert len(recs[True]) == len(recs[False]) > 0
+    for a, b in zip(recs[True], recs[False]):
+        assert a[:2] == b[:2]
+        assert abs(a[2] - b[2]) <= 1e-11 * max(1.0, abs(a[2])), (a, b)
+    ctx.close()
+
+
 def test_scf_he_converged_energy_vs_golden():
     """He MCSOR converged to 1e-12: the reference's own final energy."""
     deck = _all_mcsor(with_hydrogen0(golden_deck("he_set02")))

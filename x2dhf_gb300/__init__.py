@@ -75,7 +75,7 @@ EXPORTS = [
     "x2g_kernel_launches", "x2g_transfer_bytes", "mcsor_pthread_", "mcsor_tpool_", "coulExch_pthread_", "coulExch_tpool_",
     "tpoolStop4mcsor_", "tpoolStop4pots_", "x2g_host_table", "x2g_host_schedule", "x2g_profile",
     "x2g_relax_noalloc", "x2g_host_cluster_plan", "x2g_set_mixed_on_chip", "x2g_set_potential_clusters", "x2g_cluster_occupancy",
-    "x2g_set_mixed_colouring", "x2g_set_residual_overlap",
+    "x2g_set_mixed_colouring", "x2g_set_residual_overlap", "x2g_set_gram_orthonormalise",
     "x2g_host_cluster_chunks", "x2g_host_free_chunks", "x2g_host_band_schedule",
     "x2g_convert_selftest", "x2g_set_wait_limit", "x2g_host_sor_schedule",
 ]
@@ -139,6 +139,7 @@ def lib():
     L.x2g_set_potential_clusters.argtypes = [P, I]
     L.x2g_set_mixed_colouring.argtypes = [P, I]
     L.x2g_set_residual_overlap.argtypes = [P, I]
+    L.x2g_set_gram_orthonormalise.argtypes = [P, I]
     L.x2g_cluster_occupancy.argtypes = [P, P, C.POINTER(I), C.POINTER(I)]
     L.x2g_set_wait_limit.argtypes = [P, D]
     L.x2g_kernel_launches.restype = C.c_long
@@ -451,6 +452,13 @@ class Context:
         if colouring not in ("reference", "free"):
             raise ValueError("colouring must be 'reference' or 'free'")
         _check(self.L.x2g_set_mixed_colouring(self.h, 1 if colouring == "free" else 0))
+
+    def set_gram_orthonormalise(self, on):
+        """Batch mode 2: the orthonormalisation of an iteration in rounds
+        with the loop's own sums (False, the default: bit-identical to the
+        orbital-by-orbital loop) or through the orbitals' Gram matrix (True:
+        faster, equal in exact arithmetic)."""
+        _check(self.L.x2g_set_gram_orthonormalise(self.h, 1 if on else 0))
 
     def set_residual_overlap(self, on):
         """Potential batches beyond one wave of clusters: the later jobs' FP64

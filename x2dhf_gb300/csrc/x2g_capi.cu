@@ -216,6 +216,12 @@ int x2g_set_potential_clusters(x2g_ctx *c, int mode) {
   return X2G_OK;
 }
 
+int x2g_set_gram_orthonormalise(x2g_ctx *c, int on) {
+  if (!c || on < 0 || on > 1) return set_status(X2G_ERR_ARG, "on must be 0 or 1");
+  c->gram_ortho = on;
+  return X2G_OK;
+}
+
 int x2g_set_residual_overlap(x2g_ctx *c, int on) {
   if (!c || on < 0 || on > 1) return set_status(X2G_ERR_ARG, "on must be 0 or 1");
   c->residual_overlap = on;
@@ -345,6 +351,11 @@ int x2g_grid_create(x2g_ctx *ctx, int nnu, int nmu, double r, double rinf, doubl
   UP(h.g, g);
   UP(h.wgt1, wgt1);
   UP(h.wgt2, wgt2);
+  {
+    std::vector<double> wf(h.wgt2.size());
+    for (size_t k = 0; k < wf.size(); ++k) wf[k] = h.wgt2[k] * h.f4[k];
+    UP(wf, wf);
+  }
   UP(h.leg, leg);
   UP(h.dmu9, dmu9);
   UP(h.dni9, dni9);

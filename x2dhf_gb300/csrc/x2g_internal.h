@@ -111,6 +111,7 @@ struct GridDev {
   double dmu1[4], dmu2[4], dni1[4], dni2[4], exeven[5], diag;
   const double *borb_mu, *bpot_mu, *f3_mu, *d_nu;
   const double *e, *f0, *f1, *f2, *f4, *g, *wgt1, *wgt2, *leg;
+  const double *wf;  // wgt2 f4: the weight of the orbital inner products (Gram-matrix orthonormalisation)
   const double *dmu9, *dni9;
   const double *vxi, *vxisq, *veta, *vetasq;
   const int *tile_row0, *tile_row1, *pts, *off, *pts_rc;
@@ -215,6 +216,8 @@ struct x2g_ctx {
   int f64_blocks = -1;          // co-resident blocks of the cooperative FP64 sweep on this device
   int sor_blocks = -1;          // co-resident blocks of the cooperative list-order SOR sweep
   int ortho_blocks = -1;        // co-resident blocks of the one-launch orthonormalisation
+  int gram_blocks = -1;         // co-resident blocks of its Gram-matrix form
+  int gram_ortho = 0;           // batch mode 2: orthonormalise in rounds (0) or through the Gram matrix (1)
   unsigned long long wait_limit_ns = x2g::kDefaultWaitLimitNs;  // device-side wait limit (x2g_set_wait_limit)
   // optional per-launch timing of the sweep kernels (CUDA events on stream)
   int profiling = 0;

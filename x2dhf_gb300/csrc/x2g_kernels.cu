@@ -1930,6 +1930,172 @@ __global__ void __launch_bounds__(kThreads) k_orthonormalise(GridDev g, const __
   }
 }
 
+// The same orthonormalisation through the inner products of the orbitals
+// (one pass over the points, one grid barrier, one pass applying the
+// result).  With Z_j the orbital after setCiOrb (homonuclear: the first half
+// of each row mirrored onto the second, the sign by g/u) and <a,b> = sum
+// wgt2 f4 a b, the loop "scale orbital j by 1/sqrt(<X_j,X_j>) (then setCiOrb),
+// then Gram-Schmidt against its partners Y_q" (normOrtho.F90:14-59,
+// 103-207) makes every final orbital a combination Y_j = sum_m C_jm Z_m of
+// the orbitals of its symmetry block, and the loop's overlaps are
+//   ovl_q = zarea_j sum_m C_qm <Z_j, Z_m>,
+// so C, the norms and the overlaps follow exactly from the Gram matrix, in
+// the reference's orbital order.  Equal to the loop in exact arithmetic; the
+// rounding differs (the loop's sums of the scaled, partly orthogonalised
+// orbitals become sums of products of inner products).
+constexpr int kGramOrbs = 16, kGramSlots = 64;
+struct GramPlan {
+  double *psi[kGramOrbs];
+  double *norm_out[kGramOrbs], *ovl_out[kGramOrbs];
+  int ihomo[kGramOrbs];               // 0 heteronuclear; +-1 setCiOrb parity
+  int npart[kGramOrbs];
+  signed char part[kGramOrbs][kGramOrbs];  // partners (plan indices, earlier in the order)
+  signed char slot_of[kGramOrbs][kGramOrbs];  // slot of <Z_a, Z_b> (a != b), of <X_a, X_a> (a == b)
+  signed char sa[kGramSlots], sb[kGramSlots];
+  int n, nslots, homo;
+};
+
+__global__ void __launch_bounds__(kThreads) k_orthonormalise_gram(GridDev g, const __grid_constant__ GramPlan P,
+                                                                  double *partials, BarrierDev bar) {
+  __shared__ double s_h[kGramSlots];
+  __shared__ double s_z[kGramOrbs];
+  __shared__ double s_c[kGramOrbs][kGramOrbs];
+  const int nb = int(gridDim.x), n = P.n, n2 = g.nni / 2 + 1;
+  // inner products, kMaxK slots per pass; the values are read where the
+  // slot needs them (L1 serves the repeats), so nothing is indexed at run
+  // time in registers
+  for (int s0 = 0; s0 < P.nslots; s0 += kMaxK) {
+    double v[kMaxK];
+#pragma unroll
+    for (int t = 0; t < kMaxK; ++t) v[t] = 0.0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < g.mxsize; k += gridDim.x * blockDim.x) {
+      const int mu = k / g.nni, nu = k - mu * g.nni;
+      const int row = (mu + 4) * g.n8 + 4;
+      // Z at this point: the orbital itself, or its mirrored first-half value
+      int src = nu, middle = 0, second = 0;
+      if (P.homo) {
+        if (nu > n2 - 1) {
+          src = g.nni - 1 - nu;
+          second = 1;
+        } else if (nu == n2 - 1) {
+          middle = 1;
+        }
+      }
+      const double w = g.wf[k];
+#pragma unroll
+      for (int t = 0; t < kMaxK; ++t) {
+        if (s0 + t >= P.nslots) break;
+        const int a = P.sa[s0 + t], b = P.sb[s0 + t];
+        double pr;
+        if (a == b) {
+          const double x = P.psi[a][row + nu];
+          pr = M(x, x);
+        } else {
+          double za = P.psi[a][row + src], zb = P.psi[b][row + src];
+          if (middle) {
+            za = (P.ihomo[a] == 1) ? za : 0.0;
+            zb = (P.ihomo[b] == 1) ? zb : 0.0;
+          } else if (second) {
+            za = (P.ihomo[a] == -1) ? -za : za;
+            zb = (P.ihomo[b] == -1) ? -zb : zb;
+          }
+          pr = M(za, zb);
+        }
+        v[t] = fma(w, pr, v[t]);
+      }
+    }
+    block_sum_store<kMaxK>(v, partials + size_t(s0) * nb);
+    __syncthreads();
+  }
+  __threadfence();
+  if (!grid_barrier(bar, unsigned(nb))) return;
+  // totals, one slot per warp at a time, in block order
+  {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int t = warp; t < P.nslots; t += kThreads / 32) {
+      const double *base = partials + size_t(t / kMaxK * kMaxK) * nb + (t % kMaxK);
+      double x = 0.0;
+      for (int b = lane; b < nb; b += 32) x += __ldcg(base + size_t(b) * kMaxK);
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+      if (lane == 0) s_h[t] = x;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < n) s_z[threadIdx.x] = D(1.0, sqrt(s_h[P.slot_of[threadIdx.x][threadIdx.x]]));
+  __syncthreads();
+  // the coefficients, in the reference's orbital order (every block alike)
+  if (threadIdx.x == 0) {
+    for (int j = 0; j < n; ++j)
+      for (int m = 0; m < n; ++m) s_c[j][m] = 0.0;
+    for (int j = 0; j < n; ++j) {
+      const double zarea = s_z[j];
+      double ovl[kGramOrbs];
+      double x = 0.0;
+      for (int p = 0; p < P.npart[j]; ++p) {
+        const int q = P.part[j][p];
+        double sum = 0.0;
+        for (int m = 0; m < n; ++m) {
+          const int sl = P.slot_of[j][m];
+          if (s_c[q][m] != 0.0 && sl >= 0) sum = A(sum, M(s_c[q][m], s_h[sl]));
+        }
+        ovl[p] = M(zarea, sum);
+        x = A(x, M(ovl[p], ovl[p]));
+      }
+      if (P.npart[j] == 0) {
+        s_c[j][j] = zarea;
+      } else {
+        const double ano = D(sqrt(A(1.0, x)), S(1.0, M(x, x)));
+        double row[kGramOrbs];
+        for (int m = 0; m < n; ++m) row[m] = (m == j) ? zarea : 0.0;
+        for (int p = 0; p < P.npart[j]; ++p) {
+          const int q = P.part[j][p];
+          for (int m = 0; m < n; ++m) row[m] = A(row[m], M(-ovl[p], s_c[q][m]));
+        }
+        for (int m = 0; m < n; ++m) s_c[j][m] = M(ano, row[m]);
+      }
+      if (blockIdx.x == 0) {
+        *P.norm_out[j] = s_h[P.slot_of[j][j]];
+        for (int p = 0; p < P.npart[j]; ++p) P.ovl_out[j][p] = ovl[p];
+      }
+    }
+  }
+  __syncthreads();
+  // Y = C Z, each thread owning its points (homonuclear: a first-half point
+  // and its mirror, read once, written both)
+  const int npts = P.homo ? n2 * g.nmu : g.mxsize;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < npts; k += gridDim.x * blockDim.x) {
+    int mu, nu;
+    if (P.homo) {
+      mu = k / n2;
+      nu = k - mu * n2;
+    } else {
+      mu = k / g.nni;
+      nu = k - mu * g.nni;
+    }
+    const int row = (mu + 4) * g.n8 + 4;
+    const bool middle = P.homo && nu == n2 - 1;
+    double z[kGramOrbs];
+#pragma unroll
+    for (int j = 0; j < kGramOrbs; ++j) {
+      if (j >= n) break;
+      const double x = __ldcg(P.psi[j] + row + nu);
+      z[j] = (middle && P.ihomo[j] != 1) ? 0.0 : x;
+    }
+#pragma unroll
+    for (int j = 0; j < kGramOrbs; ++j) {
+      if (j >= n) break;
+      double y = 0.0;
+#pragma unroll
+      for (int m = 0; m < kGramOrbs; ++m) {
+        if (m > j) break;
+        if (s_c[j][m] != 0.0) y = A(y, M(s_c[j][m], z[m]));
+      }
+      P.psi[j][row + nu] = y;
+      if (P.homo && !middle) P.psi[j][row + (g.nni - 1 - nu)] = (P.ihomo[j] == 1) ? y : -y;
+    }
+  }
+}
+
 // EaHF = oneelij(i,i) + (J + K): per point terms of integrals.F90:406-480
 // and lagrangeMultipliers.F90:67-72.  psi's ghost cells are read as the
 // mirrored interior values (identical to a putin ghost refresh); exact keeps
@@ -2773,6 +2939,83 @@ void launch_ortho_round(x2g_ctx *ctx, const GridDev &g, const OrthoOrbital *orbs
       ctx->launches += 2;
     }
   }
+}
+
+// the Gram-matrix form of one iteration's orthonormalisation; false: the
+// plan does not fit it (more orbitals or inner products than it holds, too
+// few co-resident blocks), the caller takes the round-by-round form
+bool launch_orthonormalise_gram(x2g_ctx *ctx, const GridDev &g, const OrthoOrbital *orbs, int n,
+                                const int *partner_index) {
+  if (n < 1 || n > kGramOrbs) return false;
+  GramPlan P{};
+  P.n = n;
+  P.homo = orbs[0].ihomo != 0;
+  for (int j = 0; j < n; ++j) {
+    P.psi[j] = orbs[j].psi;
+    P.norm_out[j] = orbs[j].norm_out;
+    P.ovl_out[j] = orbs[j].ovl_out;
+    P.ihomo[j] = orbs[j].ihomo;
+    if ((orbs[j].ihomo != 0) != (P.homo != 0)) return false;
+    P.npart[j] = orbs[j].n;
+    for (int p = 0; p < orbs[j].n; ++p) P.part[j][p] = (signed char)partner_index[j * kGramOrbs + p];
+    for (int m = 0; m < kGramOrbs; ++m) P.slot_of[j][m] = -1;
+  }
+  // slots: every norm, then <Z_a, Z_b> of every pair of a symmetry block
+  // (the orbitals a partner chain connects)
+  std::vector<int> blk(size_t(n), -1);
+  int nblk = 0;
+  for (int j = 0; j < n; ++j) {
+    if (blk[size_t(j)] < 0) blk[size_t(j)] = nblk++;
+    for (int p = 0; p < orbs[j].n; ++p) {
+      const int q = partner_index[j * kGramOrbs + p];
+      if (q < 0 || q >= j) return false;
+      if (blk[size_t(q)] != blk[size_t(j)]) {
+        const int from = blk[size_t(q)], to = blk[size_t(j)];
+        for (auto &b : blk)
+          if (b == from) b = to;
+      }
+    }
+  }
+  int ns = 0;
+  for (int j = 0; j < n; ++j) {
+    P.slot_of[j][j] = (signed char)ns;
+    P.sa[ns] = P.sb[ns] = (signed char)j;
+    ++ns;
+  }
+  for (int a = 0; a < n; ++a)
+    for (int b = a + 1; b < n; ++b)
+      if (blk[size_t(a)] == blk[size_t(b)]) {
+        if (ns >= kGramSlots) return false;
+        P.slot_of[a][b] = P.slot_of[b][a] = (signed char)ns;
+        P.sa[ns] = (signed char)a;
+        P.sb[ns] = (signed char)b;
+        ++ns;
+      }
+  P.nslots = ns;
+  if (ctx->gram_blocks < 0) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k_orthonormalise_gram, kThreads, 0) !=
+        cudaSuccess)
+      per_sm = 0;
+    (void)cudaGetLastError();
+    ctx->gram_blocks = per_sm * ctx->num_sms;
+  }
+  // two blocks per SM (the passes are latency bound), at most the partials' room
+  const int nb = std::min(std::min(2 * ctx->num_sms, ctx->gram_blocks), kRedBlocksMax);
+  if (nb < 1) return false;
+  double *part = reduction_partials(ctx, ((ns + kMaxK - 1) / kMaxK) * kMaxK);
+  if (!part) return false;
+  if (cudaMemsetAsync(ctx->bar, 0, 2 * sizeof(unsigned), ctx->stream) != cudaSuccess) return false;
+  BarrierDev bar{ctx->bar, ctx->bar + 1, reinterpret_cast<int *>(ctx->bar + 2), ctx->wait_limit_ns};
+  GridDev gd = g;
+  void *args[] = {&gd, &P, &part, &bar};
+  if (cudaLaunchCooperativeKernel((const void *)k_orthonormalise_gram, dim3(nb), dim3(kThreads), args, 0,
+                                  ctx->stream) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  ctx->launches += 1;
+  return true;
 }
 
 // every round in one cooperative launch; false: the plan does not fit it

@@ -117,6 +117,12 @@ void launch_ortho_round(x2g_ctx *ctx, const GridDev &g, const OrthoOrbital *orbs
 // round_off[r+1])); false: not launched, take launch_ortho_round per round
 bool launch_orthonormalise(x2g_ctx *ctx, const GridDev &g, const OrthoOrbital *orbs, const int *round_off,
                            int nrounds);
+// the same through the orbitals' inner products (one reduction pass, one
+// grid barrier, one update pass), orbs in the reference's order with
+// partner_index[j * 16 + p] the plan index of orbs[j].partners[p]; false:
+// not launched
+bool launch_orthonormalise_gram(x2g_ctx *ctx, const GridDev &g, const OrthoOrbital *orbs, int n,
+                                const int *partner_index);
 // EaHF of several orbitals in one launch (same sums, same order as launch_eahf)
 struct EahfItem {
   const double *psi, *coulp, *exchp;

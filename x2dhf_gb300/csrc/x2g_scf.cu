@@ -510,6 +510,26 @@ bool orthonormalise_in_rounds(x2g_scf *s) {
     for (int q : partners[iorb]) depth[iorb] = std::max(depth[iorb], depth[q] + 1);
     maxd = std::max(maxd, depth[iorb]);
   }
+  if (s->ctx->gram_ortho) {
+    // the Gram-matrix form, orbitals in the reference's order
+    std::vector<OrthoOrbital> w;
+    std::vector<int> index(norb + 1, -1), pidx;
+    for (int iorb = norb; iorb >= 1; iorb--) {
+      OrthoOrbital x{};
+      x.psi = s->orb[iorb];
+      x.n = int(partners[iorb].size());
+      for (int k = 0; k < x.n; k++) x.partners[k] = s->orb[partners[iorb][k]];
+      x.ihomo = s->cs.homonuclear ? s->ihomo[iorb] : 0;
+      x.norm_out = s->sc + x2g_scf::O_NORM + iorb;
+      x.ovl_out = s->sc + x2g_scf::O_OVL + 64 * iorb;
+      index[iorb] = int(w.size());
+      w.push_back(x);
+    }
+    pidx.assign(w.size() * 16, -1);
+    for (int iorb = norb; iorb >= 1; iorb--)
+      for (size_t k = 0; k < partners[iorb].size(); k++) pidx[size_t(index[iorb]) * 16 + k] = index[partners[iorb][k]];
+    if (launch_orthonormalise_gram(s->ctx, s->grid->d, w.data(), int(w.size()), pidx.data())) return true;
+  }
   std::vector<OrthoOrbital> v;
   std::vector<int> off(1, 0);
   for (int r = 0; r <= maxd; r++) {
