@@ -2518,13 +2518,17 @@ static int relax_batch(x2g_ctx *ctx, const GridDev &g, JobTable &jt, int njobs, 
     // waves of the potentials' cluster variant: the first wave's FP64
     // residual, then the later waves' residuals on the low-priority
     // auxiliary stream, beside the sweeps (on the SMs they leave free);
-    // each sweep waits for its own wave's residual
+    // each sweep waits for its own wave's residual.  The short wave (the
+    // remainder) goes first: its residual is the only one on the critical
+    // path, the full waves' residuals run beside sweeps
     const int nw = (njobs + wave - 1) / wave;
     std::vector<JobTable> w(size_t(nw), JobTable{});
+    std::vector<int> sz(size_t(nw), wave);
+    if (njobs % wave) sz[0] = njobs % wave;
     const unsigned nblk = unsigned(grid_blocks((g.nni - 2) * (g.nmu - 5)));
-    for (int c = 0; c < nw; ++c)
-      for (int i = c * wave; i < njobs && i < (c + 1) * wave; ++i) w[c].j[i - c * wave] = jt.j[i];
-    auto size = [&](int c) { return std::min(njobs, (c + 1) * wave) - c * wave; };
+    for (int c = 0, i0 = 0; c < nw; i0 += sz[size_t(c)], ++c)
+      for (int i = 0; i < sz[size_t(c)]; ++i) w[size_t(c)].j[i] = jt.j[i0 + i];
+    auto size = [&](int c) { return sz[size_t(c)]; };
     k_residual<false><<<dim3(nblk, size(0)), kThreads, 0, ctx->stream>>>(g, w[0], 0, 0);
     ctx->launches += 1;
     if ((err = cudaEventRecord(ctx->ev_split[0], ctx->stream)) != cudaSuccess ||
