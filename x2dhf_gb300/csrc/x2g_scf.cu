@@ -48,7 +48,7 @@ struct x2g_scf {
   // scalar block offsets (doubles)
   enum { O_EE = 0, O_NORM = 64, O_OVL = 128, O_CM = 128 + 64 * 64, O_EX = O_CM + 64 * 8 };
   size_t sc_count = 0;
-  std::vector<double> hsc;
+  double *hsc = nullptr;  // pinned host copy of the first O_CM scalars
   std::vector<std::vector<PotSlot>> pots;
   // exchange-moment list (initLP:1592-1626)
   std::vector<int> mm_i1, mm_i2, mm_idel, mm_ipc;
@@ -755,11 +755,13 @@ int etotal(x2g_scf *s) {
   return X2G_OK;
 }
 
+// the energies, norms and overlap rows of the iteration (orbitals 0..norb),
+// into pinned memory
 int read_scalars(x2g_scf *s) {
-  cudaError_t e = cudaMemcpyAsync(s->hsc.data(), s->sc, size_t(x2g_scf::O_CM) * sizeof(double),
-                                  cudaMemcpyDeviceToHost, s->ctx->stream);
+  const size_t n = size_t(x2g_scf::O_OVL) + 64 * size_t(s->norb + 1);
+  cudaError_t e = cudaMemcpyAsync(s->hsc, s->sc, n * sizeof(double), cudaMemcpyDeviceToHost, s->ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "scalar readback");
-  count_copy(s->ctx, 0, size_t(x2g_scf::O_CM) * sizeof(double));
+  count_copy(s->ctx, 0, n * sizeof(double));
   int rc = x2g_synchronize(s->ctx);
   if (rc) return rc;
   for (int i = 1; i <= s->norb; i++) {
@@ -1013,6 +1015,7 @@ int x2g_scf_destroy(x2g_scf *s) {
   if (!s) return X2G_OK;
   if (s->ctx) cudaStreamSynchronize(s->ctx->stream);
   for (void *p : s->allocs) cudaFree(p);
+  if (s->hsc) cudaFreeHost(s->hsc);
   if (s->grid) x2g_grid_destroy(s->grid);
   delete s;
   return X2G_OK;
@@ -1115,7 +1118,11 @@ int x2g_scf_create(x2g_ctx *ctx, const x2g_case *c, x2g_scf **out) {
   s->nslots = norb * (norb + 1) + 2;
   s->sc_count = size_t(x2g_scf::O_EX) + 8 * size_t(s->nslots) + 2048;
   ok &= (s->sc = dalloc(s, s->sc_count)) != nullptr;
-  s->hsc.assign(s->sc_count, 0.0);
+  if (cudaHostAlloc(reinterpret_cast<void **>(&s->hsc), size_t(x2g_scf::O_CM) * sizeof(double),
+                    cudaHostAllocDefault) == cudaSuccess)
+    std::fill(s->hsc, s->hsc + x2g_scf::O_CM, 0.0);
+  else
+    ok = false;
   if (!ok) {
     x2g_scf_destroy(s);
     return set_status(X2G_ERR_ALLOC, "device allocation failed");
