@@ -96,7 +96,8 @@ int x2g_create(x2g_ctx **out, int device) {
     return cuda_status(e, "auxiliary stream");
   }
   if ((e = cudaMalloc(&c->bar, kBarWords * sizeof(unsigned))) != cudaSuccess ||
-      (e = cudaMemset(c->bar, 0, kBarWords * sizeof(unsigned))) != cudaSuccess) {
+      (e = cudaMemsetAsync(c->bar, 0, kBarWords * sizeof(unsigned), c->stream)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(c->stream)) != cudaSuccess) {
     cudaStreamDestroy(c->stream);
     cudaStreamDestroy(c->aux);
     cudaEventDestroy(c->ev_split[0]);
@@ -154,11 +155,12 @@ int x2g_synchronize(x2g_ctx *c) {
   }
   c->pending.clear();
   int err = 0;
-  e = cudaMemcpy(&err, c->bar + 2, sizeof(int), cudaMemcpyDeviceToHost);
+  e = cudaMemcpyAsync(&err, c->bar + 2, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_status(e, "error word readback");
   count_copy(c, 0, sizeof(int));
   if (err) {
-    cudaMemset(c->bar, 0, kBarWords * sizeof(unsigned));
+    cudaMemsetAsync(c->bar, 0, kBarWords * sizeof(unsigned), c->stream);
     return set_status(err, "device-side barrier wait timed out (kernel returned early)");
   }
   return X2G_OK;
@@ -268,7 +270,12 @@ static int upload(x2g_grid *gr, const void *src, size_t bytes, const void **dst)
   cudaError_t e = cudaMalloc(&p, bytes < 16 ? 16 : bytes);
   if (e != cudaSuccess) return cuda_status(e, "grid table allocation");
   gr->allocs.push_back(p);
-  e = cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
+  // on the context's stream, whose kernels read the table (a legacy-stream
+  // copy from pageable memory may return before its DMA lands, and the
+  // non-blocking stream is not ordered after it); synchronised because src
+  // may be freed on return
+  e = cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, gr->ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(gr->ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "grid table upload");
   count_copy(gr->ctx, bytes, 0);
   *dst = p;

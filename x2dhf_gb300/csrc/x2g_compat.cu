@@ -100,9 +100,11 @@ apply_common : {
     bpot[i] = sup[i4[1] - 1 + i * nni];
   }
   for (int j = 0; j < nni; j++) dnu[j] = sup[i4[2] - 1 + nni + j];
-  cudaMemcpy(const_cast<double *>(d.borb_mu), borb.data(), nmu * sizeof(double), cudaMemcpyHostToDevice);
-  cudaMemcpy(const_cast<double *>(d.bpot_mu), bpot.data(), nmu * sizeof(double), cudaMemcpyHostToDevice);
-  cudaMemcpy(const_cast<double *>(d.d_nu), dnu.data(), nni * sizeof(double), cudaMemcpyHostToDevice);
+  cudaStream_t st = g_ctx->stream;
+  cudaMemcpyAsync(const_cast<double *>(d.borb_mu), borb.data(), nmu * sizeof(double), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(const_cast<double *>(d.bpot_mu), bpot.data(), nmu * sizeof(double), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(const_cast<double *>(d.d_nu), dnu.data(), nni * sizeof(double), cudaMemcpyHostToDevice, st);
+  cudaStreamSynchronize(st);  // the host vectors are freed on return
   count_copy(g_ctx, (2 * size_t(nmu) + nni) * sizeof(double), 0);
 }
   return X2G_OK;

@@ -71,7 +71,9 @@ extern "C" int x2g_relax_noalloc(x2g_ctx *ctx, x2g_grid *grid, const x2g_job *jo
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "stream synchronize");
   int err = 0;
-  e = cudaMemcpy(&err, static_cast<char *>(scratch) + 2 * sizeof(unsigned), sizeof(int), cudaMemcpyDeviceToHost);
+  e = cudaMemcpyAsync(&err, static_cast<char *>(scratch) + 2 * sizeof(unsigned), sizeof(int), cudaMemcpyDeviceToHost,
+                      ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "scratch error word readback");
   count_copy(ctx, 0, sizeof(int));
   if (err) return set_status(err, "device-side barrier wait timed out (kernel returned early)");

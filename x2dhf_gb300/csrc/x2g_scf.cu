@@ -74,7 +74,9 @@ namespace {
 double *dalloc(x2g_scf *s, size_t n) {
   void *p = nullptr;
   if (cudaMalloc(&p, n * sizeof(double)) != cudaSuccess) return nullptr;
-  cudaMemset(p, 0, n * sizeof(double));
+  // on the context's stream: its kernels are not ordered after the legacy
+  // default stream (the stream is non-blocking)
+  cudaMemsetAsync(p, 0, n * sizeof(double), s->ctx->stream);
   s->allocs.push_back(p);
   return static_cast<double *>(p);
 }
@@ -247,7 +249,9 @@ int upload_ext(x2g_scf *s, double *dst, const std::vector<double> &plain) {
   std::vector<double> ext(g.next, 0.0);
   for (int i = 0; i < g.nmu; i++)
     for (int j = 0; j < g.nni; j++) ext[(i + 4) * g.n8 + j + 4] = plain[i * g.nni + j];
-  cudaError_t e = cudaMemcpy(dst, ext.data(), ext.size() * sizeof(double), cudaMemcpyHostToDevice);
+  cudaError_t e =
+      cudaMemcpyAsync(dst, ext.data(), ext.size() * sizeof(double), cudaMemcpyHostToDevice, s->ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->ctx->stream);  // ext is freed on return
   count_copy(s->ctx, ext.size() * sizeof(double), 0);
   return e == cudaSuccess ? X2G_OK : cuda_status(e, "function upload");
 }
@@ -1304,7 +1308,8 @@ int x2g_scf_set_start_values(x2g_scf *s, const double *ee, const double *orbnorm
   int rc = x2g_synchronize(s->ctx);
   if (rc) return rc;
   std::vector<double> h(s->sc_count);
-  cudaError_t e = cudaMemcpy(h.data(), s->sc, h.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaError_t e = cudaMemcpyAsync(h.data(), s->sc, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s->ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "start values");
   const int norb = s->norb;
   for (int i = 1; i <= norb; i++) {
@@ -1314,7 +1319,8 @@ int x2g_scf_set_start_values(x2g_scf *s, const double *ee, const double *orbnorm
   }
   for (int ipc = 1; ipc < s->nslots && size_t(ipc) <= kExcLen; ipc++)
     for (int k = 1; k <= 8; k++) h[x2g_scf::O_EX + 8 * size_t(ipc) + (k - 1)] = exc[(k - 1) * kExcLen + ipc - 1];
-  e = cudaMemcpy(s->sc, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice);
+  e = cudaMemcpyAsync(s->sc, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, s->ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->ctx->stream);  // h is freed on return
   count_copy(s->ctx, h.size() * sizeof(double), h.size() * sizeof(double));
   return e == cudaSuccess ? X2G_OK : cuda_status(e, "start values");
 }
@@ -1325,7 +1331,8 @@ int x2g_scf_get_start_values(x2g_scf *s, double *ee, double *orbnorm, double *cm
   int rc = x2g_synchronize(s->ctx);
   if (rc) return rc;
   std::vector<double> h(s->sc_count);
-  cudaError_t e = cudaMemcpy(h.data(), s->sc, h.size() * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaError_t e = cudaMemcpyAsync(h.data(), s->sc, h.size() * sizeof(double), cudaMemcpyDeviceToHost, s->ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "start values");
   count_copy(s->ctx, 0, h.size() * sizeof(double));
   const int norb = s->norb;
