@@ -67,7 +67,9 @@ const char *x2g_last_error(void);
 /* ------------------------------------------------------------------ */
 /* context                                                            */
 /* ------------------------------------------------------------------ */
-/* Create a context on CUDA device `device` with its own non-blocking stream. */
+/* Create a context on CUDA device `device` with its own non-blocking stream
+ * (highest priority; not ordered after the legacy default stream: device
+ * inputs written on other streams must be complete before a call). */
 int x2g_create(x2g_ctx **ctx, int device);
 int x2g_destroy(x2g_ctx *ctx);
 /* Wait for all work queued on the context's stream. */
