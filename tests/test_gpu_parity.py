@@ -113,6 +113,7 @@ def test_mixed_relaxation_tracks_fp64(ctx):
     dev = torch.device("cuda:0")
     u = torch.tensor(uext, device=dev)
     dl, dr = torch.tensor(lhs, device=dev), torch.tensor(rhs, device=dev)
+    torch.cuda.synchronize()  # the context's stream is not ordered after torch's
     xg.relax(ctx, g, [xg.Job(u=u.data_ptr(), lhs=dl.data_ptr(), rhs=dr.data_ptr(), omega=omega, isym=1, kind=0)],
              10, xg.MIXED)
     ctx.synchronize()
@@ -142,6 +143,7 @@ def test_mixed_on_chip_matches_persistent_band_path(ctx, name):
     for on_chip in (True, False):
         ctx.set_mixed_on_chip(on_chip)
         u = torch.tensor(uext, device=dev)
+        torch.cuda.synchronize()
         xg.relax(ctx, g, [xg.Job(u=u.data_ptr(), lhs=dl.data_ptr(), rhs=dr.data_ptr(), omega=omega, isym=isym,
                                  kind=0)], 10, xg.MIXED)
         ctx.synchronize()
@@ -544,6 +546,7 @@ def test_mixed_persistent_sweep_batches_track_fp64():
             us.append(u)
             jobs.append(xg.Job(u=u.data_ptr(), psa=ua.data_ptr(), psb=ub.data_ptr(), omega=1.95,
                                isym=1 if idel % 2 == 0 else -1, idel=idel, kind=1))
+        torch.cuda.synchronize()
         xg.relax(ctx, g, jobs, 10, prec)
         ctx.synchronize()
         out[prec] = [u.cpu().numpy() for u in us]
