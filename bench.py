@@ -263,11 +263,10 @@ def max_over_ranks(values, world, device):
 # the N2 workload's full oracle solve (FP64, reference order), written by
 # tests/golden/make_oracle_solves.py: the |dE| of every form against it
 ORACLE_SOLVES = {"n2": os.path.join(ROOT, "tests", "golden", "n2_331x481_oracle.json")}
-# SCF forms timed by the GPU arm: (name, precision, batch mode); the last is
-# the headline `value` (the benchmark spec's batched mixed form)
-# (name, precision 0 FP64 / 1 mixed, batch mode, MCSOR sweeps per relaxation:
-# 0 the deck's own, else the mcsor card's maxsor for orbitals and potentials);
-# the last leg is the headline
+# SCF forms timed by the GPU arm: (name, precision 0 FP64 / 1 mixed, batch
+# mode, MCSOR sweeps per relaxation: 0 the deck's own, else the mcsor card's
+# maxsor for orbitals and potentials); the last leg, the batched mixed form,
+# is the headline `value`
 SCF_LEGS = (("fp64", 0, 0, 0), ("fp64_batched", 0, 2, 0), ("mixed_reference_order", 1, 0, 0),
             ("mixed_sweeps40", 1, 2, 40), ("mixed", 1, 2, 0))
 # workloads that run the sweeps40 leg (a few-second full solve each)
