@@ -659,9 +659,9 @@ def run_serve(args):
             out[name + "_converged"] = [c.converged for c in done]
             if name == "mixed":
                 # every request: template, grid, bond length, SCF iterations, exit (0: the iteration cap
-                # or stagnation, 1: energy threshold, 2: norm threshold)
+                # or stagnation, 1: energy threshold, 2: norm threshold), and the error of a failed one
                 out[name]["per_request"] = [[q.template, q.nnu, q.nmu, round(q.r, 4), c.iterations, c.converged]
-                                            for q, c in zip(reqs, done)]
+                                            + ([c.error] if c.error else []) for q, c in zip(reqs, done)]
         # the mixed form at other arrival rates (the same seeded stream,
         # arrival times scaled): throughput and latency against the load
         sweep = []
@@ -672,7 +672,9 @@ def run_serve(args):
             sm = serve.summary(done, wall)
             sweep.append({"rate": rate, "solves_per_s": sm["solves_per_s"], "latency_p50_s": sm["latency_p50_s"],
                           "latency_p99_s": sm["latency_p99_s"], "converged": sm["converged"]})
-    de = max(abs(a - b) for a, b in zip(out["mixed_energies"], out["fp64_energies"]))
+    # failed requests (recorded with NaN energies and their error) are left out
+    de = max((abs(a - b) for a, b in zip(out["mixed_energies"], out["fp64_energies"]) if a == a and b == b),
+             default=None)
     both = [i for i, (a, b) in enumerate(zip(out["mixed_converged"], out["fp64_converged"])) if a and b]
     de_conv = max((abs(out["mixed_energies"][i] - out["fp64_energies"][i]) for i in both), default=None)
     same = out["mixed_energies"] == out["mixed_tight_budget_energies"]

@@ -74,3 +74,36 @@ def test_arrivals_are_honoured():
     done, wall = serve.Server(slots=2, backend=FakeBackend()).run(reqs)
     for q, c in zip(reqs, done):
         assert c.start >= q.arrival - 1e-6 and c.latency >= c.end - c.start
+
+
+class FailingBackend(FakeBackend):
+    """FakeBackend whose every fifth request fails the way a library call
+    reports a NaN."""
+
+    def solve(self, h, q):
+        if q.rid % 5 == 2:
+            raise xg.X2GError(5, "NaN in orbital energy")
+        return super().solve(h, q)
+
+
+def test_failed_requests_are_recorded_and_serving_continues():
+    reqs = serve.make_requests(TEMPLATES, 20, rate=0.0, seed=9)
+    done, wall = serve.Server(slots=3, backend=FailingBackend()).run(reqs, realtime=False)
+    assert [c.rid for c in done] == [q.rid for q in reqs]
+    for c in done:
+        if c.rid % 5 == 2:
+            assert "NaN" in c.error and not c.converged and c.total_energy != c.total_energy
+        else:
+            assert not c.error and c.iterations == 10 + c.rid
+    s = serve.summary(done, wall)
+    assert s["failed"] == 4 and s["converged"] == 16 and s["unconverged"] == 0
+
+
+def test_other_errors_stop_the_run():
+    class Broken(FakeBackend):
+        def solve(self, h, q):
+            raise RuntimeError("backend bug")
+
+    with pytest.raises(RuntimeError):
+        serve.Server(slots=2, backend=Broken()).run(serve.make_requests(TEMPLATES, 4, rate=0.0, seed=1),
+                                                   realtime=False)

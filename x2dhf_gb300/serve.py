@@ -32,7 +32,7 @@ import time
 
 import numpy as np
 
-from . import MIXED, SCF, Context, parse_deck, round_grid
+from . import MIXED, SCF, Context, X2GError, parse_deck, round_grid
 
 # cards of the template decks that the served solve does not use
 _DROP = ("mmoments", "conv", "stop", "omega", "altsweeps", "lagra", "!", "grid", "scf", "mcsor", "title")
@@ -62,6 +62,7 @@ class Completed:
     converged: int
     total_energy: float
     orbital_energies: tuple
+    error: str = ""         # the library's message when the solve failed
 
     @property
     def latency(self):
@@ -162,7 +163,10 @@ class Server:
     def run(self, requests, realtime=True):
         """Serve the requests (sorted by arrival); with realtime=False every
         request is taken to have arrived at time 0.  Returns the completions
-        in request order and the run's wall time."""
+        in request order and the run's wall time.  A solve that fails with a
+        library status (X2GError) completes with that error and NaN energies
+        and its slot goes on serving; any other exception stops the run and
+        is raised."""
         reqs = sorted(requests, key=lambda q: (q.arrival, q.rid))
         self.peak_bytes = 0
         self.budget_waits = 0
@@ -218,10 +222,16 @@ class Server:
                     if q is None:
                         return
                     start = clock()
+                    arrival = q.arrival if realtime else 0.0
                     try:
                         it, conv, etot, ee = self.backend.solve(ctx, q)
-                        done[q.rid] = Completed(q.rid, q.template, q.arrival if realtime else 0.0, start, clock(),
-                                                it, conv, etot, ee)
+                        done[q.rid] = Completed(q.rid, q.template, arrival, start, clock(), it, conv, etot, ee)
+                    except X2GError as e:
+                        # the request failed (a NaN, a device wait limit):
+                        # recorded, and the slot serves the next one
+                        nan = float("nan")
+                        done[q.rid] = Completed(q.rid, q.template, arrival, start, clock(), 0, 0, nan,
+                                                (nan,) * q.norb, error=str(e))
                     except Exception as e:
                         with lock:
                             errors.append(e)
@@ -254,5 +264,6 @@ def summary(completed, wall):
             "converged": sum(1 for c in completed if c.converged),
             "converged_energy": sum(1 for c in completed if c.converged == 1),
             "converged_norm": sum(1 for c in completed if c.converged == 2),
-            "unconverged": sum(1 for c in completed if not c.converged),
+            "unconverged": sum(1 for c in completed if not c.converged and not c.error),
+            "failed": sum(1 for c in completed if c.error),
             "converged_solves_per_s": sum(1 for c in completed if c.converged) / wall}
